@@ -1,0 +1,490 @@
+#!/usr/bin/env python
+"""Benchmark: conv applies/s on the 64^3 / 30 A / mmax 3 / mrso 2 workload.
+
+One step = one convolution round trip of the excess-functional term, the
+stages of Solver::energy_cproj_mrso between the density and the excess
+potential (src/mini-mdft.hpp:152-170):
+
+    angl2proj(delta_rho -> p)  ->  Convolution::execute(p)  ->  proj2angl(p -> vexc)
+
+in the plain FP64 form (``value``), with delta_rho (N, ntheta, nphi, npsi)
+resident in HBM.  ``e2e`` is the same step through the C ABI with host
+buffers: pinned delta_rho copied in and vexc copied out inside the timed
+region.  The mixed (FP32) form is timed the same way and reported under
+``mixed``.  Inputs are the seeded synthetic fields of
+mini_mdft_gb300/inputs.py.  L2 is flushed (a 256 MiB write) between timed
+steps, outside the per-step CUDA-event windows.
+
+``--impl reference`` times the CPU restatement of the same round trip (the
+reference's Kokkos/kokkos-fft build is unavailable; see oracle/build.py) on
+all host cores.
+
+Multi-GPU (torchrun): the path does not shard; each rank runs an independent
+replica of the workload and ``value`` is the sum over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(n=(64, 64, 64), box=(30.0, 30.0, 30.0), mmax=3, mrso=2, dq=0.01)
+METRIC = "conv applies/s @64^3 mmax3"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def sizes():
+    from mini_mdft_gb300 import inputs as I
+    nt, nphi, npsi, no, np_ = I.angular_counts(WORKLOAD["mmax"], WORKLOAD["mrso"])
+    n = WORKLOAD["n"]
+    N = n[0] * n[1] * n[2]
+    return dict(N=N, ntheta=nt, nphi=nphi, npsi=npsi, no=no, np=np_,
+                np_new=I.np_new_count(WORKLOAD["mmax"], WORKLOAD["mrso"]))
+
+
+def algorithmic_bytes(s, real_bytes):
+    """Per-stage algorithmic bytes: each stage reads its input once and
+    writes its output once (c(q) table and maps excluded: L2-resident)."""
+    N, no, np_ = s["N"], s["no"], s["np"]
+    cb = 2 * real_bytes
+    return {
+        "angl2proj": N * (real_bytes * no + cb * np_),
+        "fft_axis": N * np_ * cb * 2,         # one axis pass: read + write p
+        "oz": N * np_ * cb * 2,
+        "proj2angl": N * (cb * np_ + real_bytes * no),
+        "round_trip": N * (2 * real_bytes * no + 8 * cb * np_),
+    }
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling while the GPU is under load."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                rows.append(dict(sm=float(parts[0]), smax=float(parts[1]),
+                                 power=float(parts[2]) if parts[2] not in ("[N/A]", "N/A") else None,
+                                 hw=parts[4], hwt=parts[5], swt=parts[6], swp=parts[7]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        smax = max(r["smax"] for r in rows)
+        loaded = [r for r in rows if r["power"] is None or r["power"] > 200.0] or rows
+        reasons = set()
+        for r in loaded:
+            if r["hw"] == "Active":
+                reasons.add("hw_slowdown")
+            if r["hwt"] == "Active":
+                reasons.add("hw_thermal_slowdown")
+            if r["swt"] == "Active":
+                reasons.add("sw_thermal_slowdown")
+            if r["swp"] == "Active":
+                reasons.add("sw_power_cap")
+        return {"sm_mhz": statistics.median(r["sm"] for r in loaded), "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(rows), "samples_under_load": len(loaded)}
+
+
+def make_problem(prec):
+    import numpy as np
+    import torch
+
+    import mini_mdft_gb300 as M
+    from mini_mdft_gb300 import inputs as I
+    n, box, mmax, mrso, dq = (WORKLOAD[k] for k in ("n", "box", "mmax", "mrso", "dq"))
+    nq = I.nq_for(n, box, dq)
+    idx, tab = I.synthetic_cq(mmax, mrso, nq, dq)
+    sg, ag = M.SpatialGrid(n, box), M.AngularGrid(mmax, mrso)
+    opt = M.OrientationProjectionTransform(sg, ag, M.OrientationProjectionMap(ag), precision=prec)
+    conv = M.Convolution.from_table(idx, tab, dq, sg, ag, precision=prec)
+    N = n[0] * n[1] * n[2]
+    rd, cd = (torch.float64, torch.complex128) if prec == "f64" else (torch.float32, torch.complex64)
+    dr_host = I.synthetic_delta_rho(N, mmax, mrso)
+    dr = torch.from_numpy(dr_host).to("cuda", dtype=rd)
+    p = torch.zeros((ag.m_np,) + tuple(n), dtype=cd, device="cuda")
+    vexc = torch.zeros_like(dr)
+    return dict(opt=opt, conv=conv, dr=dr, p=p, vexc=vexc, dr_host=dr_host, ag=ag, rd=rd, cd=cd)
+
+
+def step(P):
+    P["opt"].angl2proj(P["dr"], P["p"])
+    P["conv"].execute(P["p"])
+    P["opt"].proj2angl(P["p"], P["vexc"])
+
+
+def timed_steps(P, K, flush):
+    """Per-step CUDA events on the launching (current) stream; L2 flushed
+    between steps outside the event windows.  Returns total seconds."""
+    import torch
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    for k in range(K):
+        flush.zero_()
+        starts[k].record()
+        step(P)
+        ends[k].record()
+    torch.cuda.synchronize()
+    return sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / 1e3
+
+
+def stage_times(P, reps, flush):
+    """Average device time of each stage, for the roofline of the dominant
+    kernel (events on the launching stream)."""
+    import torch
+    res = {}
+    stages = {
+        "angl2proj": lambda: P["opt"].angl2proj(P["dr"], P["p"]),
+        "fft_forward": lambda: P["conv"].fft(P["p"], -1),
+        "oz": lambda: P["conv"].kspace(P["p"]),
+        "fft_backward": lambda: P["conv"].fft(P["p"], +1),
+        "proj2angl": lambda: P["opt"].proj2angl(P["p"], P["vexc"]),
+    }
+    for name, fn in stages.items():
+        tot = 0.0
+        for _ in range(reps):
+            flush.zero_()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            tot += a.elapsed_time(b) / 1e3
+        res[name] = tot / reps
+    return res
+
+
+def e2e_steps(P, K, warm):
+    """Same step through the public API with host buffers: pinned H2D of
+    delta_rho, the round trip, D2H of vexc, all inside the timed region."""
+    import torch
+    h_in = torch.from_numpy(P["dr_host"]).to(P["rd"]).pin_memory()
+    h_out = torch.empty(P["vexc"].shape, dtype=P["rd"]).pin_memory()
+    for _ in range(warm):
+        P["dr"].copy_(h_in, non_blocking=True)
+        step(P)
+        h_out.copy_(P["vexc"], non_blocking=True)
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(K):
+        P["dr"].copy_(h_in, non_blocking=True)
+        step(P)
+        h_out.copy_(P["vexc"], non_blocking=True)
+    b.record()
+    torch.cuda.synchronize()
+    secs = a.elapsed_time(b) / 1e3
+    nbytes = h_in.numel() * h_in.element_size()
+    return secs, nbytes, h_out.numel() * h_out.element_size()
+
+
+def fp64_peak_tflops():
+    """cuBLAS DGEMM throughput (4096^3), the FP64 roof of this GPU."""
+    import torch
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e9
+    for _ in range(3):
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.matmul(a, b)
+        e.record()
+        torch.cuda.synchronize()
+        best = min(best, s.elapsed_time(e) / 1e3)
+    return 2.0 * n ** 3 / best / 1e12
+
+
+def stage_flops(s):
+    """Algorithmic FP64 flops per stage launch (counts of the arithmetic in
+    each kernel's inner loops; 5 n log2 n per complex FFT of length n)."""
+    import math
+    N, nt, nphi, npsi, np_ = s["N"], s["ntheta"], s["nphi"], s["npsi"], s["np"]
+    K1 = (npsi - 1) // 2 + 1
+    mmax = WORKLOAD["mmax"]
+    from mini_mdft_gb300 import inputs as I
+    ms = [m for m in range(mmax + 1) for _ in range(-m, m + 1) for _ in range(m // WORKLOAD["mrso"] + 1)]
+    srot = sum(2 * m + 1 for m in ms)
+    nrec = sum(2 * l * l + 2 * l + 1 for l in range(2, mmax + 1))
+    a2p = N * (nt * nphi * K1 * (npsi * 2) + nt * nphi * K1 * nphi * 8 + np_ * nt * 4)
+    npairs = N // 2 + 4
+    oz = npairs * (4 * srot * 8 + s["np_new"] * 22 + nrec * 20)
+    n = WORKLOAD["n"][0]
+    fft_axis = N * np_ // n * 5 * n * math.log2(n)
+    return {"angl2proj": a2p, "proj2angl": a2p, "oz": oz, "fft_axis": fft_axis}
+
+
+def cpu_round_trip_rate(seconds_target=12.0, max_reps=20):
+    """The oracle's round trip on this host's cores: (applies/s, reps, cores)."""
+    import numpy as np
+
+    import oracle as O
+    from mini_mdft_gb300 import inputs as I
+    n, box, mmax, mrso, dq = (WORKLOAD[k] for k in ("n", "box", "mmax", "mrso", "dq"))
+    cores = os.cpu_count() or 1
+    o = O.Oracle(n, box, mmax, mrso, threads=cores)
+    nq = o.nq_for_dq(dq)
+    idx, tab = I.synthetic_cq(mmax, mrso, nq, dq)
+    o.set_luc(idx, tab, dq)
+    dr = I.synthetic_delta_rho(o.N, mmax, mrso)
+    o.proj2angl(o.conv_execute(o.angl2proj(dr)))  # warm (page-in, thread pool)
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        o.proj2angl(o.conv_execute(o.angl2proj(dr)))
+        reps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds_target or reps >= max_reps:
+            break
+    return reps / el, reps, cores, el
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle as O
+    import numpy as np
+    from mini_mdft_gb300 import inputs as I
+    n, box, mmax, mrso, dq = (WORKLOAD[k] for k in ("n", "box", "mmax", "mrso", "dq"))
+    cores = os.cpu_count() or 1
+    o = O.Oracle(n, box, mmax, mrso, threads=cores)
+    nq = o.nq_for_dq(dq)
+    idx, tab = I.synthetic_cq(mmax, mrso, nq, dq)
+    o.set_luc(idx, tab, dq)
+    dr = I.synthetic_delta_rho(o.N, mmax, mrso)
+    for _ in range(args.warmup):
+        o.proj2angl(o.conv_execute(o.angl2proj(dr)))
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.proj2angl(o.conv_execute(o.angl2proj(dr)))
+    el = time.perf_counter() - t0
+    v = args.steps / el
+    out = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "applies/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "64^3 grid, box 30 A, mmax 3, mrso 2, FP64 round trip "
+                               "angl2proj+Convolution::execute+proj2angl"},
+        "cpu_baseline": {"value": v, "unit": "applies/s", "cores": cores, "kind": "port",
+                         "sample": "%d full 64^3 round trips (CPU restatement, OpenMP; the "
+                                   "Kokkos reference cannot be built: Kokkos/kokkos-fft absent)"
+                                   % args.steps},
+        "e2e": {"value": v, "unit": "applies/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    ws, rank, local = dist_env()
+    dist = ws > 1
+    if dist:
+        import torch.distributed as tdist
+        torch.cuda.set_device(local)
+        tdist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.cuda.current_device()
+    import mini_mdft_gb300 as M
+    M.lib()
+    s = sizes()
+    K, W = args.steps, args.warmup
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    P = make_problem("f64")
+    clocks = ClockSampler(dev)
+    clocks.start()
+    for _ in range(W):
+        step(P)
+    torch.cuda.synchronize()
+    if dist:
+        tdist.barrier()
+    torch.cuda.synchronize()
+    secs = timed_steps(P, K, flush)
+    torch.cuda.synchronize()
+    if dist:
+        tdist.barrier()
+        t = torch.tensor([secs], dtype=torch.float64, device="cuda")
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        secs = float(t.item())
+    value = ws * K / secs
+
+    # mixed (FP32) form, same protocol
+    Pm = make_problem("f32")
+    for _ in range(W):
+        step(Pm)
+    torch.cuda.synchronize()
+    secs_m = timed_steps(Pm, K, flush)
+    # e2e through the C ABI with host buffers
+    e2e_secs, h2d, d2h = e2e_steps(P, K, max(1, W // 2))
+    clk = clocks.stop()
+
+    # stage timing for the roofline, error of the mixed form vs FP64
+    st = stage_times(P, 10, flush)
+    st_m = stage_times(Pm, 10, flush)
+    step(P)
+    step(Pm)
+    torch.cuda.synchronize()
+    v64 = P["vexc"].cpu().numpy()
+    v32 = Pm["vexc"].cpu().numpy().astype(np.float64)
+    mixed_err = float(np.abs(v32 - v64).max() / np.abs(v64).max())
+    from mini_mdft_gb300 import inputs as I
+    xi = I.synthetic_xi(s["N"], WORKLOAD["mmax"], WORKLOAD["mrso"])
+    rho0, pref = I.tip3p_constants(WORKLOAD["mrso"])
+    w = torch.from_numpy(M.AngularGrid(WORKLOAD["mmax"], WORKLOAD["mrso"]).m_w)
+    xt = torch.from_numpy(xi).cuda()
+    df = torch.zeros_like(xt)
+    ff64 = M.get_delta_f(xt, P["vexc"], w, df, rho0, pref)
+    xt32 = xt.float()
+    df32 = torch.zeros_like(xt32)
+    ff32 = M.get_delta_f(xt32, Pm["vexc"], w, df32, rho0, pref)
+    ff_err = abs(ff32 - ff64) / abs(ff64)
+
+    ab = algorithmic_bytes(s, 8)
+    per_launch = {
+        "angl2proj": (st["angl2proj"], ab["angl2proj"]),
+        "fft_axis": ((st["fft_forward"] + st["fft_backward"]) / 6.0, ab["fft_axis"]),
+        "oz": (st["oz"], ab["oz"]),
+        "proj2angl": (st["proj2angl"], ab["proj2angl"]),
+    }
+    share = {"angl2proj": st["angl2proj"], "fft_axis": st["fft_forward"] + st["fft_backward"],
+             "oz": st["oz"], "proj2angl": st["proj2angl"]}
+    dom = max(share, key=share.get)
+    t_launch, b_launch = per_launch[dom]
+    peaks = {}
+    pk_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk_path):
+        peaks = json.load(open(pk_path))
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    achieved = b_launch / t_launch / 1e9
+    traffic = None
+    tr_path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tr_path):
+        traffic = json.load(open(tr_path)).get(dom)
+    fp64_peak = fp64_peak_tflops()
+    fl = stage_flops(s)
+    fl_launch = fl[dom]
+    kernels_per_step = 1 + 3 + 1 + 3 + 1
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "applies/s", "n_gpus": ws, "steps": K,
+        "warmup": W, "ms_per_step": secs / K * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {
+            "workload": "64^3 grid, box 30 A, mmax 3, mrso 2 (ntheta 4, nphi 7, npsi 3, np 28): "
+                        "angl2proj + Convolution::execute + proj2angl, FP64",
+            "parallelism": "replicas" if ws > 1 else "single GPU",
+            "l2": "flushed (256 MiB write) between timed steps, outside the event windows",
+            "inputs": "delta_rho ~ U[-0.1,0.1] seed 0; c(q) = a exp(-s q^2), a~N(0,1), "
+                      "s~U(0.5,4), seed 2, dq 0.01, nq %d" % __import__(
+                          "mini_mdft_gb300.inputs", fromlist=["x"]).nq_for(
+                          WORKLOAD["n"], WORKLOAD["box"], WORKLOAD["dq"]),
+        },
+        "e2e": {"value": ws * K / e2e_secs, "unit": "applies/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": kernels_per_step * K,
+        "clocks": clk,
+        "roofline": {
+            "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
+            "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
+            "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)",
+            "algorithmic_bytes_per_launch": b_launch, "launch_ms": t_launch * 1e3,
+            "fp64_pipe": {"achieved_tflops": fl_launch / t_launch / 1e12,
+                          "peak_tflops": fp64_peak, "frac": fl_launch / t_launch / 1e12 / fp64_peak,
+                          "peak_source": "measured cuBLAS DGEMM 4096^3 in this run"},
+        },
+        "stages_ms": {k: v * 1e3 for k, v in st.items()},
+        "round_trip_hbm_frac": ab["round_trip"] / (secs / K) / 1e9 / hbm_peak,
+        "mixed": {
+            "value": ws * K / secs_m, "unit": "applies/s", "dtype": "f32 (FP64 recursions, FP64 energy sum)",
+            "speedup_vs_f64": secs / secs_m,
+            "vexc_rel_err_vs_f64": mixed_err, "ff_rel_err_vs_f64": ff_err,
+            "stages_ms": {k: v * 1e3 for k, v in st_m.items()},
+            "round_trip_hbm_frac": algorithmic_bytes(s, 4)["round_trip"] / (secs_m / K) / 1e9 / hbm_peak,
+        },
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        rate, reps, cores, el = cpu_round_trip_rate()
+        out["cpu_baseline"] = {"value": rate, "unit": "applies/s", "cores": cores, "kind": "port",
+                               "sample": "%d full 64^3 FP64 round trips in %.1f s (CPU restatement, "
+                                         "OpenMP, all host threads)" % (reps, el)}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if dist:
+        tdist.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,154 @@
+/*
+ * mdft_gb300.h -- C ABI of the GB300 (sm_103a) implementation of Mini-MDFT's
+ * excess-functional convolution hot path.
+ *
+ * The entry points replace the reference's C++ operator templates one for
+ * one (paths relative to the Mini_MDFT project root):
+ *
+ *   SpatialGrid + AngularGrid           common/MDFT_Grid.hpp:184-238, :264-469
+ *   OrientationProjectionMap            common/MDFT_OrientationProjectionTransform.hpp:55-155
+ *   OrientationProjectionTransform      common/MDFT_OrientationProjectionTransform.hpp:217-484
+ *   Convolution                         common/MDFT_Convolution.hpp:106-548
+ *   IO::LucData (c(q) file reader)      common/IO/MDFT_ReadCLuc.hpp:40-260
+ *   get_delta_rho / get_delta_f         common/MDFT_Solvent.hpp:578-660
+ *
+ * Conventions
+ *   - Every array is row-major (Kokkos::LayoutRight).  Complex values are two
+ *     interleaved reals (re, im), the layout of Kokkos::complex<T>.
+ *   - Orientation fields o: (nx*ny*nz, ntheta, nphi, npsi) real.
+ *     Projections p: (np, nx, ny, nz) complex.
+ *   - Field pointers are DEVICE pointers on the current CUDA device.  Work is
+ *     enqueued on `stream` (a cudaStream_t; NULL = legacy default stream) and
+ *     returns without synchronising, like Kokkos kernels on a device
+ *     execution space; the caller fences (cudaStreamSynchronize).
+ *   - MDFT_F64 handles take double / complex<double> fields (the reference's
+ *     ScalarType=double).  MDFT_F32 handles take float / complex<float> fields
+ *     (ScalarType=float): the mixed form, whose Wigner/rotation recursions and
+ *     grid-wide energy sum stay in FP64.
+ *   - No C++ exception crosses this boundary.  Functions return an
+ *     mdft_status; mdft_last_error() gives the message of the calling
+ *     thread's last failure (the text the reference's Throw_If would raise,
+ *     common/MDFT_Asserts.hpp:15-28).
+ *   - A handle is not re-entrant: two calls on one handle must not overlap on
+ *     the GPU (the reference's OPT shares one o_hat buffer between calls,
+ *     common/MDFT_OrientationProjectionTransform.hpp:208-209).
+ */
+#ifndef MDFT_GB300_H
+#define MDFT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MDFT_GB300_ABI_VERSION 1
+
+typedef enum {
+  MDFT_OK = 0,
+  MDFT_ERR_INVALID = 1,     /* bad argument / shape (reference: Throw_If) */
+  MDFT_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+  MDFT_ERR_IO = 3,          /* c(q) file missing or malformed */
+  MDFT_ERR_UNSUPPORTED = 4, /* size outside what the kernels handle */
+  MDFT_ERR_NOMEM = 5        /* device allocation failed */
+} mdft_status;
+
+typedef enum { MDFT_F64 = 0, MDFT_F32 = 1 } mdft_precision;
+
+typedef struct mdft_grid_s* mdft_grid_t;
+typedef struct mdft_opt_s* mdft_opt_t;
+typedef struct mdft_conv_s* mdft_conv_t;
+
+int mdft_abi_version(void);
+const char* mdft_last_error(void);
+
+/* ---- grids --------------------------------------------------------------
+ * SpatialGrid(n_nodes, length) and AngularGrid(mmax, molrotsymorder) in one
+ * handle (common/MDFT_Grid.hpp:184-220, :264-398).  Host-only, no GPU work.
+ * mmax in [1, 10]; n in [1, 4096] per axis. */
+int mdft_grid_create(mdft_grid_t* out, int nx, int ny, int nz, double lx,
+                     double ly, double lz, int mmax, int molrotsymorder);
+int mdft_grid_destroy(mdft_grid_t g);
+/* ints[0..10]: nx ny nz mmax mrso ntheta nphi npsi no np np_new */
+int mdft_grid_info(mdft_grid_t g, int* ints);
+/* kx,ky,kz (SpatialGrid::kproj, MDFT_Grid.hpp:222-238). */
+int mdft_grid_kvectors(mdft_grid_t g, double* kx, double* ky, double* kz);
+/* thetaofntheta, wthetaofntheta (ntheta) and w (no), MDFT_Grid.hpp:316-372. */
+int mdft_grid_angular(mdft_grid_t g, double* theta, double* wtheta, double* w);
+/* OrientationProjectionMap getters p(), m(), mup(), mu(), mu2(),
+ * wigner_small_d() (MDFT_OrientationProjectionTransform.hpp:150-155):
+ * p (mmax+1, 2mmax+1, mmax/mrso+1), the rest (np), wigner (ntheta, np). */
+int mdft_grid_opmap(mdft_grid_t g, int* p, int* m, int* mup, int* mu,
+                    int* mu2, double* wigner);
+
+/* ---- OrientationProjectionTransform ------------------------------------
+ * Constructor (MDFT_OrientationProjectionTransform.hpp:217-257): uploads the
+ * Wigner-d/quadrature tables to the current device. */
+int mdft_opt_create(mdft_opt_t* out, mdft_grid_t g, int precision);
+int mdft_opt_destroy(mdft_opt_t h);
+/* angl2proj(o, p), MDFT_OrientationProjectionTransform.hpp:270-380:
+ * real o -> complex p. */
+int mdft_opt_angl2proj(mdft_opt_t h, const void* o, void* p, void* stream);
+/* proj2angl(p, o), MDFT_OrientationProjectionTransform.hpp:391-484:
+ * complex p -> real o.  p is read only. */
+int mdft_opt_proj2angl(mdft_opt_t h, const void* p, void* o, void* stream);
+/* get_delta_rho fused into angl2proj's load: o = rho0 (xi^2 - 1) is formed
+ * in registers and never written (MDFT_Solvent.hpp:578-596 followed by
+ * MDFT_OrientationProjectionTransform.hpp:270-380). */
+int mdft_opt_angl2proj_from_xi(mdft_opt_t h, const void* xi, double rho0,
+                               void* p, void* stream);
+
+/* ---- Convolution --------------------------------------------------------
+ * Convolution(filename, grid, angular_grid, map, np_luc),
+ * MDFT_Convolution.hpp:106-313, from a c(q) table already in memory in the
+ * Luc layout: luc_index is 5 x np_luc ints (rows m, n, mu, nu, khi;
+ * ReadCLuc.hpp:88-103), luc is (np_luc, nq) complex double (host pointers),
+ * dq the q spacing.  nq must be at least int(q_max/dq + 0.5) + 2
+ * (ReadCLuc.hpp:65); extra rows are ignored as the reader ignores them.
+ * mmax <= 6 (RotationCoeffs, MDFT_Rotation.hpp:29). */
+int mdft_conv_create(mdft_conv_t* out, mdft_grid_t g, const int* luc_index,
+                     const double* luc, int np_luc, int nq, double dq,
+                     int precision);
+/* Same, reading the Luc text file (ReadCLuc.hpp:40-260). */
+int mdft_conv_create_from_file(mdft_conv_t* out, mdft_grid_t g,
+                               const char* path, int np_luc, int precision);
+int mdft_conv_destroy(mdft_conv_t h);
+/* execute(deltarho_p), MDFT_Convolution.hpp:326-548: in place on complex
+ * p (np, nx, ny, nz): forward 3-D FFT, per-(q,-q) rotation + OZ + rotation
+ * back, inverse 3-D FFT, all unnormalised as in the reference. */
+int mdft_conv_execute(mdft_conv_t h, void* p, void* stream);
+/* The two 3-D FFT passes of execute on their own (sign -1 forward,
+ * +1 backward; unnormalised), and the k-space step alone. */
+int mdft_conv_fft(mdft_conv_t h, void* p, int sign, void* stream);
+int mdft_conv_kspace(mdft_conv_t h, void* p, void* stream);
+/* Getters gamma_p_map() (npairs x 3 ints), dq(), and sizes
+ * (MDFT_Convolution.hpp:316-318). ints: npairs np_new nq */
+int mdft_conv_info(mdft_conv_t h, int* ints, double* dq);
+int mdft_conv_gamma_p_map(mdft_conv_t h, int* map);
+/* mnmunukhi_q() as (np_new, nq) complex double, host copy. */
+int mdft_conv_mnmunukhi_q(mdft_conv_t h, double* tab);
+
+/* ---- energy ---------------------------------------------------------------
+ * get_delta_rho(exec, xi, delta_rho, rho0), MDFT_Solvent.hpp:578-596:
+ * delta_rho[i] = rho0 (xi[i]^2 - 1) over n elements.  precision selects
+ * double or float arrays. */
+int mdft_get_delta_rho(const void* xi, void* delta_rho, size_t n, double rho0,
+                       int precision, void* stream);
+/* get_delta_f(exec, xi, vexc, w, delta_f, ff, rho0, prefactor),
+ * MDFT_Solvent.hpp:617-660: delta_f = 2 rho0 xi vexc and
+ * ff = sum_r rho0 prefactor sum_o vexc w (xi^2 - 1) over xi, vexc, delta_f
+ * of shape (nxyz, no) and w (no) (all device pointers, w always double).
+ * ff_dev is a device double; it is overwritten (the reference sets ff = 0
+ * first).  The sum over points is deterministic (fixed reduction tree with
+ * compensated partial sums).  Uses a stream-ordered temporary of
+ * 16 bytes per 128 points. */
+int mdft_get_delta_f(const void* xi, const void* vexc, const double* w,
+                     void* delta_f, double* ff_dev, size_t nxyz, int no,
+                     double rho0, double prefactor, int precision,
+                     void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MDFT_GB300_H */

@@ -1,0 +1,19 @@
+"""mini_mdft_gb300 -- GB300 (sm_103a) implementation of Mini-MDFT's
+excess-functional convolution hot path behind a C ABI
+(include/mdft_gb300.h), with a Python mirror of the reference's operator API.
+"""
+from . import inputs  # noqa: F401
+from .api import (  # noqa: F401
+    MDFT_F32,
+    MDFT_F64,
+    AngularGrid,
+    Convolution,
+    MdftError,
+    OrientationProjectionMap,
+    OrientationProjectionTransform,
+    SpatialGrid,
+    get_delta_f,
+    get_delta_rho,
+)
+from ._lib import LIB_PATH, lib  # noqa: F401
+

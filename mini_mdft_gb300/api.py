@@ -1,0 +1,320 @@
+"""Python mirror of the reference's operator API for the convolution hot path.
+
+Names, argument order and meaning follow the reference's C++ classes so the
+tests read like the reference's own unit tests:
+
+* ``SpatialGrid(n_nodes, length)``        -- common/MDFT_Grid.hpp:158-239
+* ``AngularGrid(mmax, molrotsymorder)``   -- common/MDFT_Grid.hpp:241-470
+* ``OrientationProjectionMap(ag)``        -- common/MDFT_OrientationProjectionTransform.hpp:20-156
+* ``OrientationProjectionTransform(sg, ag, map)`` with ``angl2proj(o, p)`` and
+  ``proj2angl(p, o)``                     -- :161-485
+* ``Convolution(filename, sg, ag, map, np_luc)`` with ``execute(p)``,
+  ``gamma_p_map()``, ``mnmunukhi_q()``, ``dq()`` -- common/MDFT_Convolution.hpp:20-549
+* ``get_delta_rho(xi, delta_rho, rho0)`` and
+  ``get_delta_f(xi, vexc, w, delta_f, rho0, prefactor) -> ff``
+                                           -- common/MDFT_Solvent.hpp:578-660
+
+Fields are torch CUDA tensors in the reference layouts (o: (N, ntheta, nphi,
+npsi) real; p: (np, nx, ny, nz) complex).  float64/complex128 selects the
+plain FP64 form, float32/complex64 the mixed form (the reference's
+ScalarType=float instantiation with FP64 recursions and energy sum).  Work
+goes to torch's current CUDA stream and is asynchronous, as Kokkos kernels
+are; errors raise ``MdftError`` (a RuntimeError, like Throw_If).
+Every call goes through the C ABI of ``libmdft_gb300.so``.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import MDFT_F32, MDFT_F64, MdftError, check, lib
+
+__all__ = [
+    "SpatialGrid", "AngularGrid", "OrientationProjectionMap",
+    "OrientationProjectionTransform", "Convolution", "get_delta_rho",
+    "get_delta_f", "MdftError", "MDFT_F64", "MDFT_F32",
+]
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _stream():
+    torch = _torch()
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _dptr(t):
+    return C.c_void_p(t.data_ptr())
+
+
+def _np_d(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _np_i(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+class _GridHandle:
+    def __init__(self, n, box, mmax, mrso):
+        h = C.c_void_p()
+        check(lib().mdft_grid_create(C.byref(h), int(n[0]), int(n[1]), int(n[2]),
+                                     float(box[0]), float(box[1]), float(box[2]),
+                                     int(mmax), int(mrso)))
+        self.h = h
+        v = np.zeros(11, np.int32)
+        check(lib().mdft_grid_info(h, _np_i(v)))
+        (self.nx, self.ny, self.nz, self.mmax, self.mrso, self.ntheta, self.nphi,
+         self.npsi, self.no, self.np, self.np_new) = [int(x) for x in v]
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib._lib is not None:
+            _lib._lib.mdft_grid_destroy(self.h)
+            self.h = None
+
+
+class SpatialGrid:
+    """SpatialGrid<ExecutionSpace, ScalarType>(n_nodes, length)."""
+
+    def __init__(self, n_nodes, length):
+        self.m_n_nodes = tuple(int(v) for v in n_nodes)
+        self.m_length = tuple(float(v) for v in length)
+        self.m_nx, self.m_ny, self.m_nz = self.m_n_nodes
+        self.m_lx, self.m_ly, self.m_lz = self.m_length
+        g = _GridHandle(self.m_n_nodes, self.m_length, 1, 1)
+        kx, ky, kz = np.zeros(self.m_nx), np.zeros(self.m_ny), np.zeros(self.m_nz)
+        check(lib().mdft_grid_kvectors(g.h, _np_d(kx), _np_d(ky), _np_d(kz)))
+        self.m_kx, self.m_ky, self.m_kz = kx, ky, kz
+        self.m_dl = tuple(l / n for l, n in zip(self.m_length, self.m_n_nodes))
+        self.m_v = float(np.prod(self.m_length))
+        self.m_dv = float(np.prod(self.m_dl))
+
+
+class AngularGrid:
+    """AngularGrid<ExecutionSpace, ScalarType>(mmax, molrotsymorder)."""
+
+    def __init__(self, mmax, molrotsymorder):
+        g = _GridHandle((1, 1, 1), (1.0, 1.0, 1.0), mmax, molrotsymorder)
+        self.m_mmax, self.m_molrotsymorder = g.mmax, g.mrso
+        self.m_ntheta, self.m_nphi, self.m_npsi = g.ntheta, g.nphi, g.npsi
+        self.m_no, self.m_np = g.no, g.np
+        th, wth, w = np.zeros(g.ntheta), np.zeros(g.ntheta), np.zeros(g.no)
+        check(lib().mdft_grid_angular(g.h, _np_d(th), _np_d(wth), _np_d(w)))
+        self.m_thetaofntheta, self.m_wthetaofntheta, self.m_w = th, wth, w
+        self.m_quadrature_norm = 8.0 * np.pi * np.pi
+
+
+class OrientationProjectionMap:
+    """OrientationProjectionMap(angular_grid) with its getters."""
+
+    def __init__(self, angular_grid):
+        ag = angular_grid
+        g = _GridHandle((1, 1, 1), (1.0, 1.0, 1.0), ag.m_mmax, ag.m_molrotsymorder)
+        K = g.mmax // g.mrso
+        self._p = np.zeros((g.mmax + 1, 2 * g.mmax + 1, K + 1), np.int32)
+        self._arr = [np.zeros(g.np, np.int32) for _ in range(4)]
+        self._wig = np.zeros((g.ntheta, g.np))
+        check(lib().mdft_grid_opmap(g.h, _np_i(self._p), *[_np_i(a) for a in self._arr],
+                                    _np_d(self._wig)))
+        self.angular_grid = ag
+
+    def p(self):
+        return self._p
+
+    def m(self):
+        return self._arr[0]
+
+    def mup(self):
+        return self._arr[1]
+
+    def mu(self):
+        return self._arr[2]
+
+    def mu2(self):
+        return self._arr[3]
+
+    def wigner_small_d(self):
+        return self._wig
+
+
+def _precision_of(dtype):
+    torch = _torch()
+    if dtype in (torch.float64, torch.complex128):
+        return MDFT_F64
+    if dtype in (torch.float32, torch.complex64):
+        return MDFT_F32
+    raise MdftError(1, "unsupported dtype %s" % dtype)
+
+
+def _check_field(t, shape_numel, dtypes, name):
+    torch = _torch()
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise MdftError(1, "%s must be a CUDA tensor" % name)
+    if t.dtype not in dtypes:
+        raise MdftError(1, "%s has dtype %s, expected one of %s" % (name, t.dtype, dtypes))
+    if not t.is_contiguous():
+        raise MdftError(1, "%s must be contiguous (LayoutRight)" % name)
+    if t.numel() != shape_numel:
+        raise MdftError(1, "%s has %d elements, expected %d" % (name, t.numel(), shape_numel))
+
+
+class OrientationProjectionTransform:
+    """OrientationProjectionTransform(spatial_grid, angular_grid, map).
+
+    ``precision`` is "f64" (plain form) or "f32" (mixed form); the dtype of
+    the tensors passed to angl2proj/proj2angl must match it."""
+
+    def __init__(self, spatial_grid, angular_grid, map=None, precision="f64"):
+        sg, ag = spatial_grid, angular_grid
+        self._g = _GridHandle(sg.m_n_nodes, sg.m_length, ag.m_mmax, ag.m_molrotsymorder)
+        self.precision = MDFT_F64 if precision in ("f64", MDFT_F64) else MDFT_F32
+        h = C.c_void_p()
+        check(lib().mdft_opt_create(C.byref(h), self._g.h, self.precision))
+        self.h = h
+        g = self._g
+        self.N = g.nx * g.ny * g.nz
+        self.ntheta, self.nphi, self.npsi, self.np, self.no = g.ntheta, g.nphi, g.npsi, g.np, g.no
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib._lib is not None:
+            _lib._lib.mdft_opt_destroy(self.h)
+            self.h = None
+
+    def _dtypes(self):
+        torch = _torch()
+        if self.precision == MDFT_F64:
+            return (torch.float64,), (torch.complex128,)
+        return (torch.float32,), (torch.complex64,)
+
+    def angl2proj(self, o, p):
+        rd, cd = self._dtypes()
+        _check_field(o, self.N * self.no, rd, "o")
+        _check_field(p, self.N * self.np, cd, "p")
+        check(lib().mdft_opt_angl2proj(self.h, _dptr(o), _dptr(p), _stream()))
+
+    def angl2proj_from_xi(self, xi, rho0, p):
+        """get_delta_rho fused into angl2proj (delta_rho never stored)."""
+        rd, cd = self._dtypes()
+        _check_field(xi, self.N * self.no, rd, "xi")
+        _check_field(p, self.N * self.np, cd, "p")
+        check(lib().mdft_opt_angl2proj_from_xi(self.h, _dptr(xi), float(rho0), _dptr(p), _stream()))
+
+    def proj2angl(self, p, o):
+        rd, cd = self._dtypes()
+        _check_field(o, self.N * self.no, rd, "o")
+        _check_field(p, self.N * self.np, cd, "p")
+        check(lib().mdft_opt_proj2angl(self.h, _dptr(p), _dptr(o), _stream()))
+
+
+class Convolution:
+    """Convolution(filename, spatial_grid, angular_grid, map, np_luc)."""
+
+    def __init__(self, filename, spatial_grid, angular_grid, map=None, np_luc=None,
+                 precision="f64", _table=None):
+        sg, ag = spatial_grid, angular_grid
+        self._g = _GridHandle(sg.m_n_nodes, sg.m_length, ag.m_mmax, ag.m_molrotsymorder)
+        self.precision = MDFT_F64 if precision in ("f64", MDFT_F64) else MDFT_F32
+        h = C.c_void_p()
+        if _table is not None:
+            idx, tab, dq = _table
+            idx = np.ascontiguousarray(idx, np.int32)
+            tab = np.ascontiguousarray(tab, np.complex128)
+            np_luc_, nq = tab.shape
+            check(lib().mdft_conv_create(C.byref(h), self._g.h, _np_i(idx),
+                                         tab.ctypes.data_as(C.POINTER(C.c_double)),
+                                         np_luc_, nq, float(dq), self.precision))
+        else:
+            check(lib().mdft_conv_create_from_file(C.byref(h), self._g.h,
+                                                   str(filename).encode(), int(np_luc),
+                                                   self.precision))
+        self.h = h
+        v = np.zeros(3, np.int32)
+        d = C.c_double()
+        check(lib().mdft_conv_info(h, _np_i(v), C.byref(d)))
+        self.npairs, self.np_new, self.nq = [int(x) for x in v]
+        self._dq = d.value
+        g = self._g
+        self.N = g.nx * g.ny * g.nz
+        self.np = g.np
+
+    @classmethod
+    def from_table(cls, luc_index, table, dq, spatial_grid, angular_grid, map=None,
+                   precision="f64"):
+        """Same operator from a c(q) table already in memory (Luc layout)."""
+        return cls(None, spatial_grid, angular_grid, map, None, precision,
+                   _table=(luc_index, table, dq))
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib._lib is not None:
+            _lib._lib.mdft_conv_destroy(self.h)
+            self.h = None
+
+    def _cdt(self):
+        torch = _torch()
+        return (torch.complex128,) if self.precision == MDFT_F64 else (torch.complex64,)
+
+    def execute(self, deltarho_p):
+        _check_field(deltarho_p, self.N * self.np, self._cdt(), "deltarho_p")
+        check(lib().mdft_conv_execute(self.h, _dptr(deltarho_p), _stream()))
+
+    def fft(self, p, sign):
+        _check_field(p, self.N * self.np, self._cdt(), "p")
+        check(lib().mdft_conv_fft(self.h, _dptr(p), int(sign), _stream()))
+
+    def kspace(self, p):
+        _check_field(p, self.N * self.np, self._cdt(), "p")
+        check(lib().mdft_conv_kspace(self.h, _dptr(p), _stream()))
+
+    def gamma_p_map(self):
+        m = np.zeros((self.npairs, 3), np.int32)
+        check(lib().mdft_conv_gamma_p_map(self.h, _np_i(m)))
+        return m
+
+    def mnmunukhi_q(self):
+        t = np.zeros((self.np_new, self.nq), np.complex128)
+        check(lib().mdft_conv_mnmunukhi_q(self.h, t.ctypes.data_as(C.POINTER(C.c_double))))
+        return t
+
+    def dq(self):
+        return self._dq
+
+
+def get_delta_rho(xi, delta_rho, rho0):
+    """delta_rho = rho0 (xi^2 - 1) (MDFT_Solvent.hpp:578-596)."""
+    torch = _torch()
+    if xi.numel() != delta_rho.numel():
+        raise MdftError(1, "size of delta_rho must be the same as the size of xi")
+    _check_field(xi, xi.numel(), (torch.float64, torch.float32), "xi")
+    _check_field(delta_rho, xi.numel(), (xi.dtype,), "delta_rho")
+    check(lib().mdft_get_delta_rho(_dptr(xi), _dptr(delta_rho), xi.numel(), float(rho0),
+                                   _precision_of(xi.dtype), _stream()))
+
+
+def get_delta_f(xi, vexc, w, delta_f, rho0, prefactor, ff_out=None):
+    """delta_f = 2 rho0 xi vexc; returns ff = sum rho0 prefactor vexc w (xi^2-1)
+    (MDFT_Solvent.hpp:617-660).  xi, vexc, delta_f are (nx, ny, nz, no) (or any
+    shape whose last axis is no); w is (no,).  Like the reference, which
+    returns ff through a host reference after a blocking reduction, this
+    synchronises and returns a Python float unless ``ff_out`` (a CUDA float64
+    tensor of one element) is given, in which case it stays asynchronous."""
+    torch = _torch()
+    no = int(w.numel())
+    if xi.shape != vexc.shape:
+        raise MdftError(1, "angular grid size of xi and vexc must be the same")
+    n = xi.numel()
+    if no <= 0 or n % no:
+        raise MdftError(1, "last axis of xi must be the orientation axis of w")
+    _check_field(xi, n, (torch.float64, torch.float32), "xi")
+    _check_field(vexc, n, (xi.dtype,), "vexc")
+    _check_field(delta_f, n, (xi.dtype,), "delta_f")
+    wd = w.to(device=xi.device, dtype=torch.float64).contiguous()
+    ff = ff_out if ff_out is not None else torch.zeros(1, dtype=torch.float64, device=xi.device)
+    check(lib().mdft_get_delta_f(_dptr(xi), _dptr(vexc), _dptr(wd), _dptr(delta_f), _dptr(ff),
+                                 n // no, no, float(rho0), float(prefactor),
+                                 _precision_of(xi.dtype), _stream()))
+    if ff_out is not None:
+        return ff_out
+    return float(ff.item())

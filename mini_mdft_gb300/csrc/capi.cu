@@ -1,0 +1,555 @@
+// capi.cu -- the extern "C" boundary declared in include/mdft_gb300.h.
+//
+// Handles own the host set-up (grids, maps, tables) and the device copies of
+// the tables; the hot-path stages are enqueued on the caller's stream.  No
+// exception leaves this file: every entry point returns an mdft_status and
+// records the message for mdft_last_error().
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/mdft_gb300.h"
+#include "common.cuh"
+
+using mdft::Cx;
+using mdft::DevBuf;
+using mdft::Error;
+using mdft::throw_if;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+template <typename F>
+int guarded(F&& f) {
+  try {
+    f();
+    return MDFT_OK;
+  } catch (const Error& e) {
+    g_last_error = e.what();
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    g_last_error = "host allocation failed";
+    return MDFT_ERR_NOMEM;
+  } catch (const std::exception& e) {
+    g_last_error = e.what();
+    return MDFT_ERR_INVALID;
+  } catch (...) {
+    g_last_error = "unknown error";
+    return MDFT_ERR_INVALID;
+  }
+}
+
+inline cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
+
+void check_prec(int precision) {
+  throw_if(precision != MDFT_F64 && precision != MDFT_F32, "precision must be MDFT_F64 or MDFT_F32");
+}
+
+constexpr long double kPiL = 3.141592653589793238462643383279502884L;
+
+// exp(-2 pi i t / n), t = 0..n-1, rounded from long double.
+template <typename T>
+std::vector<Cx<T>> twiddles(int n) {
+  std::vector<Cx<T>> tw(n > 0 ? n : 1);
+  for (int t = 0; t < n; ++t) {
+    const long double a = 2.0L * kPiL * (long double)t / (long double)n;
+    tw[t] = mdft::mkc<T>((T)std::cos(a), (T)-std::sin(a));
+  }
+  return tw;
+}
+
+template <typename T>
+std::vector<T> cast_vec(const std::vector<double>& v) {
+  return std::vector<T>(v.begin(), v.end());
+}
+
+}  // namespace
+
+struct mdft_grid_s {
+  mdft::Grid g;
+  explicit mdft_grid_s(const mdft::Grid& gg) : g(gg) {}
+};
+
+struct mdft_opt_s {
+  mdft::Grid g;
+  int prec;
+  int device;
+  DevBuf coef_a2p, coef_p2a, tw_phi, tw_psi, ip_m, ip_mup, ip_mu2, pmap;
+  mdft::AngPlan plan{};
+  explicit mdft_opt_s(const mdft::Grid& gg) : g(gg) {}
+};
+
+struct mdft_conv_s {
+  mdft::Grid g;
+  int prec;
+  int device;
+  int npairs = 0, nq = 0;
+  double dq = 0;
+  std::vector<int> pair_list;                 // reference order (getter)
+  std::vector<std::complex<double>> mnq;      // (np_new, nq) (getter)
+  DevBuf pairs, kx, ky, kz, rot, pmap, ip_m, ip_mup, ip_mu2, ia_map, ctab, tw_x, tw_y, tw_z;
+  mdft::OzPlan oz{};
+  mdft::FftAxis ax{}, ay{}, az{};
+  explicit mdft_conv_s(const mdft::Grid& gg) : g(gg) {}
+};
+
+namespace {
+
+template <typename T>
+void opt_build(mdft_opt_s* h) {
+  const mdft::Grid& g = h->g;
+  const int nt = g.ntheta, np = g.np;
+  std::vector<T> ca((size_t)nt * np), cp((size_t)nt * np);
+  const double inv = 1.0 / (double)(g.nphi * g.npsi);
+  for (int it = 0; it < nt; ++it)
+    for (int ip = 0; ip < np; ++ip) {
+      const double d = g.wigner[(size_t)it * np + ip];
+      const double f = g.fm[g.m[ip]];
+      ca[(size_t)it * np + ip] = (T)(d * g.wtheta[it] * f * inv);
+      cp[(size_t)it * np + ip] = (T)(d * f);
+    }
+  h->coef_a2p.upload(ca.data(), sizeof(T) * ca.size());
+  h->coef_p2a.upload(cp.data(), sizeof(T) * cp.size());
+  auto tp = twiddles<T>(g.nphi);
+  auto ts = twiddles<T>(g.npsi);
+  h->tw_phi.upload(tp.data(), sizeof(Cx<T>) * g.nphi);
+  h->tw_psi.upload(ts.data(), sizeof(Cx<T>) * g.npsi);
+  h->ip_m.upload(g.m.data(), sizeof(int) * np);
+  h->ip_mup.upload(g.mup.data(), sizeof(int) * np);
+  h->ip_mu2.upload(g.mu2.data(), sizeof(int) * np);
+  h->pmap.upload(g.p.data(), sizeof(int) * g.p.size());
+  mdft::AngPlan& P = h->plan;
+  P.N = g.N();
+  P.ntheta = g.ntheta;
+  P.nphi = g.nphi;
+  P.npsi = g.npsi;
+  P.K = g.K;
+  P.mmax = g.mmax;
+  P.mrso = g.mrso;
+  P.np = g.np;
+  P.no = g.no;
+  P.coef_a2p = h->coef_a2p.ptr;
+  P.coef_p2a = h->coef_p2a.ptr;
+  P.tw_phi = h->tw_phi.ptr;
+  P.tw_psi = h->tw_psi.ptr;
+  P.ip_m = h->ip_m.as<int>();
+  P.ip_mup = h->ip_mup.as<int>();
+  P.ip_mu2 = h->ip_mu2.as<int>();
+  P.pmap = h->pmap.as<int>();
+  mdft::ang_plan_finish<T>(P);
+}
+
+template <typename T>
+void fft_axis_build(mdft::FftAxis& a, DevBuf& twbuf, int n, long long S, long long ncols) {
+  throw_if(!mdft::fft_factor(n, a), "FFT length " + std::to_string(n) +
+                                        " has a prime factor above 13", MDFT_ERR_UNSUPPORTED);
+  a.S = S;
+  a.ncols = ncols;
+  auto tw = twiddles<T>(n);
+  twbuf.upload(tw.data(), sizeof(Cx<T>) * n);
+  a.tw = twbuf.ptr;
+  mdft::fft_axis_finish<T>(a);
+}
+
+template <typename T>
+void conv_build(mdft_conv_s* h, const mdft::LucTable& t) {
+  const mdft::Grid& g = h->g;
+  throw_if(g.mmax > mdft::kRotMmaxMax, "Convolution supports mmax <= 6 (RotationCoeffs)",
+           MDFT_ERR_UNSUPPORTED);
+  const int need = (int)(g.qmax() / t.dq + 0.5) + 2;
+  throw_if(t.nq < need, "c(q) table has " + std::to_string(t.nq) + " rows, the grid needs " +
+                            std::to_string(need));
+  h->nq = need;
+  h->dq = t.dq;
+  h->mnq = mdft::reorder_luc(g, t, need);
+  // device table transposed to (nq, np_new) so a pair's two rows are contiguous
+  std::vector<Cx<T>> ct((size_t)need * g.np_new);
+  for (int i = 0; i < g.np_new; ++i)
+    for (int iq = 0; iq < need; ++iq) {
+      const auto z = h->mnq[(size_t)i * need + iq];
+      ct[(size_t)iq * g.np_new + i] = mdft::mkc<T>((T)z.real(), (T)z.imag());
+    }
+  h->ctab.upload(ct.data(), sizeof(Cx<T>) * ct.size());
+  // pair list: reference order kept for the getter, device copy sorted by
+  // the linear index of q (each pair is independent; roles are unchanged)
+  h->pair_list = mdft::gamma_p_map(g.nx, g.ny, g.nz);
+  h->npairs = (int)(h->pair_list.size() / 3);
+  std::vector<int4> pr(h->npairs);
+  for (int i = 0; i < h->npairs; ++i)
+    pr[i] = make_int4(h->pair_list[3 * i], h->pair_list[3 * i + 1], h->pair_list[3 * i + 2], 0);
+  std::sort(pr.begin(), pr.end(), [&](const int4& a, const int4& b) {
+    const long long la = ((long long)a.x * g.ny + a.y) * g.nz + a.z;
+    const long long lb = ((long long)b.x * g.ny + b.y) * g.nz + b.z;
+    return la < lb;
+  });
+  h->pairs.upload(pr.data(), sizeof(int4) * pr.size());
+  h->kx.upload(g.kx.data(), sizeof(double) * g.nx);
+  h->ky.upload(g.ky.data(), sizeof(double) * g.ny);
+  h->kz.upload(g.kz.data(), sizeof(double) * g.nz);
+  mdft::RotationCoeffs rc;
+  std::vector<double> rot;
+  rot.insert(rot.end(), rc.a, rc.a + mdft::kRotL * mdft::kRotM * mdft::kRotM);
+  rot.insert(rot.end(), rc.b, rc.b + mdft::kRotL * mdft::kRotM * mdft::kRotM);
+  rot.insert(rot.end(), rc.c, rc.c + mdft::kRotL * mdft::kRotM);
+  rot.insert(rot.end(), rc.d, rc.d + mdft::kRotL * mdft::kRotM);
+  h->rot.upload(rot.data(), sizeof(double) * rot.size());
+  h->pmap.upload(g.p.data(), sizeof(int) * g.p.size());
+  h->ip_m.upload(g.m.data(), sizeof(int) * g.np);
+  h->ip_mup.upload(g.mup.data(), sizeof(int) * g.np);
+  h->ip_mu2.upload(g.mu2.data(), sizeof(int) * g.np);
+  h->ia_map.upload(g.ia_map.data(), sizeof(int) * g.ia_map.size());
+  mdft::OzPlan& O = h->oz;
+  O.nx = g.nx;
+  O.ny = g.ny;
+  O.nz = g.nz;
+  O.np = g.np;
+  O.mmax = g.mmax;
+  O.mrso = g.mrso;
+  O.K = g.K;
+  O.np_new = g.np_new;
+  O.nq = need;
+  O.npairs = h->npairs;
+  O.N = g.N();
+  O.dq = t.dq;
+  O.pairs = h->pairs.as<int4>();
+  O.kx = h->kx.as<double>();
+  O.ky = h->ky.as<double>();
+  O.kz = h->kz.as<double>();
+  O.rot = h->rot.as<double>();
+  O.pmap = h->pmap.as<int>();
+  O.ip_m = h->ip_m.as<int>();
+  O.ip_mup = h->ip_mup.as<int>();
+  O.ip_mu2 = h->ip_mu2.as<int>();
+  O.ia_map = h->ia_map.as<int>();
+  O.ctab = h->ctab.ptr;
+  mdft::oz_plan_finish<T>(O);
+  const long long N = g.N(), np = g.np;
+  fft_axis_build<T>(h->az, h->tw_z, g.nz, 1, np * g.nx * g.ny);
+  fft_axis_build<T>(h->ay, h->tw_y, g.ny, g.nz, np * g.nx * (long long)g.nz);
+  fft_axis_build<T>(h->ax, h->tw_x, g.nx, (long long)g.ny * g.nz, np * (long long)g.ny * g.nz);
+  (void)N;
+}
+
+template <typename T>
+void conv_fft(mdft_conv_s* h, void* p, int sign, cudaStream_t s) {
+  auto* d = static_cast<Cx<T>*>(p);
+  if (sign < 0) {
+    mdft::launch_fft_axis<T>(h->az, d, sign, s);
+    mdft::launch_fft_axis<T>(h->ay, d, sign, s);
+    mdft::launch_fft_axis<T>(h->ax, d, sign, s);
+  } else {
+    mdft::launch_fft_axis<T>(h->ax, d, sign, s);
+    mdft::launch_fft_axis<T>(h->ay, d, sign, s);
+    mdft::launch_fft_axis<T>(h->az, d, sign, s);
+  }
+}
+
+int current_device() {
+  int d = 0;
+  mdft::cuda_check(cudaGetDevice(&d), "cudaGetDevice");
+  return d;
+}
+
+void check_device(int dev) {
+  throw_if(current_device() != dev, "handle was created on another CUDA device");
+}
+
+// Stream-ordered scratch for the energy partials.
+struct Scratch {
+  void* p = nullptr;
+  cudaStream_t s;
+  Scratch(size_t bytes, cudaStream_t st) : s(st) {
+    cudaError_t e = cudaMallocAsync(&p, bytes, s);
+    if (e != cudaSuccess) throw Error(MDFT_ERR_NOMEM, std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
+  }
+  ~Scratch() {
+    if (p) cudaFreeAsync(p, s);
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+int mdft_abi_version(void) { return MDFT_GB300_ABI_VERSION; }
+
+const char* mdft_last_error(void) { return g_last_error.c_str(); }
+
+int mdft_grid_create(mdft_grid_t* out, int nx, int ny, int nz, double lx, double ly, double lz,
+                     int mmax, int molrotsymorder) {
+  return guarded([&] {
+    throw_if(!out, "out is NULL");
+    *out = nullptr;
+    mdft::Grid g(nx, ny, nz, lx, ly, lz, mmax, molrotsymorder);
+    *out = new mdft_grid_s(g);
+  });
+}
+
+int mdft_grid_destroy(mdft_grid_t g) {
+  delete g;
+  return MDFT_OK;
+}
+
+int mdft_grid_info(mdft_grid_t h, int* v) {
+  return guarded([&] {
+    throw_if(!h || !v, "NULL argument");
+    const mdft::Grid& g = h->g;
+    const int vals[11] = {g.nx, g.ny, g.nz, g.mmax, g.mrso, g.ntheta, g.nphi, g.npsi, g.no, g.np, g.np_new};
+    std::memcpy(v, vals, sizeof(vals));
+  });
+}
+
+int mdft_grid_kvectors(mdft_grid_t h, double* kx, double* ky, double* kz) {
+  return guarded([&] {
+    throw_if(!h || !kx || !ky || !kz, "NULL argument");
+    std::memcpy(kx, h->g.kx.data(), sizeof(double) * h->g.nx);
+    std::memcpy(ky, h->g.ky.data(), sizeof(double) * h->g.ny);
+    std::memcpy(kz, h->g.kz.data(), sizeof(double) * h->g.nz);
+  });
+}
+
+int mdft_grid_angular(mdft_grid_t h, double* theta, double* wtheta, double* w) {
+  return guarded([&] {
+    throw_if(!h || !theta || !wtheta || !w, "NULL argument");
+    std::memcpy(theta, h->g.theta.data(), sizeof(double) * h->g.ntheta);
+    std::memcpy(wtheta, h->g.wtheta.data(), sizeof(double) * h->g.ntheta);
+    std::memcpy(w, h->g.w.data(), sizeof(double) * h->g.no);
+  });
+}
+
+int mdft_grid_opmap(mdft_grid_t h, int* p, int* m, int* mup, int* mu, int* mu2, double* wigner) {
+  return guarded([&] {
+    throw_if(!h || !p || !m || !mup || !mu || !mu2 || !wigner, "NULL argument");
+    const mdft::Grid& g = h->g;
+    std::memcpy(p, g.p.data(), sizeof(int) * g.p.size());
+    std::memcpy(m, g.m.data(), sizeof(int) * g.np);
+    std::memcpy(mup, g.mup.data(), sizeof(int) * g.np);
+    std::memcpy(mu, g.mu.data(), sizeof(int) * g.np);
+    std::memcpy(mu2, g.mu2.data(), sizeof(int) * g.np);
+    std::memcpy(wigner, g.wigner.data(), sizeof(double) * g.wigner.size());
+  });
+}
+
+int mdft_opt_create(mdft_opt_t* out, mdft_grid_t g, int precision) {
+  return guarded([&] {
+    throw_if(!out || !g, "NULL argument");
+    *out = nullptr;
+    check_prec(precision);
+    auto h = std::make_unique<mdft_opt_s>(g->g);
+    h->prec = precision;
+    h->device = current_device();
+    if (precision == MDFT_F64)
+      opt_build<double>(h.get());
+    else
+      opt_build<float>(h.get());
+    *out = h.release();
+  });
+}
+
+int mdft_opt_destroy(mdft_opt_t h) {
+  delete h;
+  return MDFT_OK;
+}
+
+int mdft_opt_angl2proj(mdft_opt_t h, const void* o, void* p, void* stream) {
+  return guarded([&] {
+    throw_if(!h || !o || !p, "NULL argument");
+    check_device(h->device);
+    if (h->prec == MDFT_F64)
+      mdft::launch_angl2proj<double>(h->plan, static_cast<const double*>(o), static_cast<Cx<double>*>(p),
+                                     false, 0.0, as_stream(stream));
+    else
+      mdft::launch_angl2proj<float>(h->plan, static_cast<const float*>(o), static_cast<Cx<float>*>(p),
+                                    false, 0.0, as_stream(stream));
+  });
+}
+
+int mdft_opt_angl2proj_from_xi(mdft_opt_t h, const void* xi, double rho0, void* p, void* stream) {
+  return guarded([&] {
+    throw_if(!h || !xi || !p, "NULL argument");
+    check_device(h->device);
+    if (h->prec == MDFT_F64)
+      mdft::launch_angl2proj<double>(h->plan, static_cast<const double*>(xi), static_cast<Cx<double>*>(p),
+                                     true, rho0, as_stream(stream));
+    else
+      mdft::launch_angl2proj<float>(h->plan, static_cast<const float*>(xi), static_cast<Cx<float>*>(p),
+                                    true, rho0, as_stream(stream));
+  });
+}
+
+int mdft_opt_proj2angl(mdft_opt_t h, const void* p, void* o, void* stream) {
+  return guarded([&] {
+    throw_if(!h || !o || !p, "NULL argument");
+    check_device(h->device);
+    if (h->prec == MDFT_F64)
+      mdft::launch_proj2angl<double>(h->plan, static_cast<const Cx<double>*>(p), static_cast<double*>(o),
+                                     as_stream(stream));
+    else
+      mdft::launch_proj2angl<float>(h->plan, static_cast<const Cx<float>*>(p), static_cast<float*>(o),
+                                    as_stream(stream));
+  });
+}
+
+static int conv_create_impl(mdft_conv_t* out, mdft_grid_t g, const mdft::LucTable& t, int precision) {
+  return guarded([&] {
+    throw_if(!out || !g, "NULL argument");
+    *out = nullptr;
+    check_prec(precision);
+    auto h = std::make_unique<mdft_conv_s>(g->g);
+    h->prec = precision;
+    h->device = current_device();
+    if (precision == MDFT_F64)
+      conv_build<double>(h.get(), t);
+    else
+      conv_build<float>(h.get(), t);
+    *out = h.release();
+  });
+}
+
+int mdft_conv_create(mdft_conv_t* out, mdft_grid_t g, const int* luc_index, const double* luc,
+                     int np_luc, int nq, double dq, int precision) {
+  mdft::LucTable t;
+  int rc = guarded([&] {
+    throw_if(!luc_index || !luc, "NULL argument");
+    throw_if(np_luc <= 0 || nq <= 1 || !(dq > 0), "invalid c(q) table extents");
+    t.np_luc = np_luc;
+    t.nq = nq;
+    t.dq = dq;
+    t.index.assign(luc_index, luc_index + 5 * (size_t)np_luc);
+    t.tab.resize((size_t)np_luc * nq);
+    std::memcpy(t.tab.data(), luc, sizeof(double) * 2 * t.tab.size());
+  });
+  if (rc != MDFT_OK) {
+    if (out) *out = nullptr;
+    return rc;
+  }
+  return conv_create_impl(out, g, t, precision);
+}
+
+int mdft_conv_create_from_file(mdft_conv_t* out, mdft_grid_t g, const char* path, int np_luc,
+                               int precision) {
+  mdft::LucTable t;
+  int rc = guarded([&] {
+    throw_if(!path || !g, "NULL argument");
+    t = mdft::read_luc_file(path, np_luc, g->g.qmax());
+  });
+  if (rc != MDFT_OK) {
+    if (out) *out = nullptr;
+    return rc;
+  }
+  return conv_create_impl(out, g, t, precision);
+}
+
+int mdft_conv_destroy(mdft_conv_t h) {
+  delete h;
+  return MDFT_OK;
+}
+
+int mdft_conv_fft(mdft_conv_t h, void* p, int sign, void* stream) {
+  return guarded([&] {
+    throw_if(!h || !p, "NULL argument");
+    throw_if(sign != -1 && sign != 1, "sign must be -1 or +1");
+    check_device(h->device);
+    if (h->prec == MDFT_F64)
+      conv_fft<double>(h, p, sign, as_stream(stream));
+    else
+      conv_fft<float>(h, p, sign, as_stream(stream));
+  });
+}
+
+int mdft_conv_kspace(mdft_conv_t h, void* p, void* stream) {
+  return guarded([&] {
+    throw_if(!h || !p, "NULL argument");
+    check_device(h->device);
+    if (h->prec == MDFT_F64)
+      mdft::launch_oz<double>(h->oz, static_cast<Cx<double>*>(p), as_stream(stream));
+    else
+      mdft::launch_oz<float>(h->oz, static_cast<Cx<float>*>(p), as_stream(stream));
+  });
+}
+
+int mdft_conv_execute(mdft_conv_t h, void* p, void* stream) {
+  return guarded([&] {
+    throw_if(!h || !p, "NULL argument");
+    check_device(h->device);
+    cudaStream_t s = as_stream(stream);
+    if (h->prec == MDFT_F64) {
+      conv_fft<double>(h, p, -1, s);
+      mdft::launch_oz<double>(h->oz, static_cast<Cx<double>*>(p), s);
+      conv_fft<double>(h, p, +1, s);
+    } else {
+      conv_fft<float>(h, p, -1, s);
+      mdft::launch_oz<float>(h->oz, static_cast<Cx<float>*>(p), s);
+      conv_fft<float>(h, p, +1, s);
+    }
+  });
+}
+
+int mdft_conv_info(mdft_conv_t h, int* ints, double* dq) {
+  return guarded([&] {
+    throw_if(!h || !ints || !dq, "NULL argument");
+    ints[0] = h->npairs;
+    ints[1] = h->g.np_new;
+    ints[2] = h->nq;
+    *dq = h->dq;
+  });
+}
+
+int mdft_conv_gamma_p_map(mdft_conv_t h, int* map) {
+  return guarded([&] {
+    throw_if(!h || !map, "NULL argument");
+    std::memcpy(map, h->pair_list.data(), sizeof(int) * h->pair_list.size());
+  });
+}
+
+int mdft_conv_mnmunukhi_q(mdft_conv_t h, double* tab) {
+  return guarded([&] {
+    throw_if(!h || !tab, "NULL argument");
+    std::memcpy(tab, h->mnq.data(), sizeof(double) * 2 * h->mnq.size());
+  });
+}
+
+int mdft_get_delta_rho(const void* xi, void* delta_rho, size_t n, double rho0, int precision,
+                       void* stream) {
+  return guarded([&] {
+    check_prec(precision);
+    throw_if(n > 0 && (!xi || !delta_rho), "NULL argument");
+    if (precision == MDFT_F64)
+      mdft::launch_delta_rho<double>(static_cast<const double*>(xi), static_cast<double*>(delta_rho), n,
+                                     rho0, as_stream(stream));
+    else
+      mdft::launch_delta_rho<float>(static_cast<const float*>(xi), static_cast<float*>(delta_rho), n, rho0,
+                                    as_stream(stream));
+  });
+}
+
+int mdft_get_delta_f(const void* xi, const void* vexc, const double* w, void* delta_f, double* ff_dev,
+                     size_t nxyz, int no, double rho0, double prefactor, int precision, void* stream) {
+  return guarded([&] {
+    check_prec(precision);
+    throw_if(no <= 0, "angular grid size must be positive");
+    throw_if(!ff_dev, "NULL argument");
+    throw_if(nxyz > 0 && (!xi || !vexc || !w || !delta_f), "NULL argument");
+    cudaStream_t s = as_stream(stream);
+    const size_t nb = mdft::delta_f_partials(nxyz, no);
+    const size_t bytes = sizeof(double2) * nb + 16;
+    Scratch scratch(bytes, s);
+    mdft::cuda_check(cudaMemsetAsync(static_cast<char*>(scratch.p) + sizeof(double2) * nb, 0, 16, s),
+                     "cudaMemsetAsync");
+    if (precision == MDFT_F64)
+      mdft::launch_delta_f<double>(static_cast<const double*>(xi), static_cast<const double*>(vexc), w,
+                                   static_cast<double*>(delta_f), ff_dev, nxyz, no, rho0, prefactor,
+                                   scratch.p, s);
+    else
+      mdft::launch_delta_f<float>(static_cast<const float*>(xi), static_cast<const float*>(vexc), w,
+                                  static_cast<float*>(delta_f), ff_dev, nxyz, no, rho0, prefactor,
+                                  scratch.p, s);
+  });
+}
+
+}  // extern "C"

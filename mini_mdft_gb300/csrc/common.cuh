@@ -1,0 +1,175 @@
+// common.cuh -- complex type, launch checks and the device-side plan
+// structures shared by the hot-path kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "host_setup.hpp"
+
+namespace mdft {
+
+// Interleaved complex (re, im): the layout of Kokkos::complex<T>.
+template <typename T>
+struct __align__(2 * sizeof(T)) Cx {
+  T re, im;
+};
+
+template <typename T>
+__host__ __device__ __forceinline__ Cx<T> mkc(T r, T i) {
+  Cx<T> z;
+  z.re = r;
+  z.im = i;
+  return z;
+}
+template <typename T>
+__host__ __device__ __forceinline__ Cx<T> operator+(Cx<T> a, Cx<T> b) {
+  return mkc<T>(a.re + b.re, a.im + b.im);
+}
+template <typename T>
+__host__ __device__ __forceinline__ Cx<T> operator-(Cx<T> a, Cx<T> b) {
+  return mkc<T>(a.re - b.re, a.im - b.im);
+}
+template <typename T>
+__host__ __device__ __forceinline__ Cx<T> operator*(Cx<T> a, Cx<T> b) {
+  return mkc<T>(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
+}
+template <typename T>
+__host__ __device__ __forceinline__ Cx<T> operator*(Cx<T> a, T s) {
+  return mkc<T>(a.re * s, a.im * s);
+}
+template <typename T>
+__host__ __device__ __forceinline__ Cx<T> conj(Cx<T> a) {
+  return mkc<T>(a.re, -a.im);
+}
+// a + b * c (complex multiply-accumulate)
+template <typename T>
+__host__ __device__ __forceinline__ Cx<T> cmac(Cx<T> a, Cx<T> b, Cx<T> c) {
+  return mkc<T>(a.re + b.re * c.re - b.im * c.im, a.im + b.re * c.im + b.im * c.re);
+}
+
+inline void cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess)
+    throw Error(2, std::string(what) + ": " + cudaGetErrorString(e));
+}
+inline void launch_check(const char* what) { cuda_check(cudaGetLastError(), what); }
+
+// Owning device buffer.
+struct DevBuf {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() {
+    if (ptr) cudaFree(ptr);
+  }
+  void alloc(size_t n) {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = n;
+    if (n == 0) return;
+    cudaError_t e = cudaMalloc(&ptr, n);
+    if (e != cudaSuccess) {
+      ptr = nullptr;
+      throw Error(5, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+    }
+  }
+  void upload(const void* src, size_t n) {
+    alloc(n);
+    if (n) cuda_check(cudaMemcpy(ptr, src, n, cudaMemcpyHostToDevice), "cudaMemcpy H2D");
+  }
+  template <typename T>
+  T* as() const {
+    return static_cast<T*>(ptr);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Orientation <-> projection transform plan (device tables).
+// ---------------------------------------------------------------------------
+struct AngPlan {
+  long long N;  // grid points
+  int ntheta, nphi, npsi, K, mmax, mrso, np, no;
+  int tile_a2p, tile_p2a;           // points per CTA
+  size_t smem_a2p, smem_p2a;        // dynamic shared memory bytes
+  const void* coef_a2p;             // (ntheta, np) T : d * wtheta * fm / (nphi*npsi)
+  const void* coef_p2a;             // (ntheta, np) T : d * fm
+  const void* tw_phi;               // (nphi) Cx<T> : exp(-2 pi i t / nphi)
+  const void* tw_psi;               // (npsi) Cx<T>
+  const int* ip_m;                  // (np)
+  const int* ip_mup;                // (np)
+  const int* ip_mu2;                // (np)
+  const int* pmap;                  // (mmax+1, 2mmax+1, K+1)
+};
+
+template <typename T>
+void launch_angl2proj(const AngPlan& P, const T* o, Cx<T>* p, bool from_xi,
+                      double rho0, cudaStream_t s);
+template <typename T>
+void launch_proj2angl(const AngPlan& P, const Cx<T>* p, T* o, cudaStream_t s);
+template <typename T>
+void ang_plan_finish(AngPlan& P);  // picks tiles / smem sizes, sets attributes
+
+// ---------------------------------------------------------------------------
+// Batched 1-D FFT along one axis of a (B, n, S) complex array.
+// ---------------------------------------------------------------------------
+constexpr int kMaxRadices = 16;
+struct FftAxis {
+  int n;          // transform length
+  long long S;    // stride between consecutive elements of one transform
+  long long ncols;  // number of transforms (B * S)
+  int nr;         // number of radix stages
+  int radix[kMaxRadices];
+  int cols;       // transforms per CTA
+  size_t smem;
+  const void* tw;  // (n) Cx<T> : exp(-2 pi i t / n)
+};
+bool fft_factor(int n, FftAxis& a);  // false if n has a prime factor > 13
+template <typename T>
+void fft_axis_finish(FftAxis& a);
+template <typename T>
+void launch_fft_axis(const FftAxis& a, Cx<T>* data, int sign, cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// Fused (q,-q) rotation + Ornstein-Zernike + rotation back.
+// ---------------------------------------------------------------------------
+struct OzPlan {
+  int nx, ny, nz, np, mmax, mrso, K, np_new, nq, npairs;
+  long long N;
+  double dq;
+  const int4* pairs;       // (npairs) ix, iy, iz, 0 -- sorted by q's linear index
+  const double* kx;        // (nx)
+  const double* ky;
+  const double* kz;
+  const double* rot;       // a (5,13,13) | b (5,13,13) | c (5,13) | d (5,13)
+  const int* pmap;         // (mmax+1, 2mmax+1, K+1)
+  const int* ip_m;
+  const int* ip_mup;
+  const int* ip_mu2;
+  const int* ia_map;       // (np, mmax+1, 2mmax/mrso+1)
+  const void* ctab;        // (nq, np_new) Cx<T>, transposed mnmunukhi_q
+  int warps_per_cta;
+  size_t smem;
+};
+template <typename T>
+void oz_plan_finish(OzPlan& P);
+template <typename T>
+void launch_oz(const OzPlan& P, Cx<T>* p, cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// Energy / gradient.
+// ---------------------------------------------------------------------------
+template <typename T>
+void launch_delta_rho(const T* xi, T* dr, size_t n, double rho0, cudaStream_t s);
+// partials: >= delta_f_partials(nxyz) double2 entries + one uint counter
+// (zeroed by the caller before the first use; the kernel leaves it zero).
+size_t delta_f_partials(size_t nxyz, int no);
+template <typename T>
+void launch_delta_f(const T* xi, const T* vexc, const double* w, T* df,
+                    double* ff, size_t nxyz, int no, double rho0,
+                    double prefactor, void* work, cudaStream_t s);
+
+}  // namespace mdft

@@ -1,0 +1,330 @@
+// oz.cu -- the k-space step of Convolution::execute
+// (common/MDFT_Convolution.hpp:376-543), fused into one kernel.
+//
+// For each (q, -q) pair of the half-space pair list (:129-176) one warp:
+//   1. builds R(q), the rotation matrix between complex spherical harmonics
+//      of degree <= mmax, by the l-recursion of
+//      common/MDFT_Rotation.hpp:103-283 in FP64 (level 1 by one lane, then
+//      the entries of each level l >= 2 spread over the lanes);
+//   2. reads the np projections at q and at -q once (:420-425);
+//   3. rotates them to the q frame (:427-443);
+//   4. forms the OZ product with c(|q|) linearly interpolated between the
+//      two bracketing table rows (:449-496); the interpolation is done on the
+//      fly because every OZ coefficient is used exactly once per pair;
+//   5. chops |gamma| < epsilon to zero (:514-517), rotates back with conj(R)
+//      (:518-536) and stores q then -q, conjugating -q at the singular
+//      mid-k points (:538-541).
+// Pairs are visited sorted by the linear index of q, so neighbouring warps
+// touch neighbouring addresses of each projection plane.
+#include <cfloat>
+
+#include "common.cuh"
+
+namespace mdft {
+
+namespace {
+
+constexpr int kRotL5 = 5, kRotM13 = 13;  // RotationCoeffs extents (l-2, m+6)
+
+__host__ __device__ inline int roff(int l) { return l * (2 * l - 1) * (2 * l + 1) / 3; }
+__host__ __device__ inline int nrot(int mmax) { return roff(mmax + 1); }
+
+template <typename T>
+struct OzSmem {
+  size_t R, gq, gmq, dq, dmq, per_warp;
+  __host__ __device__ OzSmem(int mmax, int np) {
+    size_t o = 0;
+    R = o;
+    o += sizeof(Cx<double>) * nrot(mmax);
+    gq = o;
+    o += sizeof(Cx<T>) * np;
+    gmq = o;
+    o += sizeof(Cx<T>) * np;
+    dq = o;
+    o += sizeof(Cx<T>) * np;
+    dmq = o;
+    o += sizeof(Cx<T>) * np;
+    per_warp = (o + 15) & ~size_t(15);
+  }
+};
+
+template <typename T>
+__device__ __forceinline__ T eps_of();
+template <>
+__device__ __forceinline__ double eps_of<double>() {
+  return DBL_EPSILON;
+}
+template <>
+__device__ __forceinline__ float eps_of<float>() {
+  return FLT_EPSILON;
+}
+
+// prevent_underflow (common/MDFT_Math_Utils.hpp:102-113)
+template <typename T>
+__device__ __forceinline__ Cx<T> chop(Cx<T> x) {
+  const T e = eps_of<T>();
+  if (fabs(x.re) < e) x.re = T(0);
+  if (fabs(x.im) < e) x.im = T(0);
+  return x;
+}
+
+template <typename T>
+__device__ __forceinline__ Cx<T> to(Cx<double> z) {
+  return mkc<T>((T)z.re, (T)z.im);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+oz_kernel(const OzPlan P, Cx<T>* __restrict__ p) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const long long pair = (long long)blockIdx.x * P.warps_per_cta + wib;
+  if (pair >= P.npairs) return;  // whole warp exits together
+  const OzSmem<T> L(P.mmax, P.np);
+  unsigned char* base = sm + (size_t)wib * L.per_warp;
+  Cx<double>* R = reinterpret_cast<Cx<double>*>(base + L.R);
+  Cx<T>* gq = reinterpret_cast<Cx<T>*>(base + L.gq);
+  Cx<T>* gmq = reinterpret_cast<Cx<T>*>(base + L.gmq);
+  Cx<T>* dq = reinterpret_cast<Cx<T>*>(base + L.dq);
+  Cx<T>* dmq = reinterpret_cast<Cx<T>*>(base + L.dmq);
+
+  const int mmax = P.mmax, mrso = P.mrso, K1 = P.K + 1, np = P.np;
+  const int nphi = 2 * mmax + 1, n2 = 2 * mmax / mrso + 1;
+  const int4 pr = P.pairs[pair];
+  const int ix = pr.x, iy = pr.y, iz = pr.z;
+  const int ixm = ix == 0 ? 0 : P.nx - ix;
+  const int iym = iy == 0 ? 0 : P.ny - iy;
+  const int izm = iz == 0 ? 0 : P.nz - iz;
+  const double q0 = P.kx[ix], q1 = P.ky[iy], q2 = P.kz[iz];
+  const double* A = P.rot;
+  const double* B = A + kRotL5 * kRotM13 * kRotM13;
+  const double* Cc = B + kRotL5 * kRotM13 * kRotM13;
+  const double* D = Cc + kRotL5 * kRotM13;
+  constexpr int mm = 6;
+#define RI(l, m, m1) (roff(l) + ((m) + (l)) * (2 * (l) + 1) + ((m1) + (l)))
+#define AA(l, i, j) A[((l)*kRotM13 + (i)) * kRotM13 + (j)]
+#define BB(l, i, j) B[((l)*kRotM13 + (i)) * kRotM13 + (j)]
+#define CC(l, i) Cc[(l)*kRotM13 + (i)]
+#define DD(l, i) D[(l)*kRotM13 + (i)]
+
+  // ---- 1. R(q) -----------------------------------------------------------
+  if (lane == 0) {
+    R[0] = mkc<double>(1.0, 0.0);
+    double r2[3], r1[3], r0[3];
+    if (q0 == 0.0 && q1 == 0.0 && q2 == 0.0) {
+      r2[0] = 0.0;
+      r2[1] = 0.0;
+      r2[2] = 1.0;
+    } else {
+      r2[0] = q0;
+      r2[1] = q1;
+      r2[2] = q2;
+    }
+    if (r2[0] != 0.0 || r2[1] != 0.0) {  // cross((0,0,1), r2)
+      r1[0] = 0.0 * r2[2] - 1.0 * r2[1];
+      r1[1] = 1.0 * r2[0] - 0.0 * r2[2];
+      r1[2] = 0.0 * r2[1] - 0.0 * r2[0];
+    } else {  // cross(r2, (1,0,0))
+      r1[0] = r2[1] * 0.0 - r2[2] * 0.0;
+      r1[1] = r2[2] * 1.0 - r2[0] * 0.0;
+      r1[2] = r2[0] * 0.0 - r2[1] * 1.0;
+    }
+    double n2v = sqrt(r2[0] * r2[0] + r2[1] * r2[1] + r2[2] * r2[2]);
+    for (int i = 0; i < 3; ++i) r2[i] = r2[i] / n2v;
+    double n1v = sqrt(r1[0] * r1[0] + r1[1] * r1[1] + r1[2] * r1[2]);
+    for (int i = 0; i < 3; ++i) r1[i] = r1[i] / n1v;
+    r0[0] = r1[1] * r2[2] - r1[2] * r2[1];
+    r0[1] = r1[2] * r2[0] - r1[0] * r2[2];
+    r0[2] = r1[0] * r2[1] - r1[1] * r2[0];
+    const double is2 = 1.0 / sqrt(2.0);
+    R[RI(1, -1, -1)] = mkc<double>((r1[1] + r0[0]) * 0.5, (r0[1] - r1[0]) * 0.5);
+    R[RI(1, -1, 0)] = mkc<double>(r2[0] * is2, r2[1] * is2);
+    R[RI(1, -1, 1)] = mkc<double>((r1[1] - r0[0]) * 0.5, (-r0[1] - r1[0]) * 0.5);
+    R[RI(1, 0, -1)] = mkc<double>(r0[2] * is2, -r1[2] * is2);
+    R[RI(1, 0, 0)] = mkc<double>(r2[2], 0.0);
+    R[RI(1, 0, 1)] = mkc<double>(-r0[2] * is2, -r1[2] * is2);
+    R[RI(1, 1, -1)] = mkc<double>((r1[1] - r0[0]) * 0.5, (r0[1] + r1[0]) * 0.5);
+    R[RI(1, 1, 0)] = mkc<double>(-r2[0] * is2, r2[1] * is2);
+    R[RI(1, 1, 1)] = mkc<double>((r1[1] + r0[0]) * 0.5, (r1[0] - r0[1]) * 0.5);
+  }
+  __syncwarp();
+  for (int l = 2; l <= mmax; ++l) {
+    // entries (m, m1): m in [-l, l], m1 in [m>0 ? 1 : 0, l]
+    const int cnt = (2 * l + 1) * (l + 1) - l;  // l rows (m>0) lack m1 = 0
+    const Cx<double> R1m0 = R[RI(1, -1, 0)], R1z0 = R[RI(1, 0, 0)], R1p0 = R[RI(1, 1, 0)];
+    const Cx<double> R1m1 = R[RI(1, -1, 1)], R1z1 = R[RI(1, 0, 1)], R1p1 = R[RI(1, 1, 1)];
+    for (int e = lane; e < cnt; e += 32) {
+      // decode: rows m = -l..0 have l+1 entries (m1 = 0..l), rows m = 1..l have l
+      int m, m1;
+      const int first = (l + 1) * (l + 1);
+      if (e < first) {
+        m = -l + e / (l + 1);
+        m1 = e % (l + 1);
+      } else {
+        const int e2 = e - first;
+        m = 1 + e2 / l;
+        m1 = 1 + e2 % l;
+      }
+      const int l1 = l - 1;
+      double f, g;
+      if (m1 <= l - 1) {
+        if (m == -l) {
+          const double bt = BB(l - 2, mm - m, mm + m1);
+          const Cx<double> a = R1m0, b = R[RI(l1, m + 1, m1)];
+          f = bt * (a.re * b.re - a.im * b.im);
+          g = bt * (a.re * b.im + a.im * b.re);
+        } else if (m == l) {
+          const double bt = BB(l - 2, mm + m, mm + m1);
+          const Cx<double> a = R1p0, b = R[RI(l1, m - 1, m1)];
+          f = bt * (a.re * b.re - a.im * b.im);
+          g = bt * (a.re * b.im + a.im * b.re);
+        } else {
+          const double at = AA(l - 2, mm + m, mm + m1);
+          const double bp = BB(l - 2, mm + m, mm + m1);
+          const double bn = BB(l - 2, mm - m, mm + m1);
+          const Cx<double> R0 = R1z0, Ra = R1p0, Rb = R1m0;
+          const Cx<double> Rm0 = R[RI(l1, m, m1)];
+          const Cx<double> Rm1 = (m + 1 <= l1) ? R[RI(l1, m + 1, m1)] : mkc<double>(0, 0);
+          const Cx<double> Rm2 = (m - 1 >= -l1) ? R[RI(l1, m - 1, m1)] : mkc<double>(0, 0);
+          f = at * (R0.re * Rm0.re) + bp * (Ra.re * Rm2.re - Ra.im * Rm2.im) +
+              bn * (Rb.re * Rm1.re - Rb.im * Rm1.im);
+          g = at * (R0.re * Rm0.im) + bp * (Ra.re * Rm2.im + Ra.im * Rm2.re) +
+              bn * (Rb.re * Rm1.im + Rb.im * Rm1.re);
+        }
+      } else {  // m1 == l
+        if (m == -l) {
+          const double dt = DD(l - 2, mm - m);
+          const Cx<double> a = R1m1, b = R[RI(l1, m + 1, m1 - 1)];
+          f = dt * (a.re * b.re - a.im * b.im);
+          g = dt * (a.re * b.im + a.im * b.re);
+        } else if (m == l) {
+          const double dt = DD(l - 2, mm + m);
+          const Cx<double> a = R1p1, b = R[RI(l1, m - 1, m1 - 1)];
+          f = dt * (a.re * b.re - a.im * b.im);
+          g = dt * (a.re * b.im + a.im * b.re);
+        } else {
+          const double ct = CC(l - 2, mm + m);
+          const double dp = DD(l - 2, mm + m);
+          const double dn = DD(l - 2, mm - m);
+          const Cx<double> R0 = R1z1, Ra = R1p1, Rb = R1m1;
+          const Cx<double> Rm0 = R[RI(l1, m, m1 - 1)];
+          const Cx<double> Rm1 = (m + 1 <= l1) ? R[RI(l1, m + 1, m1 - 1)] : mkc<double>(0, 0);
+          const Cx<double> Rm2 = (m - 1 >= -l1) ? R[RI(l1, m - 1, m1 - 1)] : mkc<double>(0, 0);
+          f = ct * (R0.re * Rm0.re - R0.im * Rm0.im) + dp * (Ra.re * Rm2.re - Ra.im * Rm2.im) +
+              dn * (Rb.re * Rm1.re - Rb.im * Rm1.im);
+          g = ct * (R0.re * Rm0.im + R0.im * Rm0.re) + dp * (Ra.re * Rm2.im + Ra.im * Rm2.re) +
+              dn * (Rb.re * Rm1.im + Rb.im * Rm1.re);
+        }
+      }
+      R[RI(l, m, m1)] = mkc<double>(f, g);
+      const double pw = ((m + m1) & 1) ? -1.0 : 1.0;
+      R[RI(l, -m, -m1)] = mkc<double>(pw * f, -pw * g);
+    }
+    __syncwarp();
+  }
+
+  // ---- 2. load gamma(q), gamma(-q) ------------------------------------------
+  const long long N = P.N;
+  const long long lq = ((long long)ix * P.ny + iy) * P.nz + iz;
+  const long long lmq = ((long long)ixm * P.ny + iym) * P.nz + izm;
+  for (int ip = lane; ip < np; ip += 32) {
+    gq[ip] = p[(long long)ip * N + lq];
+    gmq[ip] = p[(long long)ip * N + lmq];
+  }
+  __syncwarp();
+  // ---- 3. rotation to the q frame ---------------------------------------------
+  for (int ip = lane; ip < np; ip += 32) {
+    const int im = P.ip_m[ip], ikhi = P.ip_mup[ip], imu2 = P.ip_mu2[ip];
+    Cx<T> a = mkc<T>(0, 0), b = mkc<T>(0, 0);
+    for (int imup = -im; imup <= im; ++imup) {
+      const int ipm = P.pmap[(im * nphi + imup + mmax) * K1 + imu2];
+      a = cmac(a, gq[ipm], to<T>(R[RI(im, imup, ikhi)]));
+      b = cmac(b, gmq[ipm], to<T>(R[RI(im, imup, -ikhi)]));
+    }
+    dq[ip] = a;
+    dmq[ip] = (im & 1) ? mkc<T>(-b.re, -b.im) : b;
+  }
+  __syncwarp();
+  // ---- 4. OZ with interpolated c(|q|) -------------------------------------
+  const double qn = sqrt(q0 * q0 + q1 * q1 + q2 * q2);
+  const double eiq = qn / P.dq;
+  // |q| <= q_max and nq = int(q_max/dq + 0.5) + 2 keep iq + 1 < nq; the
+  // clamp only guards the table bounds against rounding at that edge.
+  const int iq = min((int)eiq, P.nq - 2);
+  const T alpha = (T)(eiq - (double)iq);
+  const T beta = T(1) - alpha;
+  const Cx<T>* ctab = static_cast<const Cx<T>*>(P.ctab);
+  const Cx<T>* clo = ctab + (size_t)iq * P.np_new;
+  const Cx<T>* chi = ctab + (size_t)(iq + 1) * P.np_new;
+  for (int ip = lane; ip < np; ip += 32) {
+    const int ikhi = P.ip_mup[ip];
+    Cx<T> sq = mkc<T>(0, 0), smq = mkc<T>(0, 0);
+    for (int in = abs(ikhi); in <= mmax; ++in) {
+      for (int inu2 = -in / mrso; inu2 <= in / mrso; ++inu2) {
+        const int ia = P.ia_map[((size_t)ip * (mmax + 1) + in) * n2 + inu2 + mmax / mrso];
+        const Cx<T> h = chi[ia], lo = clo[ia];
+        const Cx<T> c = mkc<T>(alpha * h.re + beta * lo.re, alpha * h.im + beta * lo.im);
+        if (inu2 < 0) {
+          const int ipm = P.pmap[(in * nphi + ikhi + mmax) * K1 + (-inu2)];
+          sq = cmac(sq, c, dq[ipm]);
+          smq = cmac(smq, c, dmq[ipm]);
+        } else {
+          const int ipm = P.pmap[(in * nphi + ikhi + mmax) * K1 + inu2];
+          sq = cmac(sq, c, conj(dmq[ipm]));
+          smq = cmac(smq, c, conj(dq[ipm]));
+        }
+      }
+    }
+    gq[ip] = sq;
+    gmq[ip] = smq;
+  }
+  __syncwarp();
+  // ---- 5. chop, rotate back, store -----------------------------------------
+  const bool qeq = (ixm == ix && iym == iy && izm == iz);
+  const bool singular = qeq && (ix == P.nx / 2 || iy == P.ny / 2 || iz == P.nz / 2);
+  for (int ip = lane; ip < np; ip += 32) {
+    const int im = P.ip_m[ip], imup = P.ip_mup[ip], imu2 = P.ip_mu2[ip];
+    Cx<T> a = mkc<T>(0, 0), b = mkc<T>(0, 0);
+    for (int ikhi = -im; ikhi <= im; ++ikhi) {
+      const int ipm = P.pmap[(im * nphi + ikhi + mmax) * K1 + imu2];
+      a = cmac(a, chop(gq[ipm]), conj(to<T>(R[RI(im, imup, ikhi)])));
+      b = cmac(b, chop(gmq[ipm]), conj(to<T>(R[RI(im, imup, -ikhi)])));
+    }
+    if (im & 1) b = mkc<T>(-b.re, -b.im);
+    p[(long long)ip * N + lq] = a;
+    p[(long long)ip * N + lmq] = singular ? conj(b) : b;
+  }
+#undef RI
+#undef AA
+#undef BB
+#undef CC
+#undef DD
+}
+
+}  // namespace
+
+template <typename T>
+void oz_plan_finish(OzPlan& P) {
+  const OzSmem<T> L(P.mmax, P.np);
+  P.warps_per_cta = 8;
+  P.smem = L.per_warp * P.warps_per_cta;
+  throw_if(P.smem > 200 * 1024, "mmax too large for the OZ kernel", 4);
+  cuda_check(cudaFuncSetAttribute(oz_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)P.smem),
+             "cudaFuncSetAttribute(oz)");
+}
+
+template <typename T>
+void launch_oz(const OzPlan& P, Cx<T>* p, cudaStream_t s) {
+  if (P.npairs == 0) return;
+  const long long nb = (P.npairs + P.warps_per_cta - 1) / P.warps_per_cta;
+  oz_kernel<T><<<(unsigned)nb, 32 * P.warps_per_cta, P.smem, s>>>(P, p);
+  launch_check("oz kernel launch");
+}
+
+template void oz_plan_finish<double>(OzPlan&);
+template void oz_plan_finish<float>(OzPlan&);
+template void launch_oz<double>(const OzPlan&, Cx<double>*, cudaStream_t);
+template void launch_oz<float>(const OzPlan&, Cx<float>*, cudaStream_t);
+
+}  // namespace mdft
