@@ -47,6 +47,9 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mode", choices=["full", "steps"], default="full",
+                    help="steps: only W warm-up + K timed FP64 and FP32 round trips "
+                         "(a short, fixed launch sequence for ncu captures)")
     return ap.parse_args()
 
 
@@ -355,6 +358,17 @@ def run_ours(args):
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
     P = make_problem("f64")
+    if args.mode == "steps":
+        Pm = make_problem("f32")
+        for PP in (P, Pm):
+            for _ in range(W):
+                step(PP)
+            torch.cuda.synchronize()
+            t = timed_steps(PP, K, flush)
+            if rank == 0:
+                print(json.dumps({"mode": "steps", "dtype": str(PP["rd"]).replace("torch.", ""),
+                                  "ms_per_step": t / K * 1e3}), flush=True)
+        return
     clocks = ClockSampler(dev)
     clocks.start()
     for _ in range(W):

@@ -244,15 +244,9 @@ void ang_plan_finish(AngPlan& P) {
   P.smem_p2a = P2ASmem<T>(P, tp).total;
   throw_if(P.smem_a2p > 200 * 1024 || P.smem_p2a > 200 * 1024,
            "angular grid too large for the shared-memory tile", 4);
-  cuda_check(cudaFuncSetAttribute(angl2proj_kernel<T, false>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem_a2p),
-             "cudaFuncSetAttribute(angl2proj)");
-  cuda_check(cudaFuncSetAttribute(angl2proj_kernel<T, true>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem_a2p),
-             "cudaFuncSetAttribute(angl2proj)");
-  cuda_check(cudaFuncSetAttribute(proj2angl_kernel<T>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem_p2a),
-             "cudaFuncSetAttribute(proj2angl)");
+  allow_max_smem(angl2proj_kernel<T, false>, P.smem_a2p, "angl2proj smem attribute");
+  allow_max_smem(angl2proj_kernel<T, true>, P.smem_a2p, "angl2proj smem attribute");
+  allow_max_smem(proj2angl_kernel<T>, P.smem_p2a, "proj2angl smem attribute");
 }
 
 template <typename T>

@@ -56,6 +56,20 @@ inline void cuda_check(cudaError_t e, const char* what) {
 }
 inline void launch_check(const char* what) { cuda_check(cudaGetLastError(), what); }
 
+// Opts a kernel in to the device's full dynamic shared-memory size.  The
+// attribute is per function, so it is never lowered to one plan's size (a
+// later, smaller plan would otherwise make earlier plans' launches fail).
+template <typename K>
+inline void allow_max_smem(K* func, size_t needed, const char* what) {
+  int dev = 0, optin = 0;
+  cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  cuda_check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev),
+             "cudaDeviceGetAttribute");
+  if (needed > (size_t)optin)
+    throw Error(4, std::string(what) + ": needs more shared memory than the device offers");
+  cuda_check(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, optin), what);
+}
+
 // Owning device buffer.
 struct DevBuf {
   void* ptr = nullptr;

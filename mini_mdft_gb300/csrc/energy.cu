@@ -124,10 +124,7 @@ void launch_delta_f(const T* xi, const T* vexc, const double* w, T* df, double* 
   throw_if(nb > 0x7fffffffULL, "grid too large", 4);
   const size_t smem = sizeof(double) * ((size_t)no + (size_t)kEnergyPoints * no);
   throw_if(smem > 200 * 1024, "too many orientations for the energy kernel", 4);
-  if (smem > 48 * 1024)
-    cuda_check(cudaFuncSetAttribute(delta_f_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem),
-               "cudaFuncSetAttribute(delta_f)");
+  if (smem > 48 * 1024) allow_max_smem(delta_f_kernel<T>, smem, "delta_f smem attribute");
   double2* partials = static_cast<double2*>(work);
   unsigned* counter = reinterpret_cast<unsigned*>(partials + nb);
   if (nb == 0) {

@@ -174,9 +174,7 @@ void fft_axis_finish(FftAxis& a) {
   a.cols = cols;
   a.smem = sizeof(Cx<T>) * ((size_t)2 * a.n * cols + a.n);
   throw_if(a.smem > 200 * 1024, "FFT length too large for the shared-memory tile", 4);
-  cuda_check(cudaFuncSetAttribute(fft_axis_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)a.smem),
-             "cudaFuncSetAttribute(fft)");
+  allow_max_smem(fft_axis_kernel<T>, a.smem, "fft smem attribute");
 }
 
 template <typename T>

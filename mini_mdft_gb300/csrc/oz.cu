@@ -309,9 +309,7 @@ void oz_plan_finish(OzPlan& P) {
   P.warps_per_cta = 8;
   P.smem = L.per_warp * P.warps_per_cta;
   throw_if(P.smem > 200 * 1024, "mmax too large for the OZ kernel", 4);
-  cuda_check(cudaFuncSetAttribute(oz_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)P.smem),
-             "cudaFuncSetAttribute(oz)");
+  allow_max_smem(oz_kernel<T>, P.smem, "oz smem attribute");
 }
 
 template <typename T>
