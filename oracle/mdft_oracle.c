@@ -713,7 +713,9 @@ int mdfto_set_luc(mdft_oracle* o, const int* luc_index, const double* luc,
   int m2 = 2 * mmax + 1;
   int need = mdfto_nq_for_dq(o, dq);
   if (nq < need) return 1;
-  /* The reader keeps exactly `need` rows. */
+  /* The reader keeps exactly `need` rows; `stride` is the caller's row
+   * length. */
+  const int stride = nq;
   nq = need;
   int* p5 = (int*)calloc((size_t)(mmax + 1) * (mmax + 1) * npm * npm * m2, sizeof(int));
 #define P5(a, b, c, d, e) p5[((((a) * (mmax + 1) + (b)) * npm + (c)) * npm + (d)) * m2 + (e)]
@@ -744,7 +746,7 @@ int mdfto_set_luc(mdft_oracle* o, const int* luc_index, const double* luc,
             khi_new[i] = ikhi;
             int ip = P5(im, in, imu2 + K, inu2 + K, ikhi + mmax);
             for (int iq = 0; iq < nq; iq++)
-              o->mnmunukhi_q[(size_t)i * nq + iq] = L[(size_t)ip * nq + iq];
+              o->mnmunukhi_q[(size_t)i * nq + iq] = L[(size_t)ip * stride + iq];
             i++;
           }
 #undef P5

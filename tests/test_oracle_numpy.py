@@ -226,3 +226,35 @@ def test_prefactor_matches_reference_formula():
     rho0, pref = I.tip3p_constants()
     assert abs(pref - O.prefactor(298.0, 2, I.TIP3P_N0)) < 1e-15 * abs(pref)
     assert abs(rho0 - I.TIP3P_N0 / (8 * math.pi ** 2 / 2)) < 1e-18
+
+
+def numpy_mnmunukhi_q(mmax, mrso, idx, tab, nq):
+    """common/MDFT_Convolution.hpp:271-311 restated: reorder the Luc table
+    into (m, khi, mu2, n, nu2) order and fold the (-1)^(khi+nu) / (-1)^n
+    signs in."""
+    K = mmax // mrso
+    pos = {}
+    for ip in range(idx.shape[1]):
+        m, n, mu, nu, khi = (int(v) for v in idx[:, ip])
+        pos[(m, n, mu // mrso + K, nu // mrso + K, khi + mmax)] = ip
+    rows = []
+    for im in range(mmax + 1):
+        for ikhi in range(-im, im + 1):
+            for imu2 in range(im // mrso + 1):
+                for in_ in range(abs(ikhi), mmax + 1):
+                    for inu2 in range(-(in_ // mrso), in_ // mrso + 1):
+                        ip = pos.get((im, in_, imu2 + K, inu2 + K, ikhi + mmax), 0)
+                        nu = inu2 * mrso
+                        s = (-1.0) ** (ikhi + nu) if nu < 0 else (-1.0) ** in_
+                        rows.append(s * tab[ip, :nq])
+    return np.array(rows)
+
+
+@pytest.mark.parametrize("mmax,mrso,extra", [(3, 2, 0), (3, 2, 7), (5, 2, 3), (2, 1, 1), (4, 3, 0)])
+def test_luc_reorder_matches_numpy(mmax, mrso, extra):
+    o = O.Oracle((6, 5, 4), (9., 8., 7.), mmax, mrso)
+    nq = o.nq_for_dq(0.01)
+    idx, tab = I.synthetic_cq(mmax, mrso, nq + extra, 0.01)
+    o.set_luc(idx, tab, 0.01)
+    assert o.nq == nq
+    assert np.array_equal(o.mnmunukhi_q(), numpy_mnmunukhi_q(mmax, mrso, idx, tab, nq))
