@@ -255,6 +255,7 @@ void launch_angl2proj(const AngPlan& P, const T* o, Cx<T>* p, bool from_xi,
   if (P.N == 0) return;
   const long long nb = (P.N + P.tile_a2p - 1) / P.tile_a2p;
   throw_if(nb > 0x7fffffffLL, "grid too large", 4);
+  clear_stale_error();
   if (from_xi)
     angl2proj_kernel<T, true><<<(unsigned)nb, kAngThreads, P.smem_a2p, s>>>(P, o, p, (T)rho0);
   else
@@ -267,6 +268,7 @@ void launch_proj2angl(const AngPlan& P, const Cx<T>* p, T* o, cudaStream_t s) {
   if (P.N == 0) return;
   const long long nb = (P.N + P.tile_p2a - 1) / P.tile_p2a;
   throw_if(nb > 0x7fffffffLL, "grid too large", 4);
+  clear_stale_error();
   proj2angl_kernel<T><<<(unsigned)nb, kAngThreads, P.smem_p2a, s>>>(P, p, o);
   launch_check("proj2angl kernel launch");
 }

@@ -51,10 +51,15 @@ __host__ __device__ __forceinline__ Cx<T> cmac(Cx<T> a, Cx<T> b, Cx<T> c) {
 }
 
 inline void cuda_check(cudaError_t e, const char* what) {
-  if (e != cudaSuccess)
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // a non-sticky error must not resurface at a later check
     throw Error(2, std::string(what) + ": " + cudaGetErrorString(e));
+  }
 }
 inline void launch_check(const char* what) { cuda_check(cudaGetLastError(), what); }
+// Clears a non-sticky error left by an earlier, unrelated runtime call so that
+// the launch_check after our launch reports our launch only.
+inline void clear_stale_error() { (void)cudaGetLastError(); }
 
 // Opts a kernel in to the device's full dynamic shared-memory size.  The
 // attribute is per function, so it is never lowered to one plan's size (a
@@ -65,9 +70,12 @@ inline void allow_max_smem(K* func, size_t needed, const char* what) {
   cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
   cuda_check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev),
              "cudaDeviceGetAttribute");
-  if (needed > (size_t)optin)
+  cudaFuncAttributes fa;
+  cuda_check(cudaFuncGetAttributes(&fa, func), what);
+  const int maxdyn = optin - (int)fa.sharedSizeBytes;  // static smem counts against the opt-in
+  if (needed > (size_t)maxdyn)
     throw Error(4, std::string(what) + ": needs more shared memory than the device offers");
-  cuda_check(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, optin), what);
+  cuda_check(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, maxdyn), what);
 }
 
 // Owning device buffer.

@@ -113,6 +113,7 @@ void launch_delta_rho(const T* xi, T* dr, size_t n, double rho0, cudaStream_t s)
   if (n == 0) return;
   size_t nb = (n + kEnergyThreads - 1) / kEnergyThreads;
   if (nb > 152 * 64) nb = 152 * 64;
+  clear_stale_error();
   delta_rho_kernel<T><<<(unsigned)nb, kEnergyThreads, 0, s>>>(xi, dr, n, (T)rho0);
   launch_check("delta_rho kernel launch");
 }
@@ -131,6 +132,7 @@ void launch_delta_f(const T* xi, const T* vexc, const double* w, T* df, double* 
     cuda_check(cudaMemsetAsync(ff, 0, sizeof(double), s), "cudaMemsetAsync(ff)");
     return;
   }
+  clear_stale_error();
   delta_f_kernel<T><<<(unsigned)nb, kEnergyThreads, smem, s>>>(xi, vexc, w, df, ff, nxyz, no, rho0,
                                                                prefactor, partials, counter);
   launch_check("delta_f kernel launch");

@@ -182,6 +182,7 @@ void launch_fft_axis(const FftAxis& a, Cx<T>* data, int sign, cudaStream_t s) {
   if (a.n <= 1 || a.ncols == 0) return;
   const long long nb = (a.ncols + a.cols - 1) / a.cols;
   throw_if(nb > 0x7fffffffLL, "FFT batch too large", 4);
+  clear_stale_error();
   fft_axis_kernel<T><<<(unsigned)nb, kFftThreads, a.smem, s>>>(a, data, sign);
   launch_check("fft kernel launch");
 }
