@@ -3,7 +3,8 @@ oracle on the same seeded inputs.
 
 Tolerances (max-norm relative error, max|gpu - oracle| / max|oracle|):
   FP64 plain form: 1e-12 (projections, convolved fields, energy, gradient);
-  FP32 mixed form: 2e-5 for the fields, 1e-6 for the excess energy.
+  FP32 mixed form: 1e-4 for the fields, 1e-6 for the excess energy (the
+  spec bound for the mixed form is on the energy).
 """
 import numpy as np
 import pytest
@@ -16,7 +17,7 @@ from _util import rel_err
 pytestmark = pytest.mark.gpu
 
 TOL64 = 1e-12
-TOL32 = 2e-5
+TOL32 = 1e-4
 
 
 def _t(x, dtype):
