@@ -277,6 +277,20 @@ def stage_flops(s):
     return {"angl2proj": a2p, "proj2angl": a2p, "oz": oz, "fft_axis": fft_axis}
 
 
+def read_traffic(kernel):
+    """dram read+write bytes per launch of `kernel` from the committed ncu
+    summary (profiles/dram_traffic_64cubed_mmax3.md), or None."""
+    import re
+    path = os.path.join(ROOT, "profiles", "dram_traffic_64cubed_mmax3.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        m = re.match(r"^\|\s*([a-z0-9_]+)\s*\|\s*(\d+)\s*\|", line)
+        if m and m.group(1) == kernel:
+            return int(m.group(2))
+    return None
+
+
 def cpu_round_trip_rate(seconds_target=12.0, max_reps=20):
     """The oracle's round trip on this host's cores: (applies/s, reps, cores)."""
     import numpy as np
@@ -435,10 +449,7 @@ def run_ours(args):
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
     achieved = b_launch / t_launch / 1e9
-    traffic = None
-    tr_path = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tr_path):
-        traffic = json.load(open(tr_path)).get(dom)
+    traffic = read_traffic(dom)
     fp64_peak = fp64_peak_tflops()
     fl = stage_flops(s)
     fl_launch = fl[dom]
