@@ -148,6 +148,23 @@ int mdft_get_delta_f(const void* xi, const void* vexc, const double* w,
                      double rho0, double prefactor, int precision,
                      void* stream);
 
+/* get_delta_f for callers that cannot allocate device memory while they run
+ * (an application that gives the whole GPU to its own pool allocator up
+ * front and forbids allocations behind its back, or a loop that must not
+ * pay for an allocation call).  No counterpart in the reference: it is the
+ * same computation as mdft_get_delta_f, but its per-CTA partial sums live in
+ * one fixed 1 MiB array of the library's device memory (held on every GPU
+ * that loads the library until exit) instead of a stream-ordered temporary;
+ * it calls no allocation routine.  Limit: nxyz <= 2,097,152 grid points
+ * (128^3); larger grids return MDFT_ERR_UNSUPPORTED.  All calls share the
+ * array, so calls that overlap on the GPU race and must be serialised by the
+ * caller.  The first call on a device looks up the array's address for that
+ * device; make it before any stream capture. */
+int mdft_get_delta_f_noalloc(const void* xi, const void* vexc, const double* w,
+                             void* delta_f, double* ff_dev, size_t nxyz, int no,
+                             double rho0, double prefactor, int precision,
+                             void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -49,6 +49,7 @@ SIGNATURES = {
     "mdft_conv_mnmunukhi_q": (i32, [vp, dp]),
     "mdft_get_delta_rho": (i32, [vp, vp, sz, f64, i32, vp]),
     "mdft_get_delta_f": (i32, [vp, vp, vp, vp, vp, sz, i32, f64, f64, i32, vp]),
+    "mdft_get_delta_f_noalloc": (i32, [vp, vp, vp, vp, vp, sz, i32, f64, f64, i32, vp]),
 }
 
 

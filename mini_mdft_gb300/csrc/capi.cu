@@ -70,6 +70,11 @@ std::vector<T> cast_vec(const std::vector<double>& v) {
 
 }  // namespace
 
+int mdft::record_error(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
 struct mdft_grid_s {
   mdft::Grid g;
   explicit mdft_grid_s(const mdft::Grid& gg) : g(gg) {}

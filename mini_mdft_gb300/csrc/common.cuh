@@ -189,6 +189,10 @@ void launch_delta_rho(const T* xi, T* dr, size_t n, double rho0, cudaStream_t s)
 // partials: >= delta_f_partials(nxyz) double2 entries + one uint counter
 // (zeroed by the caller before the first use; the kernel leaves it zero).
 size_t delta_f_partials(size_t nxyz, int no);
+// Stores `msg` as the calling thread's mdft_last_error() text and returns
+// `code` (for extern "C" entry points defined outside capi.cu).
+int record_error(int code, const std::string& msg);
+
 template <typename T>
 void launch_delta_f(const T* xi, const T* vexc, const double* w, T* df,
                     double* ff, size_t nxyz, int no, double rho0,

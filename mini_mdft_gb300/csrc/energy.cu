@@ -7,6 +7,9 @@
 // compensated (two-sum) arithmetic.  The tile sums go to a small partials
 // array; the last CTA to finish adds them in a fixed order, so ff is
 // deterministic and independent of scheduling.
+#include <mutex>
+#include <string>
+
 #include "common.cuh"
 
 namespace mdft {
@@ -145,4 +148,89 @@ template void launch_delta_f<double>(const double*, const double*, const double*
 template void launch_delta_f<float>(const float*, const float*, const double*, float*, double*,
                                     size_t, int, double, double, void*, cudaStream_t);
 
+
+// ---------------------------------------------------------------------------
+// get_delta_f without any device allocation.
+//
+// Some callers of this library cannot allocate device memory while they run
+// the solve: an application that hands the whole GPU to its own pool
+// allocator up front (as Kokkos-based codes often do) and treats any
+// cudaMalloc behind its back as a budget violation, or a time-critical loop
+// that must not pay for, or serialise on, an allocation call.  For them
+// mdft_get_delta_f_noalloc runs the same reduction as mdft_get_delta_f with
+// its per-CTA partial sums kept in one fixed array in the library's own
+// device memory instead of a stream-ordered temporary.
+//
+// The array holds kNoAllocMaxPartials partials (one per 32 grid points), so
+// grids of up to 2,097,152 points (128^3) are accepted and larger ones are
+// rejected with an error; it costs 1 MiB of device memory on every GPU that
+// loads the library, held until the process exits.  All calls share it and
+// it keeps the last call's contents, so calls that overlap on the GPU (on
+// different streams, or from different threads) race and must be ordered by
+// the caller.  The completion counter is cleared on the caller's stream at
+// the start of every call.  The first call on a device looks up the array's
+// device address (cudaGetSymbolAddress) for that device and caches it; make
+// that first call before any stream capture.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr size_t kNoAllocMaxPartials = size_t(1) << 16;
+constexpr size_t kNoAllocBytes = kNoAllocMaxPartials * sizeof(double2) + 256;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kMaxDevices] = {nullptr};
+
+// Device address of g_noalloc_scratch on the current device, looked up once
+// per device with that device current.
+void* noalloc_scratch_for_current_device() {
+  int dev = 0;
+  cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  throw_if(dev < 0 || dev >= kMaxDevices, "device index out of range for the fixed scratch table");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* ptr = nullptr;
+    cuda_check(cudaGetSymbolAddress(&ptr, g_noalloc_scratch), "cudaGetSymbolAddress(fixed scratch)");
+    throw_if(ptr == nullptr, "cudaGetSymbolAddress returned a null scratch address", 2);
+    g_noalloc_ptr[dev] = ptr;
+  }
+  return g_noalloc_ptr[dev];
+}
+}  // namespace
+
 }  // namespace mdft
+
+extern "C" int mdft_get_delta_f_noalloc(const void* xi, const void* vexc, const double* w,
+                                        void* delta_f, double* ff_dev, size_t nxyz, int no,
+                                        double rho0, double prefactor, int precision,
+                                        void* stream) {
+  using namespace mdft;
+  try {
+    throw_if(precision != 0 && precision != 1, "precision must be MDFT_F64 or MDFT_F32");
+    throw_if(no <= 0, "angular grid size must be positive");
+    throw_if(!ff_dev, "NULL argument");
+    throw_if(nxyz > 0 && (!xi || !vexc || !w || !delta_f), "NULL argument");
+    const size_t nb = delta_f_partials(nxyz, no);
+    throw_if(nb > kNoAllocMaxPartials,
+             "mdft_get_delta_f_noalloc: " + std::to_string(nxyz) +
+                 " grid points exceed the fixed scratch limit of " +
+                 std::to_string(kNoAllocMaxPartials * 32) + " points",
+             4);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    unsigned char* scratch = static_cast<unsigned char*>(noalloc_scratch_for_current_device());
+    // partials first, then the completion counter, which must start at zero
+    unsigned char* counter = scratch + sizeof(double2) * nb;
+    cuda_check(cudaMemsetAsync(counter, 0, sizeof(unsigned), s), "cudaMemsetAsync(fixed scratch counter)");
+    if (precision == 0)
+      launch_delta_f<double>(static_cast<const double*>(xi), static_cast<const double*>(vexc), w,
+                             static_cast<double*>(delta_f), ff_dev, nxyz, no, rho0, prefactor, scratch, s);
+    else
+      launch_delta_f<float>(static_cast<const float*>(xi), static_cast<const float*>(vexc), w,
+                            static_cast<float*>(delta_f), ff_dev, nxyz, no, rho0, prefactor, scratch, s);
+    return 0;
+  } catch (const Error& e) {
+    return record_error(e.code, e.what());
+  } catch (const std::exception& e) {
+    return record_error(1, e.what());
+  }
+}

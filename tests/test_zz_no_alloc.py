@@ -1,0 +1,77 @@
+"""mdft_get_delta_f_noalloc: the energy/gradient reduction for callers that
+cannot allocate device memory during their solve (e.g. an application whose
+pool allocator owns the whole GPU, or a loop that must not pay for an
+allocation call).  Its scratch is a fixed array inside the library, so it
+must give what mdft_get_delta_f gives, call after call.
+
+Collected last (file name) so that a run stopping at the first failure has
+run every other test first.  Calls go straight through the C ABI."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+MAX_POINTS = 1 << 21  # 2,097,152 grid points (128^3): the fixed scratch limit
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr())
+
+
+def _run(L, fn, xi, vexc, w, df, ff, prec, stream):
+    no = w.numel()
+    rc = fn(_ptr(xi), _ptr(vexc), _ptr(w), _ptr(df), _ptr(ff), xi.numel() // no, no,
+            0.000424, -15.7, prec, stream)
+    return rc
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_noalloc_matches_allocating_entry_point_twice(gpu_lib, prec):
+    import torch
+    L = gpu_lib.lib()
+    dt = torch.float64 if prec == 0 else torch.float32
+    rng = np.random.default_rng(2024)
+    shape = (40, 40, 40, 84)
+    xi = torch.from_numpy(rng.uniform(0.9, 1.1, shape)).to("cuda", dt)
+    vexc = torch.from_numpy(rng.uniform(-1.0, 1.0, shape)).to("cuda", dt)
+    w = torch.from_numpy(rng.uniform(0.0, 1.0, 84)).to("cuda", torch.float64)
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    df_ref = torch.zeros_like(xi)
+    ff_ref = torch.zeros(1, dtype=torch.float64, device="cuda")
+    assert _run(L, L.mdft_get_delta_f, xi, vexc, w, df_ref, ff_ref, prec, stream) == 0
+
+    for _ in range(2):  # two calls in a row share the fixed scratch
+        df = torch.full_like(xi, 7.0)
+        ff = torch.full((1,), 7.0, dtype=torch.float64, device="cuda")
+        assert _run(L, L.mdft_get_delta_f_noalloc, xi, vexc, w, df, ff, prec, stream) == 0, \
+            L.mdft_last_error()
+        torch.cuda.synchronize()
+        assert torch.equal(df, df_ref)
+        a, b = float(ff.item()), float(ff_ref.item())
+        assert abs(a - b) <= 1e-12 * abs(b)
+
+
+def test_noalloc_rejects_grids_beyond_the_limit(gpu_lib):
+    import torch
+    L = gpu_lib.lib()
+    no = 1
+    n = MAX_POINTS + 1
+    xi = torch.ones(n, dtype=torch.float64, device="cuda")
+    vexc = torch.ones(n, dtype=torch.float64, device="cuda")
+    w = torch.ones(no, dtype=torch.float64, device="cuda")
+    df = torch.zeros(n, dtype=torch.float64, device="cuda")
+    ff = torch.zeros(1, dtype=torch.float64, device="cuda")
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    rc = L.mdft_get_delta_f_noalloc(_ptr(xi), _ptr(vexc), _ptr(w), _ptr(df), _ptr(ff), n, no,
+                                    0.3, 0.3, 0, stream)
+    assert rc == 4
+    assert b"fixed scratch limit" in L.mdft_last_error()
+    # the largest accepted grid still runs
+    rc = L.mdft_get_delta_f_noalloc(_ptr(xi), _ptr(vexc), _ptr(w), _ptr(df), _ptr(ff),
+                                    MAX_POINTS, no, 0.3, 0.3, 0, stream)
+    assert rc == 0, L.mdft_last_error()
+    torch.cuda.synchronize()
+    assert float(ff.item()) == 0.0  # xi = 1 -> xi^2 - 1 = 0
