@@ -271,7 +271,8 @@ def stage_flops(s):
     nrec = sum(2 * l * l + 2 * l + 1 for l in range(2, mmax + 1))
     a2p = N * (nt * nphi * K1 * (npsi * 2) + nt * nphi * K1 * nphi * 8 + np_ * nt * 4)
     npairs = N // 2 + 4
-    oz = npairs * (4 * srot * 8 + s["np_new"] * 22 + nrec * 20)
+    # R(q) comes from the per-plan table, so the recursion is not per-apply work
+    oz = npairs * (4 * srot * 8 + s["np_new"] * 22)
     n = WORKLOAD["n"][0]
     fft_axis = N * np_ // n * 5 * n * math.log2(n)
     return {"angl2proj": a2p, "proj2angl": a2p, "oz": oz, "fft_axis": fft_axis}

@@ -98,6 +98,7 @@ struct mdft_conv_s {
   std::vector<int> pair_list;                 // reference order (getter)
   std::vector<std::complex<double>> mnq;      // (np_new, nq) (getter)
   DevBuf pairs, kx, ky, kz, rot, pmap, ip_m, ip_mup, ip_mu2, ia_map, ctab, tw_x, tw_y, tw_z;
+  DevBuf pinfo, palpha, ia_start, rtab;  // lane-per-pair OZ path
   mdft::OzPlan oz{};
   mdft::FftAxis ax{}, ay{}, az{};
   explicit mdft_conv_s(const mdft::Grid& gg) : g(gg) {}
@@ -233,6 +234,48 @@ void conv_build(mdft_conv_s* h, const mdft::LucTable& t) {
   O.ia_map = h->ia_map.as<int>();
   O.ctab = h->ctab.ptr;
   mdft::oz_plan_finish<T>(O);
+  if (O.lane_path) {
+    // Per-pair geometry of the lane path, in the sorted pair order: linear
+    // indices of q and -q, the c(q) row iq and weight alpha of
+    // MDFT_Convolution.hpp:449-455 (FP64, host, no contraction), and the
+    // singular mid-k flag of :507-509.
+    O.npairs_pad = ((long long)h->npairs + 31) / 32 * 32;
+    O.nR = (g.mmax + 1) * (2 * g.mmax + 1) * (2 * g.mmax + 3) / 3;
+    std::vector<int4> info((size_t)O.npairs_pad, make_int4(0, 0, 0, 0));
+    std::vector<T> alpha((size_t)O.npairs_pad, T(0));
+    for (int i = 0; i < h->npairs; ++i) {
+      const int ix = pr[i].x, iy = pr[i].y, iz = pr[i].z;
+      const int ixm = ix == 0 ? 0 : g.nx - ix, iym = iy == 0 ? 0 : g.ny - iy, izm = iz == 0 ? 0 : g.nz - iz;
+      const double q[3] = {g.kx[ix], g.ky[iy], g.kz[iz]};
+      double s2 = 0;
+      for (int k = 0; k < 3; ++k) s2 += q[k] * q[k];
+      const double eiq = std::sqrt(s2) / t.dq;
+      const int iq = std::min((int)eiq, need - 2);
+      const bool qeq = (ixm == ix && iym == iy && izm == iz);
+      const bool sing = qeq && (ix == g.nx / 2 || iy == g.ny / 2 || iz == g.nz / 2);
+      info[i] = make_int4((int)(((long long)ix * g.ny + iy) * g.nz + iz),
+                          (int)(((long long)ixm * g.ny + iym) * g.nz + izm), iq, sing ? 1 : 0);
+      alpha[i] = (T)(eiq - (double)iq);
+    }
+    h->pinfo.upload(info.data(), sizeof(int4) * info.size());
+    h->palpha.upload(alpha.data(), sizeof(T) * alpha.size());
+    // first OZ coefficient of each projection (the ia_map enumeration order,
+    // MDFT_Convolution.hpp:186-195)
+    std::vector<int> ia0(g.np);
+    {
+      int ia = 0;
+      for (int ip = 0; ip < g.np; ++ip) {
+        ia0[ip] = ia;
+        for (int in = std::abs(g.mup[ip]); in <= g.mmax; ++in) ia += 2 * (in / g.mrso) + 1;
+      }
+    }
+    h->ia_start.upload(ia0.data(), sizeof(int) * ia0.size());
+    O.pinfo = h->pinfo.as<int4>();
+    O.palpha = h->palpha.ptr;
+    O.ia_start = h->ia_start.as<int>();
+    mdft::oz_build_rtab<T>(O, h->rtab);
+    O.rtab = h->rtab.ptr;
+  }
   const long long N = g.N(), np = g.np;
   fft_axis_build<T>(h->az, h->tw_z, g.nz, 1, np * g.nx * g.ny);
   fft_axis_build<T>(h->ay, h->tw_y, g.ny, g.nz, np * g.nx * (long long)g.nz);

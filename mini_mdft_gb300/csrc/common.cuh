@@ -175,9 +175,20 @@ struct OzPlan {
   const void* ctab;        // (nq, np_new) Cx<T>, transposed mnmunukhi_q
   int warps_per_cta;
   size_t smem;
+  // Lane-per-pair path: per-pair geometry computed once at plan creation.
+  int lane_path;           // 1: oz_lane_kernel, 0: warp-per-pair fallback
+  long long npairs_pad;    // npairs rounded up to a multiple of 32
+  int nR;                  // compact R entries per pair: sum_l (2l+1)^2
+  const int4* pinfo;       // (npairs_pad) lq, lmq, iq, singular (padding: zeros)
+  const void* palpha;      // (npairs_pad) T interpolation weight of row iq+1
+  const int* ia_start;     // (np) first OZ coefficient of each projection
+  const void* rtab;        // (npairs_pad/32, nR, 32) Cx<T>: R(q) of 32 pairs, lane fastest
 };
 template <typename T>
 void oz_plan_finish(OzPlan& P);
+// Fills the R(q) table of the lane path (FP64 recursion, stored as T).
+template <typename T>
+void oz_build_rtab(const OzPlan& P, DevBuf& rtab);
 template <typename T>
 void launch_oz(const OzPlan& P, Cx<T>* p, cudaStream_t s);
 

@@ -26,8 +26,8 @@ namespace {
 
 constexpr int kRotL5 = 5, kRotM13 = 13;  // RotationCoeffs extents (l-2, m+6)
 
-__host__ __device__ inline int roff(int l) { return l * (2 * l - 1) * (2 * l + 1) / 3; }
-__host__ __device__ inline int nrot(int mmax) { return roff(mmax + 1); }
+__host__ __device__ constexpr int roff(int l) { return l * (2 * l - 1) * (2 * l + 1) / 3; }
+__host__ __device__ constexpr int nrot(int mmax) { return roff(mmax + 1); }
 
 template <typename T>
 struct OzSmem {
@@ -294,10 +294,315 @@ oz_kernel(const OzPlan P, Cx<T>* __restrict__ p) {
 #undef DD
 }
 
+// ---------------------------------------------------------------------------
+// Lane-per-pair path.
+//
+// R(q) depends only on the grid, so it is computed once per plan by
+// rot_table_kernel (the same FP64 l-recursion, one thread per pair) into a
+// resident table laid out (pair block of 32, entry, lane): 32 consecutive
+// pairs read each entry as one coalesced 32-wide access.  oz_lane_kernel then
+// gives every lane its own pair.  All pairs run the identical instruction
+// stream (same mmax, same maps), so no lane idles or diverges; each lane
+// keeps its rotated projections in its own column of shared memory
+// ([projection][lane], conflict-free), and the OZ output of each (m, mu2)
+// block is rotated back from registers and stored straight to HBM.
+// ---------------------------------------------------------------------------
+
+// Strided view of one pair's compact R entries.
+struct RView {
+  Cx<double>* base;
+  long long stride;
+  __device__ Cx<double>& operator[](int e) const { return base[(long long)e * stride]; }
+};
+
+// rotation_matrix_between_complex_spherical_harmonics_lu
+// (common/MDFT_Rotation.hpp:103-283), sequential, FP64.
+__device__ void rot_recursion(double q0, double q1, double q2, int mmax, const double* A,
+                              const double* B, const double* Cc, const double* D, const RView& R) {
+  constexpr int mm = 6;
+#define RI(l, m, m1) (roff(l) + ((m) + (l)) * (2 * (l) + 1) + ((m1) + (l)))
+#define AA(l, i, j) A[((l)*kRotM13 + (i)) * kRotM13 + (j)]
+#define BB(l, i, j) B[((l)*kRotM13 + (i)) * kRotM13 + (j)]
+#define CC(l, i) Cc[(l)*kRotM13 + (i)]
+#define DD(l, i) D[(l)*kRotM13 + (i)]
+  R[0] = mkc<double>(1.0, 0.0);
+  double r2[3], r1[3], r0[3];
+  if (q0 == 0.0 && q1 == 0.0 && q2 == 0.0) {
+    r2[0] = 0.0;
+    r2[1] = 0.0;
+    r2[2] = 1.0;
+  } else {
+    r2[0] = q0;
+    r2[1] = q1;
+    r2[2] = q2;
+  }
+  if (r2[0] != 0.0 || r2[1] != 0.0) {
+    r1[0] = 0.0 * r2[2] - 1.0 * r2[1];
+    r1[1] = 1.0 * r2[0] - 0.0 * r2[2];
+    r1[2] = 0.0 * r2[1] - 0.0 * r2[0];
+  } else {
+    r1[0] = r2[1] * 0.0 - r2[2] * 0.0;
+    r1[1] = r2[2] * 1.0 - r2[0] * 0.0;
+    r1[2] = r2[0] * 0.0 - r2[1] * 1.0;
+  }
+  const double n2v = sqrt(r2[0] * r2[0] + r2[1] * r2[1] + r2[2] * r2[2]);
+  for (int i = 0; i < 3; ++i) r2[i] = r2[i] / n2v;
+  const double n1v = sqrt(r1[0] * r1[0] + r1[1] * r1[1] + r1[2] * r1[2]);
+  for (int i = 0; i < 3; ++i) r1[i] = r1[i] / n1v;
+  r0[0] = r1[1] * r2[2] - r1[2] * r2[1];
+  r0[1] = r1[2] * r2[0] - r1[0] * r2[2];
+  r0[2] = r1[0] * r2[1] - r1[1] * r2[0];
+  const double is2 = 1.0 / sqrt(2.0);
+  R[RI(1, -1, -1)] = mkc<double>((r1[1] + r0[0]) * 0.5, (r0[1] - r1[0]) * 0.5);
+  R[RI(1, -1, 0)] = mkc<double>(r2[0] * is2, r2[1] * is2);
+  R[RI(1, -1, 1)] = mkc<double>((r1[1] - r0[0]) * 0.5, (-r0[1] - r1[0]) * 0.5);
+  R[RI(1, 0, -1)] = mkc<double>(r0[2] * is2, -r1[2] * is2);
+  R[RI(1, 0, 0)] = mkc<double>(r2[2], 0.0);
+  R[RI(1, 0, 1)] = mkc<double>(-r0[2] * is2, -r1[2] * is2);
+  R[RI(1, 1, -1)] = mkc<double>((r1[1] - r0[0]) * 0.5, (r0[1] + r1[0]) * 0.5);
+  R[RI(1, 1, 0)] = mkc<double>(-r2[0] * is2, r2[1] * is2);
+  R[RI(1, 1, 1)] = mkc<double>((r1[1] + r0[0]) * 0.5, (r1[0] - r0[1]) * 0.5);
+  const Cx<double> R1m0 = R[RI(1, -1, 0)], R1z0 = R[RI(1, 0, 0)], R1p0 = R[RI(1, 1, 0)];
+  const Cx<double> R1m1 = R[RI(1, -1, 1)], R1z1 = R[RI(1, 0, 1)], R1p1 = R[RI(1, 1, 1)];
+  for (int l = 2; l <= mmax; ++l) {
+    const int l1 = l - 1;
+    for (int m = -l; m <= l; ++m) {
+      const int m1min = m > 0 ? 1 : 0;
+      for (int m1 = m1min; m1 <= l; ++m1) {
+        double f, g;
+        if (m1 <= l - 1) {
+          if (m == -l) {
+            const double bt = BB(l - 2, mm - m, mm + m1);
+            const Cx<double> a = R1m0, b = R[RI(l1, m + 1, m1)];
+            f = bt * (a.re * b.re - a.im * b.im);
+            g = bt * (a.re * b.im + a.im * b.re);
+          } else if (m == l) {
+            const double bt = BB(l - 2, mm + m, mm + m1);
+            const Cx<double> a = R1p0, b = R[RI(l1, m - 1, m1)];
+            f = bt * (a.re * b.re - a.im * b.im);
+            g = bt * (a.re * b.im + a.im * b.re);
+          } else {
+            const double at = AA(l - 2, mm + m, mm + m1);
+            const double bp = BB(l - 2, mm + m, mm + m1);
+            const double bn = BB(l - 2, mm - m, mm + m1);
+            const Cx<double> Rm0 = R[RI(l1, m, m1)];
+            const Cx<double> Rm1 = (m + 1 <= l1) ? R[RI(l1, m + 1, m1)] : mkc<double>(0, 0);
+            const Cx<double> Rm2 = (m - 1 >= -l1) ? R[RI(l1, m - 1, m1)] : mkc<double>(0, 0);
+            f = at * (R1z0.re * Rm0.re) + bp * (R1p0.re * Rm2.re - R1p0.im * Rm2.im) +
+                bn * (R1m0.re * Rm1.re - R1m0.im * Rm1.im);
+            g = at * (R1z0.re * Rm0.im) + bp * (R1p0.re * Rm2.im + R1p0.im * Rm2.re) +
+                bn * (R1m0.re * Rm1.im + R1m0.im * Rm1.re);
+          }
+        } else {
+          if (m == -l) {
+            const double dt = DD(l - 2, mm - m);
+            const Cx<double> a = R1m1, b = R[RI(l1, m + 1, m1 - 1)];
+            f = dt * (a.re * b.re - a.im * b.im);
+            g = dt * (a.re * b.im + a.im * b.re);
+          } else if (m == l) {
+            const double dt = DD(l - 2, mm + m);
+            const Cx<double> a = R1p1, b = R[RI(l1, m - 1, m1 - 1)];
+            f = dt * (a.re * b.re - a.im * b.im);
+            g = dt * (a.re * b.im + a.im * b.re);
+          } else {
+            const double ct = CC(l - 2, mm + m);
+            const double dp = DD(l - 2, mm + m);
+            const double dn = DD(l - 2, mm - m);
+            const Cx<double> Rm0 = R[RI(l1, m, m1 - 1)];
+            const Cx<double> Rm1 = (m + 1 <= l1) ? R[RI(l1, m + 1, m1 - 1)] : mkc<double>(0, 0);
+            const Cx<double> Rm2 = (m - 1 >= -l1) ? R[RI(l1, m - 1, m1 - 1)] : mkc<double>(0, 0);
+            f = ct * (R1z1.re * Rm0.re - R1z1.im * Rm0.im) + dp * (R1p1.re * Rm2.re - R1p1.im * Rm2.im) +
+                dn * (R1m1.re * Rm1.re - R1m1.im * Rm1.im);
+            g = ct * (R1z1.re * Rm0.im + R1z1.im * Rm0.re) + dp * (R1p1.re * Rm2.im + R1p1.im * Rm2.re) +
+                dn * (R1m1.re * Rm1.im + R1m1.im * Rm1.re);
+          }
+        }
+        R[RI(l, m, m1)] = mkc<double>(f, g);
+        const double pw = ((m + m1) & 1) ? -1.0 : 1.0;
+        R[RI(l, -m, -m1)] = mkc<double>(pw * f, -pw * g);
+      }
+    }
+  }
+#undef RI
+#undef AA
+#undef BB
+#undef CC
+#undef DD
+}
+
+// One thread per (padded) pair: R(q) in FP64 straight into the table layout.
+__global__ void rot_table_kernel(const OzPlan P, Cx<double>* __restrict__ rt64) {
+  const long long pair = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (pair >= P.npairs_pad) return;
+  double q0 = 0, q1 = 0, q2 = 0;
+  if (pair < P.npairs) {
+    const int4 pr = P.pairs[pair];
+    q0 = P.kx[pr.x];
+    q1 = P.ky[pr.y];
+    q2 = P.kz[pr.z];
+  }
+  const double* A = P.rot;
+  const double* B = A + kRotL5 * kRotM13 * kRotM13;
+  const double* Cc = B + kRotL5 * kRotM13 * kRotM13;
+  const double* D = Cc + kRotL5 * kRotM13;
+  const long long blk = pair >> 5, lane = pair & 31;
+  RView R{rt64 + blk * (long long)P.nR * 32 + lane, 32};
+  rot_recursion(q0, q1, q2, P.mmax, A, B, Cc, D, R);
+}
+
+__global__ void rot_table_to_f32(const Cx<double>* __restrict__ a, Cx<float>* __restrict__ b, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    b[i] = mkc<float>((float)a[i].re, (float)a[i].im);
+}
+
+// Projection index of (m, mup, mu2) in OrientationProjectionMap order
+// (m outer, mup, mu2 inner).
+struct PIndex {
+  int base[8];
+  int mrso;
+  __device__ __forceinline__ int operator()(int m, int mup, int mu2) const {
+    return base[m] + (mup + m) * (m / mrso + 1) + mu2;
+  }
+};
+
+template <typename T, int MMAX>
+__global__ void __launch_bounds__(256)
+oz_lane_kernel(const OzPlan P, Cx<T>* __restrict__ p) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const long long blk = (long long)blockIdx.x * P.warps_per_cta + wib;
+  if (blk * 32 >= P.npairs) return;  // whole warp exits together
+  const long long pair = blk * 32 + lane;
+  const bool valid = pair < P.npairs;
+  const int np = P.np, mrso = P.mrso;
+  Cx<T>* Dq = reinterpret_cast<Cx<T>*>(sm + (size_t)wib * 2 * np * 32 * sizeof(Cx<T>));
+  Cx<T>* Dmq = Dq + (size_t)np * 32;
+  PIndex ipx;
+  ipx.mrso = mrso;
+  {
+    int b = 0;
+#pragma unroll
+    for (int m = 0; m <= MMAX; ++m) {
+      ipx.base[m] = b;
+      b += (2 * m + 1) * (m / mrso + 1);
+    }
+  }
+  const int4 info = P.pinfo[pair];
+  const long long N = P.N, lq = info.x, lmq = info.y;
+  const Cx<T>* Rt = static_cast<const Cx<T>*>(P.rtab) + blk * (long long)P.nR * 32 + lane;
+#define RT(l, m, m1) Rt[(roff(l) + ((m) + (l)) * (2 * (l) + 1) + ((m1) + (l))) * 32]
+
+  // rotation to the q frame (MDFT_Convolution.hpp:427-443), block by block
+#pragma unroll
+  for (int m = 0; m <= MMAX; ++m) {
+    for (int mu2 = 0; mu2 <= m / mrso; ++mu2) {
+      Cx<T> gq[2 * MMAX + 1], gmq[2 * MMAX + 1];
+#pragma unroll
+      for (int a = 0; a <= 2 * m; ++a) {
+        const long long off = (long long)ipx(m, a - m, mu2) * N;
+        gq[a] = p[off + lq];
+        gmq[a] = p[off + lmq];
+      }
+#pragma unroll 1
+      for (int k = -m; k <= m; ++k) {
+        Cx<T> x = mkc<T>(0, 0), y = mkc<T>(0, 0);
+#pragma unroll
+        for (int a = 0; a <= 2 * m; ++a) {
+          x = cmac(x, gq[a], RT(m, a - m, k));
+          y = cmac(y, gmq[a], RT(m, a - m, -k));
+        }
+        const int j = ipx(m, k, mu2) * 32 + lane;
+        Dq[j] = x;
+        Dmq[j] = (m & 1) ? mkc<T>(-y.re, -y.im) : y;
+      }
+    }
+  }
+  // OZ with c(|q|) interpolated on the fly (:449-496), chop (:514-517),
+  // rotation back (:518-536) and the stores (:538-541)
+  const int iq = info.z;
+  const bool singular = info.w != 0;
+  const T alpha = static_cast<const T*>(P.palpha)[pair];
+  const T beta = T(1) - alpha;
+  const Cx<T>* clo = static_cast<const Cx<T>*>(P.ctab) + (size_t)iq * P.np_new;
+  const Cx<T>* chi = clo + P.np_new;
+#pragma unroll
+  for (int m = 0; m <= MMAX; ++m) {
+    for (int mu2 = 0; mu2 <= m / mrso; ++mu2) {
+      Cx<T> gq[2 * MMAX + 1], gmq[2 * MMAX + 1];
+#pragma unroll
+      for (int k = -m; k <= m; ++k) {
+        int ia = P.ia_start[ipx(m, k, mu2)];
+        Cx<T> sq = mkc<T>(0, 0), smq = mkc<T>(0, 0);
+#pragma unroll
+        for (int n = (k < 0 ? -k : k); n <= MMAX; ++n) {
+          const int nn = n / mrso;
+          for (int nu2 = -nn; nu2 <= nn; ++nu2, ++ia) {
+            const Cx<T> h = chi[ia], lo = clo[ia];
+            const Cx<T> c = mkc<T>(alpha * h.re + beta * lo.re, alpha * h.im + beta * lo.im);
+            if (nu2 < 0) {
+              const int j = ipx(n, k, -nu2) * 32 + lane;
+              sq = cmac(sq, c, Dq[j]);
+              smq = cmac(smq, c, Dmq[j]);
+            } else {
+              const int j = ipx(n, k, nu2) * 32 + lane;
+              sq = cmac(sq, c, conj(Dmq[j]));
+              smq = cmac(smq, c, conj(Dq[j]));
+            }
+          }
+        }
+        gq[k + m] = chop(sq);
+        gmq[k + m] = chop(smq);
+      }
+#pragma unroll 1
+      for (int a = -m; a <= m; ++a) {
+        Cx<T> x = mkc<T>(0, 0), y = mkc<T>(0, 0);
+#pragma unroll
+        for (int k = -m; k <= m; ++k) {
+          x = cmac(x, gq[k + m], conj(RT(m, a, k)));
+          y = cmac(y, gmq[k + m], conj(RT(m, a, -k)));
+        }
+        if (m & 1) y = mkc<T>(-y.re, -y.im);
+        if (valid) {
+          const long long off = (long long)ipx(m, a, mu2) * N;
+          p[off + lq] = x;
+          p[off + lmq] = singular ? conj(y) : y;
+        }
+      }
+    }
+  }
+#undef RT
+}
+
+constexpr int kLaneMaxMmax = 6;
+
+template <typename T>
+size_t lane_smem_per_warp(int np) {
+  return (size_t)2 * np * 32 * sizeof(Cx<T>);
+}
+
 }  // namespace
 
 template <typename T>
 void oz_plan_finish(OzPlan& P) {
+  // Lane path when one warp's shared columns fit with room for a few warps
+  // per SM; otherwise the warp-per-pair kernel (R computed on the fly).
+  const size_t per_warp = lane_smem_per_warp<T>(P.np);
+  P.lane_path = (P.mmax <= kLaneMaxMmax && per_warp <= 64 * 1024 && P.N < (1LL << 31)) ? 1 : 0;
+  if (P.lane_path) {
+    int w = (int)((200 * 1024) / per_warp);
+    P.warps_per_cta = w < 1 ? 1 : (w > 8 ? 8 : w);
+    P.smem = per_warp * P.warps_per_cta;
+    switch (P.mmax) {
+      case 1: allow_max_smem(oz_lane_kernel<T, 1>, P.smem, "oz smem attribute"); break;
+      case 2: allow_max_smem(oz_lane_kernel<T, 2>, P.smem, "oz smem attribute"); break;
+      case 3: allow_max_smem(oz_lane_kernel<T, 3>, P.smem, "oz smem attribute"); break;
+      case 4: allow_max_smem(oz_lane_kernel<T, 4>, P.smem, "oz smem attribute"); break;
+      case 5: allow_max_smem(oz_lane_kernel<T, 5>, P.smem, "oz smem attribute"); break;
+      case 6: allow_max_smem(oz_lane_kernel<T, 6>, P.smem, "oz smem attribute"); break;
+    }
+    return;
+  }
   const OzSmem<T> L(P.mmax, P.np);
   P.warps_per_cta = 8;
   P.smem = L.per_warp * P.warps_per_cta;
@@ -306,16 +611,53 @@ void oz_plan_finish(OzPlan& P) {
 }
 
 template <typename T>
+void oz_build_rtab(const OzPlan& P, DevBuf& rtab) {
+  const long long n = P.npairs_pad * (long long)P.nR;
+  DevBuf rt64;
+  DevBuf& target64 = sizeof(T) == sizeof(double) ? rtab : rt64;
+  target64.alloc(sizeof(Cx<double>) * (size_t)n);
+  const long long nb = (P.npairs_pad + 127) / 128;
+  clear_stale_error();
+  rot_table_kernel<<<(unsigned)nb, 128>>>(P, target64.as<Cx<double>>());
+  launch_check("R(q) table kernel launch");
+  if (sizeof(T) != sizeof(double)) {
+    rtab.alloc(sizeof(Cx<float>) * (size_t)n);
+    rot_table_to_f32<<<152 * 8, 256>>>(rt64.as<Cx<double>>(), rtab.as<Cx<float>>(), n);
+    launch_check("R(q) table conversion launch");
+  }
+  cuda_check(cudaDeviceSynchronize(), "R(q) table build");
+}
+
+template <typename T>
 void launch_oz(const OzPlan& P, Cx<T>* p, cudaStream_t s) {
   if (P.npairs == 0) return;
-  const long long nb = (P.npairs + P.warps_per_cta - 1) / P.warps_per_cta;
   clear_stale_error();
+  if (P.lane_path) {
+    const long long nblk = P.npairs_pad / 32;
+    const long long nb = (nblk + P.warps_per_cta - 1) / P.warps_per_cta;
+    throw_if(nb > 0x7fffffffLL, "too many k-space pairs", 4);
+    const dim3 grid((unsigned)nb), block(32 * P.warps_per_cta);
+    switch (P.mmax) {
+      case 1: oz_lane_kernel<T, 1><<<grid, block, P.smem, s>>>(P, p); break;
+      case 2: oz_lane_kernel<T, 2><<<grid, block, P.smem, s>>>(P, p); break;
+      case 3: oz_lane_kernel<T, 3><<<grid, block, P.smem, s>>>(P, p); break;
+      case 4: oz_lane_kernel<T, 4><<<grid, block, P.smem, s>>>(P, p); break;
+      case 5: oz_lane_kernel<T, 5><<<grid, block, P.smem, s>>>(P, p); break;
+      case 6: oz_lane_kernel<T, 6><<<grid, block, P.smem, s>>>(P, p); break;
+      default: throw Error(4, "mmax outside the lane kernel's range");
+    }
+    launch_check("oz lane kernel launch");
+    return;
+  }
+  const long long nb = (P.npairs + P.warps_per_cta - 1) / P.warps_per_cta;
   oz_kernel<T><<<(unsigned)nb, 32 * P.warps_per_cta, P.smem, s>>>(P, p);
   launch_check("oz kernel launch");
 }
 
 template void oz_plan_finish<double>(OzPlan&);
 template void oz_plan_finish<float>(OzPlan&);
+template void oz_build_rtab<double>(const OzPlan&, DevBuf&);
+template void oz_build_rtab<float>(const OzPlan&, DevBuf&);
 template void launch_oz<double>(const OzPlan&, Cx<double>*, cudaStream_t);
 template void launch_oz<float>(const OzPlan&, Cx<float>*, cudaStream_t);
 
