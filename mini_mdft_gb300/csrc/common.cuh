@@ -147,6 +147,7 @@ struct FftAxis {
   int radix[kMaxRadices];
   int cols;       // transforms per CTA
   size_t smem;
+  int fixed;      // 1: compile-time-length kernel for n, 0: runtime-radix kernel
   const void* tw;  // (n) Cx<T> : exp(-2 pi i t / n)
 };
 bool fft_factor(int n, FftAxis& a);  // false if n has a prime factor > 13

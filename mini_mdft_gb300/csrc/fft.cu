@@ -158,10 +158,267 @@ fft_axis_kernel(const FftAxis A, Cx<T>* __restrict__ data, int sign) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Compile-time-length kernels for the grid sizes of the workloads
+// (16..256 with radices 4, 2, 3, 5).  The radix schedule, the tile width and
+// every index stride are compile-time constants, so the butterflies stay in
+// registers and no runtime division is left in the loops.  Tiles are stored
+// [element][column] with one column of padding, which keeps both the
+// contiguous z-axis load and the column-wise butterflies bank-conflict-free.
+// ---------------------------------------------------------------------------
+template <int... Rs>
+struct RList {};
+template <int N>
+struct FftRadices;
+template <> struct FftRadices<16> { using type = RList<4, 4>; };
+template <> struct FftRadices<32> { using type = RList<4, 4, 2>; };
+template <> struct FftRadices<64> { using type = RList<4, 4, 4>; };
+template <> struct FftRadices<128> { using type = RList<4, 4, 4, 2>; };
+template <> struct FftRadices<256> { using type = RList<4, 4, 4, 4>; };
+template <> struct FftRadices<48> { using type = RList<4, 4, 3>; };
+template <> struct FftRadices<96> { using type = RList<4, 4, 2, 3>; };
+template <> struct FftRadices<192> { using type = RList<4, 4, 4, 3>; };
+template <> struct FftRadices<80> { using type = RList<4, 4, 5>; };
+template <> struct FftRadices<160> { using type = RList<4, 4, 2, 5>; };
+
+template <typename T, bool FWD>
+__device__ __forceinline__ Cx<T> tw_at(const Cx<T>* tw, int idx) {
+  Cx<T> t = tw[idx];
+  if (!FWD) t.im = -t.im;
+  return t;
+}
+
+// DFT of length R (2, 3, 4, 5) on registers.
+template <typename T, int R, bool FWD>
+__device__ __forceinline__ void dft_small(Cx<T>* v, const Cx<T>* tw, int n) {
+  if constexpr (R == 2) {
+    const Cx<T> a = v[0], b = v[1];
+    v[0] = a + b;
+    v[1] = a - b;
+  } else if constexpr (R == 4) {
+    const Cx<T> a0 = v[0] + v[2], a1 = v[0] - v[2];
+    const Cx<T> b0 = v[1] + v[3], b1 = v[1] - v[3];
+    const Cx<T> jb = FWD ? mkc<T>(b1.im, -b1.re) : mkc<T>(-b1.im, b1.re);
+    v[0] = a0 + b0;
+    v[1] = a1 + jb;
+    v[2] = a0 - b0;
+    v[3] = a1 - jb;
+  } else if constexpr (R == 3) {
+    const T s3 = T(0.86602540378443864676372317075293618);
+    const Cx<T> a = v[0], b = v[1], c = v[2];
+    const Cx<T> bc = b + c;
+    const Cx<T> t = mkc<T>(a.re - T(0.5) * bc.re, a.im - T(0.5) * bc.im);
+    const Cx<T> u = mkc<T>(s3 * (b.re - c.re), s3 * (b.im - c.im));
+    v[0] = a + bc;
+    if (FWD) {
+      v[1] = mkc<T>(t.re + u.im, t.im - u.re);
+      v[2] = mkc<T>(t.re - u.im, t.im + u.re);
+    } else {
+      v[1] = mkc<T>(t.re - u.im, t.im + u.re);
+      v[2] = mkc<T>(t.re + u.im, t.im - u.re);
+    }
+  } else {
+    static_assert(R == 5, "radix");
+    Cx<T> out[5];
+    const int step = n / 5;
+#pragma unroll
+    for (int s = 0; s < 5; ++s) {
+      Cx<T> acc = v[0];
+#pragma unroll
+      for (int q = 1; q < 5; ++q) acc = cmac(acc, v[q], tw_at<T, FWD>(tw, ((q * s) % 5) * step));
+      out[s] = acc;
+    }
+#pragma unroll
+    for (int s = 0; s < 5; ++s) v[s] = out[s];
+  }
+}
+
+template <typename T, int N, int LD, bool FWD, int Ns>
+__device__ __forceinline__ Cx<T>* stages(Cx<T>* in, Cx<T>* out, const Cx<T>* tw, int cols, int cc,
+                                         RList<>) {
+  return in;
+}
+
+template <typename T, int N, int LD, bool FWD, int Ns, int R, int... Rest>
+__device__ __forceinline__ Cx<T>* stages(Cx<T>* in, Cx<T>* out, const Cx<T>* tw, int cols, int cc,
+                                         RList<R, Rest...>) {
+  constexpr int NR = N / R;
+  constexpr int TWS = N / (Ns * R);
+  __syncthreads();
+  for (int w = threadIdx.x; w < NR * cols; w += blockDim.x) {
+    const int c = w % cols, j = w / cols;
+    if (c < cc) {
+      const int k = j % Ns;
+      Cx<T> v[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const Cx<T> x = in[(j + r * NR) * LD + c];
+        v[r] = r == 0 ? x : x * tw_at<T, FWD>(tw, k * r * TWS);
+      }
+      dft_small<T, R, FWD>(v, tw, N);
+      const int d = (j / Ns) * Ns * R + k;
+#pragma unroll
+      for (int r = 0; r < R; ++r) out[(d + r * Ns) * LD + c] = v[r];
+    }
+  }
+  return stages<T, N, LD, FWD, Ns * R>(out, in, tw, cols, cc, RList<Rest...>{});
+}
+
+template <typename T, int N, int COLS, bool FWD>
+__global__ void __launch_bounds__(256)
+fft_fixed_kernel(const FftAxis A, Cx<T>* __restrict__ data) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  constexpr int LD = COLS + 1;  // padded column stride of the tile
+  Cx<T>* buf0 = reinterpret_cast<Cx<T>*>(sm);
+  Cx<T>* buf1 = buf0 + N * LD;
+  Cx<T>* tw = buf1 + N * LD;
+  const int tid = threadIdx.x, bd = blockDim.x;
+  const long long c0 = (long long)blockIdx.x * COLS;
+  const int cc = (int)min((long long)COLS, A.ncols - c0);
+  const long long S = A.S;
+  for (int i = tid; i < N; i += bd) tw[i] = static_cast<const Cx<T>*>(A.tw)[i];
+  if (S == 1) {
+    const Cx<T>* src = data + c0 * N;
+    for (int i = tid; i < N * cc; i += bd) {
+      const int c = i / N, j = i % N;
+      buf0[j * LD + c] = src[i];
+    }
+  } else {
+    const long long b = c0 / S, s0 = c0 % S;
+    if (s0 + cc <= S) {  // the tile's columns are one contiguous run per row
+      Cx<T>* base = data + b * N * S + s0;
+      for (int i = tid; i < N * COLS; i += bd) {
+        const int j = i / COLS, c = i % COLS;
+        if (c < cc) buf0[j * LD + c] = base[(long long)j * S + c];
+      }
+    } else {
+      for (int i = tid; i < N * COLS; i += bd) {
+        const int j = i / COLS, c = i % COLS;
+        if (c < cc) {
+          const long long col = c0 + c, bb = col / S, ss = col % S;
+          buf0[j * LD + c] = data[(bb * N + j) * S + ss];
+        }
+      }
+    }
+  }
+  Cx<T>* res = stages<T, N, LD, FWD, 1>(buf0, buf1, tw, COLS, cc, typename FftRadices<N>::type{});
+  __syncthreads();
+  if (S == 1) {
+    Cx<T>* dst = data + c0 * N;
+    for (int i = tid; i < N * cc; i += bd) {
+      const int c = i / N, j = i % N;
+      dst[i] = res[j * LD + c];
+    }
+  } else {
+    const long long b = c0 / S, s0 = c0 % S;
+    if (s0 + cc <= S) {
+      Cx<T>* base = data + b * N * S + s0;
+      for (int i = tid; i < N * COLS; i += bd) {
+        const int j = i / COLS, c = i % COLS;
+        if (c < cc) base[(long long)j * S + c] = res[j * LD + c];
+      }
+    } else {
+      for (int i = tid; i < N * COLS; i += bd) {
+        const int j = i / COLS, c = i % COLS;
+        if (c < cc) {
+          const long long col = c0 + c, bb = col / S, ss = col % S;
+          data[(bb * N + j) * S + ss] = res[j * LD + c];
+        }
+      }
+    }
+  }
+}
+
+template <typename T>
+constexpr int fixed_cols() {
+  return sizeof(T) == 8 ? 16 : 32;
+}
+
+template <typename T, int N>
+size_t fixed_smem() {
+  constexpr int LD = fixed_cols<T>() + 1;
+  return sizeof(Cx<T>) * ((size_t)2 * N * LD + N);
+}
+
+template <typename T, int N>
+void fixed_attr() {
+  allow_max_smem(fft_fixed_kernel<T, N, fixed_cols<T>(), true>, fixed_smem<T, N>(), "fft smem attribute");
+  allow_max_smem(fft_fixed_kernel<T, N, fixed_cols<T>(), false>, fixed_smem<T, N>(), "fft smem attribute");
+}
+
+template <typename T, int N>
+void fixed_launch(const FftAxis& a, Cx<T>* data, int sign, cudaStream_t s) {
+  constexpr int COLS = fixed_cols<T>();
+  const long long nb = (a.ncols + COLS - 1) / COLS;
+  throw_if(nb > 0x7fffffffLL, "FFT batch too large", 4);
+  if (sign < 0)
+    fft_fixed_kernel<T, N, COLS, true><<<(unsigned)nb, 256, fixed_smem<T, N>(), s>>>(a, data);
+  else
+    fft_fixed_kernel<T, N, COLS, false><<<(unsigned)nb, 256, fixed_smem<T, N>(), s>>>(a, data);
+}
+
+#define MDFT_FIXED_SIZES(X) X(16) X(32) X(64) X(128) X(256) X(48) X(96) X(192) X(80) X(160)
+
+template <typename T>
+bool fixed_supported(int n) {
+  switch (n) {
+#define X(N) case N:
+    MDFT_FIXED_SIZES(X)
+#undef X
+    return true;
+  }
+  return false;
+}
+
+template <typename T>
+void fixed_setup(int n) {
+  switch (n) {
+#define X(N) \
+  case N:    \
+    fixed_attr<T, N>(); \
+    return;
+    MDFT_FIXED_SIZES(X)
+#undef X
+  }
+}
+
+template <typename T>
+size_t fixed_smem_of(int n) {
+  switch (n) {
+#define X(N) \
+  case N:    \
+    return fixed_smem<T, N>();
+    MDFT_FIXED_SIZES(X)
+#undef X
+  }
+  return 0;
+}
+
+template <typename T>
+void fixed_dispatch(const FftAxis& a, Cx<T>* data, int sign, cudaStream_t s) {
+  switch (a.n) {
+#define X(N) \
+  case N:    \
+    fixed_launch<T, N>(a, data, sign, s); \
+    return;
+    MDFT_FIXED_SIZES(X)
+#undef X
+  }
+  throw Error(4, "no fixed-length FFT kernel for this length");
+}
+
 }  // namespace
 
 template <typename T>
 void fft_axis_finish(FftAxis& a) {
+  if (fixed_supported<T>(a.n)) {
+    a.fixed = 1;
+    a.cols = fixed_cols<T>();
+    a.smem = fixed_smem_of<T>(a.n);
+    fixed_setup<T>(a.n);
+    return;
+  }
+  a.fixed = 0;
   // transforms per CTA: keep the two ping-pong tiles near 32-64 KB
   int cols = 16;
   if (a.n <= 16) cols = 64;
@@ -180,6 +437,12 @@ void fft_axis_finish(FftAxis& a) {
 template <typename T>
 void launch_fft_axis(const FftAxis& a, Cx<T>* data, int sign, cudaStream_t s) {
   if (a.n <= 1 || a.ncols == 0) return;
+  if (a.fixed) {
+    clear_stale_error();
+    fixed_dispatch<T>(a, data, sign, s);
+    launch_check("fft kernel launch");
+    return;
+  }
   const long long nb = (a.ncols + a.cols - 1) / a.cols;
   throw_if(nb > 0x7fffffffLL, "FFT batch too large", 4);
   clear_stale_error();
