@@ -54,7 +54,16 @@ typedef enum {
   MDFT_ERR_NOMEM = 5        /* device allocation failed */
 } mdft_status;
 
-typedef enum { MDFT_F64 = 0, MDFT_F32 = 1 } mdft_precision;
+/* MDFT_F64: double fields, FP64 arithmetic (the reference's
+ *   ScalarType=double).
+ * MDFT_F32: float fields, FP32 arithmetic with FP64 recursions and energy
+ *   sum (the mixed form).
+ * MDFT_F64_DF: double fields, arithmetic in double-float (each value a pair
+ *   of floats, ~48 significand bits, error-free sums and products) on the
+ *   FP32 pipes, which on this GPU are 64x wider than the FP64 pipe; results
+ *   stay within 1e-12 of the FP64 form.  Recursions (Wigner-d, R(q)) and the
+ *   energy sum remain FP64. */
+typedef enum { MDFT_F64 = 0, MDFT_F32 = 1, MDFT_F64_DF = 2 } mdft_precision;
 
 typedef struct mdft_grid_s* mdft_grid_t;
 typedef struct mdft_opt_s* mdft_opt_t;

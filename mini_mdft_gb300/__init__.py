@@ -6,6 +6,7 @@ from . import inputs  # noqa: F401
 from .api import (  # noqa: F401
     MDFT_F32,
     MDFT_F64,
+    MDFT_F64_DF,
     AngularGrid,
     Convolution,
     MdftError,

@@ -14,6 +14,7 @@ HEADER_PATH = os.path.join(os.path.dirname(_PKG), "include", "mdft_gb300.h")
 MDFT_OK = 0
 MDFT_F64 = 0
 MDFT_F32 = 1
+MDFT_F64_DF = 2
 
 _lib = None
 

@@ -27,13 +27,23 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import MDFT_F32, MDFT_F64, MdftError, check, lib
+from ._lib import MDFT_F32, MDFT_F64, MDFT_F64_DF, MdftError, check, lib
 
 __all__ = [
     "SpatialGrid", "AngularGrid", "OrientationProjectionMap",
     "OrientationProjectionTransform", "Convolution", "get_delta_rho",
-    "get_delta_f", "MdftError", "MDFT_F64", "MDFT_F32",
+    "get_delta_f", "MdftError", "MDFT_F64", "MDFT_F32", "MDFT_F64_DF",
 ]
+
+_PRECISIONS = {"f64": MDFT_F64, "f32": MDFT_F32, "f64df": MDFT_F64_DF,
+               MDFT_F64: MDFT_F64, MDFT_F32: MDFT_F32, MDFT_F64_DF: MDFT_F64_DF}
+
+
+def _precision_arg(precision):
+    try:
+        return _PRECISIONS[precision]
+    except (KeyError, TypeError):
+        raise MdftError(1, "precision must be 'f64', 'f32' or 'f64df'")
 
 
 def _torch():
@@ -164,13 +174,15 @@ def _check_field(t, shape_numel, dtypes, name):
 class OrientationProjectionTransform:
     """OrientationProjectionTransform(spatial_grid, angular_grid, map).
 
-    ``precision`` is "f64" (plain form) or "f32" (mixed form); the dtype of
-    the tensors passed to angl2proj/proj2angl must match it."""
+    ``precision`` is "f64" (plain form), "f32" (mixed form) or "f64df" (FP64
+    fields, double-float arithmetic on the FP32 pipes); the dtype of the
+    tensors passed to angl2proj/proj2angl must match it (float64/complex128
+    for "f64" and "f64df")."""
 
     def __init__(self, spatial_grid, angular_grid, map=None, precision="f64"):
         sg, ag = spatial_grid, angular_grid
         self._g = _GridHandle(sg.m_n_nodes, sg.m_length, ag.m_mmax, ag.m_molrotsymorder)
-        self.precision = MDFT_F64 if precision in ("f64", MDFT_F64) else MDFT_F32
+        self.precision = _precision_arg(precision)
         h = C.c_void_p()
         check(lib().mdft_opt_create(C.byref(h), self._g.h, self.precision))
         self.h = h
@@ -185,9 +197,9 @@ class OrientationProjectionTransform:
 
     def _dtypes(self):
         torch = _torch()
-        if self.precision == MDFT_F64:
-            return (torch.float64,), (torch.complex128,)
-        return (torch.float32,), (torch.complex64,)
+        if self.precision == MDFT_F32:
+            return (torch.float32,), (torch.complex64,)
+        return (torch.float64,), (torch.complex128,)
 
     def angl2proj(self, o, p):
         rd, cd = self._dtypes()
@@ -216,7 +228,7 @@ class Convolution:
                  precision="f64", _table=None):
         sg, ag = spatial_grid, angular_grid
         self._g = _GridHandle(sg.m_n_nodes, sg.m_length, ag.m_mmax, ag.m_molrotsymorder)
-        self.precision = MDFT_F64 if precision in ("f64", MDFT_F64) else MDFT_F32
+        self.precision = _precision_arg(precision)
         h = C.c_void_p()
         if _table is not None:
             idx, tab, dq = _table
@@ -254,7 +266,7 @@ class Convolution:
 
     def _cdt(self):
         torch = _torch()
-        return (torch.complex128,) if self.precision == MDFT_F64 else (torch.complex64,)
+        return (torch.complex64,) if self.precision == MDFT_F32 else (torch.complex128,)
 
     def execute(self, deltarho_p):
         _check_field(deltarho_p, self.N * self.np, self._cdt(), "deltarho_p")

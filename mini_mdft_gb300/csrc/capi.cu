@@ -47,18 +47,41 @@ int guarded(F&& f) {
 inline cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
 
 void check_prec(int precision) {
-  throw_if(precision != MDFT_F64 && precision != MDFT_F32, "precision must be MDFT_F64 or MDFT_F32");
+  throw_if(precision != MDFT_F64 && precision != MDFT_F32 && precision != MDFT_F64_DF,
+           "precision must be MDFT_F64, MDFT_F32 or MDFT_F64_DF");
+}
+
+// Calls f(S{}, C{}) with the storage and arithmetic types of a precision:
+// MDFT_F64 (double, double), MDFT_F32 (float, float), MDFT_F64_DF (double,
+// double-float).
+template <typename F>
+void with_types(int precision, F&& f) {
+  switch (precision) {
+    case MDFT_F64: f(double{}, double{}); return;
+    case MDFT_F32: f(float{}, float{}); return;
+    case MDFT_F64_DF: f(double{}, mdft::DF{}); return;
+  }
+  throw Error(MDFT_ERR_INVALID, "precision must be MDFT_F64, MDFT_F32 or MDFT_F64_DF");
 }
 
 constexpr long double kPiL = 3.141592653589793238462643383279502884L;
 
 // exp(-2 pi i t / n), t = 0..n-1, rounded from long double.
 template <typename T>
+T from_ld(long double x) {
+  return (T)x;
+}
+template <>
+mdft::DF from_ld<mdft::DF>(long double x) {
+  return mdft::DF(x);
+}
+
+template <typename T>
 std::vector<Cx<T>> twiddles(int n) {
   std::vector<Cx<T>> tw(n > 0 ? n : 1);
   for (int t = 0; t < n; ++t) {
     const long double a = 2.0L * kPiL * (long double)t / (long double)n;
-    tw[t] = mdft::mkc<T>((T)std::cos(a), (T)-std::sin(a));
+    tw[t] = mdft::mkc<T>(from_ld<T>(std::cos(a)), from_ld<T>(-std::sin(a)));
   }
   return tw;
 }
@@ -106,7 +129,7 @@ struct mdft_conv_s {
 
 namespace {
 
-template <typename T>
+template <typename S, typename T>
 void opt_build(mdft_opt_s* h) {
   const mdft::Grid& g = h->g;
   const int nt = g.ntheta, np = g.np;
@@ -116,8 +139,8 @@ void opt_build(mdft_opt_s* h) {
     for (int ip = 0; ip < np; ++ip) {
       const double d = g.wigner[(size_t)it * np + ip];
       const double f = g.fm[g.m[ip]];
-      ca[(size_t)it * np + ip] = (T)(d * g.wtheta[it] * f * inv);
-      cp[(size_t)it * np + ip] = (T)(d * f);
+      ca[(size_t)it * np + ip] = from_ld<T>((long double)d * g.wtheta[it] * f * inv);
+      cp[(size_t)it * np + ip] = from_ld<T>((long double)d * f);
     }
   h->coef_a2p.upload(ca.data(), sizeof(T) * ca.size());
   h->coef_p2a.upload(cp.data(), sizeof(T) * cp.size());
@@ -147,10 +170,10 @@ void opt_build(mdft_opt_s* h) {
   P.ip_mup = h->ip_mup.as<int>();
   P.ip_mu2 = h->ip_mu2.as<int>();
   P.pmap = h->pmap.as<int>();
-  mdft::ang_plan_finish<T>(P);
+  mdft::ang_plan_finish<S, T>(P);
 }
 
-template <typename T>
+template <typename ST, typename T>
 void fft_axis_build(mdft::FftAxis& a, DevBuf& twbuf, int n, long long S, long long ncols) {
   throw_if(!mdft::fft_factor(n, a), "FFT length " + std::to_string(n) +
                                         " has a prime factor above 13", MDFT_ERR_UNSUPPORTED);
@@ -159,10 +182,10 @@ void fft_axis_build(mdft::FftAxis& a, DevBuf& twbuf, int n, long long S, long lo
   auto tw = twiddles<T>(n);
   twbuf.upload(tw.data(), sizeof(Cx<T>) * n);
   a.tw = twbuf.ptr;
-  mdft::fft_axis_finish<T>(a);
+  mdft::fft_axis_finish<ST, T>(a);
 }
 
-template <typename T>
+template <typename S, typename T>
 void conv_build(mdft_conv_s* h, const mdft::LucTable& t) {
   const mdft::Grid& g = h->g;
   throw_if(g.mmax > mdft::kRotMmaxMax, "Convolution supports mmax <= 6 (RotationCoeffs)",
@@ -173,14 +196,6 @@ void conv_build(mdft_conv_s* h, const mdft::LucTable& t) {
   h->nq = need;
   h->dq = t.dq;
   h->mnq = mdft::reorder_luc(g, t, need);
-  // device table transposed to (nq, np_new) so a pair's two rows are contiguous
-  std::vector<Cx<T>> ct((size_t)need * g.np_new);
-  for (int i = 0; i < g.np_new; ++i)
-    for (int iq = 0; iq < need; ++iq) {
-      const auto z = h->mnq[(size_t)i * need + iq];
-      ct[(size_t)iq * g.np_new + i] = mdft::mkc<T>((T)z.real(), (T)z.imag());
-    }
-  h->ctab.upload(ct.data(), sizeof(Cx<T>) * ct.size());
   // pair list: reference order kept for the getter, device copy sorted by
   // the linear index of q (each pair is independent; roles are unchanged)
   h->pair_list = mdft::gamma_p_map(g.nx, g.ny, g.nz);
@@ -232,8 +247,25 @@ void conv_build(mdft_conv_s* h, const mdft::LucTable& t) {
   O.ip_mup = h->ip_mup.as<int>();
   O.ip_mu2 = h->ip_mu2.as<int>();
   O.ia_map = h->ia_map.as<int>();
+  mdft::oz_plan_finish<S, T>(O);
+  // c(q) table transposed to (nq, np_new) so a pair's two rows are
+  // contiguous, in the arithmetic type of the kernel that reads it
+  auto upload_ctab = [&](auto tag) {
+    using U = decltype(tag);
+    std::vector<Cx<U>> ct((size_t)need * g.np_new);
+    for (int i = 0; i < g.np_new; ++i)
+      for (int iq = 0; iq < need; ++iq) {
+        const auto z = h->mnq[(size_t)i * need + iq];
+        ct[(size_t)iq * g.np_new + i] =
+            mdft::mkc<U>(from_ld<U>((long double)z.real()), from_ld<U>((long double)z.imag()));
+      }
+    h->ctab.upload(ct.data(), sizeof(Cx<U>) * ct.size());
+  };
+  if (O.lane_path)
+    upload_ctab(T{});
+  else
+    upload_ctab(S{});
   O.ctab = h->ctab.ptr;
-  mdft::oz_plan_finish<T>(O);
   if (O.lane_path) {
     // Per-pair geometry of the lane path, in the sorted pair order: linear
     // indices of q and -q, the c(q) row iq and weight alpha of
@@ -255,7 +287,7 @@ void conv_build(mdft_conv_s* h, const mdft::LucTable& t) {
       const bool sing = qeq && (ix == g.nx / 2 || iy == g.ny / 2 || iz == g.nz / 2);
       info[i] = make_int4((int)(((long long)ix * g.ny + iy) * g.nz + iz),
                           (int)(((long long)ixm * g.ny + iym) * g.nz + izm), iq, sing ? 1 : 0);
-      alpha[i] = (T)(eiq - (double)iq);
+      alpha[i] = from_ld<T>((long double)(eiq - (double)iq));
     }
     h->pinfo.upload(info.data(), sizeof(int4) * info.size());
     h->palpha.upload(alpha.data(), sizeof(T) * alpha.size());
@@ -277,23 +309,23 @@ void conv_build(mdft_conv_s* h, const mdft::LucTable& t) {
     O.rtab = h->rtab.ptr;
   }
   const long long N = g.N(), np = g.np;
-  fft_axis_build<T>(h->az, h->tw_z, g.nz, 1, np * g.nx * g.ny);
-  fft_axis_build<T>(h->ay, h->tw_y, g.ny, g.nz, np * g.nx * (long long)g.nz);
-  fft_axis_build<T>(h->ax, h->tw_x, g.nx, (long long)g.ny * g.nz, np * (long long)g.ny * g.nz);
+  fft_axis_build<S, T>(h->az, h->tw_z, g.nz, 1, np * g.nx * g.ny);
+  fft_axis_build<S, T>(h->ay, h->tw_y, g.ny, g.nz, np * g.nx * (long long)g.nz);
+  fft_axis_build<S, T>(h->ax, h->tw_x, g.nx, (long long)g.ny * g.nz, np * (long long)g.ny * g.nz);
   (void)N;
 }
 
-template <typename T>
+template <typename S, typename T>
 void conv_fft(mdft_conv_s* h, void* p, int sign, cudaStream_t s) {
-  auto* d = static_cast<Cx<T>*>(p);
+  auto* d = static_cast<Cx<S>*>(p);
   if (sign < 0) {
-    mdft::launch_fft_axis<T>(h->az, d, sign, s);
-    mdft::launch_fft_axis<T>(h->ay, d, sign, s);
-    mdft::launch_fft_axis<T>(h->ax, d, sign, s);
+    mdft::launch_fft_axis<S, T>(h->az, d, sign, s);
+    mdft::launch_fft_axis<S, T>(h->ay, d, sign, s);
+    mdft::launch_fft_axis<S, T>(h->ax, d, sign, s);
   } else {
-    mdft::launch_fft_axis<T>(h->ax, d, sign, s);
-    mdft::launch_fft_axis<T>(h->ay, d, sign, s);
-    mdft::launch_fft_axis<T>(h->az, d, sign, s);
+    mdft::launch_fft_axis<S, T>(h->ax, d, sign, s);
+    mdft::launch_fft_axis<S, T>(h->ay, d, sign, s);
+    mdft::launch_fft_axis<S, T>(h->az, d, sign, s);
   }
 }
 
@@ -391,10 +423,7 @@ int mdft_opt_create(mdft_opt_t* out, mdft_grid_t g, int precision) {
     auto h = std::make_unique<mdft_opt_s>(g->g);
     h->prec = precision;
     h->device = current_device();
-    if (precision == MDFT_F64)
-      opt_build<double>(h.get());
-    else
-      opt_build<float>(h.get());
+    with_types(precision, [&](auto st, auto ct) { opt_build<decltype(st), decltype(ct)>(h.get()); });
     *out = h.release();
   });
 }
@@ -408,12 +437,11 @@ int mdft_opt_angl2proj(mdft_opt_t h, const void* o, void* p, void* stream) {
   return guarded([&] {
     throw_if(!h || !o || !p, "NULL argument");
     check_device(h->device);
-    if (h->prec == MDFT_F64)
-      mdft::launch_angl2proj<double>(h->plan, static_cast<const double*>(o), static_cast<Cx<double>*>(p),
-                                     false, 0.0, as_stream(stream));
-    else
-      mdft::launch_angl2proj<float>(h->plan, static_cast<const float*>(o), static_cast<Cx<float>*>(p),
-                                    false, 0.0, as_stream(stream));
+    with_types(h->prec, [&](auto st, auto ct) {
+      using S = decltype(st);
+      mdft::launch_angl2proj<S, decltype(ct)>(h->plan, static_cast<const S*>(o), static_cast<Cx<S>*>(p),
+                                               false, 0.0, as_stream(stream));
+    });
   });
 }
 
@@ -421,12 +449,11 @@ int mdft_opt_angl2proj_from_xi(mdft_opt_t h, const void* xi, double rho0, void* 
   return guarded([&] {
     throw_if(!h || !xi || !p, "NULL argument");
     check_device(h->device);
-    if (h->prec == MDFT_F64)
-      mdft::launch_angl2proj<double>(h->plan, static_cast<const double*>(xi), static_cast<Cx<double>*>(p),
-                                     true, rho0, as_stream(stream));
-    else
-      mdft::launch_angl2proj<float>(h->plan, static_cast<const float*>(xi), static_cast<Cx<float>*>(p),
-                                    true, rho0, as_stream(stream));
+    with_types(h->prec, [&](auto st, auto ct) {
+      using S = decltype(st);
+      mdft::launch_angl2proj<S, decltype(ct)>(h->plan, static_cast<const S*>(xi), static_cast<Cx<S>*>(p),
+                                               true, rho0, as_stream(stream));
+    });
   });
 }
 
@@ -434,12 +461,11 @@ int mdft_opt_proj2angl(mdft_opt_t h, const void* p, void* o, void* stream) {
   return guarded([&] {
     throw_if(!h || !o || !p, "NULL argument");
     check_device(h->device);
-    if (h->prec == MDFT_F64)
-      mdft::launch_proj2angl<double>(h->plan, static_cast<const Cx<double>*>(p), static_cast<double*>(o),
-                                     as_stream(stream));
-    else
-      mdft::launch_proj2angl<float>(h->plan, static_cast<const Cx<float>*>(p), static_cast<float*>(o),
-                                    as_stream(stream));
+    with_types(h->prec, [&](auto st, auto ct) {
+      using S = decltype(st);
+      mdft::launch_proj2angl<S, decltype(ct)>(h->plan, static_cast<const Cx<S>*>(p), static_cast<S*>(o),
+                                               as_stream(stream));
+    });
   });
 }
 
@@ -451,10 +477,7 @@ static int conv_create_impl(mdft_conv_t* out, mdft_grid_t g, const mdft::LucTabl
     auto h = std::make_unique<mdft_conv_s>(g->g);
     h->prec = precision;
     h->device = current_device();
-    if (precision == MDFT_F64)
-      conv_build<double>(h.get(), t);
-    else
-      conv_build<float>(h.get(), t);
+    with_types(precision, [&](auto st, auto ct) { conv_build<decltype(st), decltype(ct)>(h.get(), t); });
     *out = h.release();
   });
 }
@@ -503,10 +526,9 @@ int mdft_conv_fft(mdft_conv_t h, void* p, int sign, void* stream) {
     throw_if(!h || !p, "NULL argument");
     throw_if(sign != -1 && sign != 1, "sign must be -1 or +1");
     check_device(h->device);
-    if (h->prec == MDFT_F64)
-      conv_fft<double>(h, p, sign, as_stream(stream));
-    else
-      conv_fft<float>(h, p, sign, as_stream(stream));
+    with_types(h->prec, [&](auto st, auto ct) {
+      conv_fft<decltype(st), decltype(ct)>(h, p, sign, as_stream(stream));
+    });
   });
 }
 
@@ -514,10 +536,10 @@ int mdft_conv_kspace(mdft_conv_t h, void* p, void* stream) {
   return guarded([&] {
     throw_if(!h || !p, "NULL argument");
     check_device(h->device);
-    if (h->prec == MDFT_F64)
-      mdft::launch_oz<double>(h->oz, static_cast<Cx<double>*>(p), as_stream(stream));
-    else
-      mdft::launch_oz<float>(h->oz, static_cast<Cx<float>*>(p), as_stream(stream));
+    with_types(h->prec, [&](auto st, auto ct) {
+      using S = decltype(st);
+      mdft::launch_oz<S, decltype(ct)>(h->oz, static_cast<Cx<S>*>(p), as_stream(stream));
+    });
   });
 }
 
@@ -526,15 +548,13 @@ int mdft_conv_execute(mdft_conv_t h, void* p, void* stream) {
     throw_if(!h || !p, "NULL argument");
     check_device(h->device);
     cudaStream_t s = as_stream(stream);
-    if (h->prec == MDFT_F64) {
-      conv_fft<double>(h, p, -1, s);
-      mdft::launch_oz<double>(h->oz, static_cast<Cx<double>*>(p), s);
-      conv_fft<double>(h, p, +1, s);
-    } else {
-      conv_fft<float>(h, p, -1, s);
-      mdft::launch_oz<float>(h->oz, static_cast<Cx<float>*>(p), s);
-      conv_fft<float>(h, p, +1, s);
-    }
+    with_types(h->prec, [&](auto st, auto ct) {
+      using S = decltype(st);
+      using C = decltype(ct);
+      conv_fft<S, C>(h, p, -1, s);
+      mdft::launch_oz<S, C>(h->oz, static_cast<Cx<S>*>(p), s);
+      conv_fft<S, C>(h, p, +1, s);
+    });
   });
 }
 
@@ -567,7 +587,7 @@ int mdft_get_delta_rho(const void* xi, void* delta_rho, size_t n, double rho0, i
   return guarded([&] {
     check_prec(precision);
     throw_if(n > 0 && (!xi || !delta_rho), "NULL argument");
-    if (precision == MDFT_F64)
+    if (precision != MDFT_F32)  // MDFT_F64 and MDFT_F64_DF fields are double
       mdft::launch_delta_rho<double>(static_cast<const double*>(xi), static_cast<double*>(delta_rho), n,
                                      rho0, as_stream(stream));
     else
@@ -589,7 +609,7 @@ int mdft_get_delta_f(const void* xi, const void* vexc, const double* w, void* de
     Scratch scratch(bytes, s);
     mdft::cuda_check(cudaMemsetAsync(static_cast<char*>(scratch.p) + sizeof(double2) * nb, 0, 16, s),
                      "cudaMemsetAsync");
-    if (precision == MDFT_F64)
+    if (precision != MDFT_F32)  // MDFT_F64 and MDFT_F64_DF fields are double
       mdft::launch_delta_f<double>(static_cast<const double*>(xi), static_cast<const double*>(vexc), w,
                                    static_cast<double*>(delta_f), ff_dev, nxyz, no, rho0, prefactor,
                                    scratch.p, s);

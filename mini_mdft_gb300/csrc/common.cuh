@@ -50,6 +50,75 @@ __host__ __device__ __forceinline__ Cx<T> cmac(Cx<T> a, Cx<T> b, Cx<T> c) {
   return mkc<T>(a.re + b.re * c.re - b.im * c.im, a.im + b.re * c.im + b.im * c.re);
 }
 
+// ---------------------------------------------------------------------------
+// Double-float: a value hi + lo held as two floats with |lo| <= ulp(hi)/2,
+// about 48 significand bits.  Sums use Knuth's TwoSum and products Dekker's
+// TwoProd through FMA, then a fast renormalisation (Dekker 1971; the
+// "sloppy" pair addition of Joldes, Muller and Popescu 2017, whose error is
+// bounded relative to |a| + |b|, the norm-wise bound FFT and matrix-vector
+// error analyses need).  It lets the FP64 form run on the FP32 pipes, which
+// are 64x wider than the FP64 pipe of this GPU.
+// ---------------------------------------------------------------------------
+struct DF {
+  float hi, lo;
+  DF() = default;
+  __host__ __device__ constexpr DF(float h, float l) : hi(h), lo(l) {}
+  __host__ __device__ constexpr DF(int v) : hi((float)v), lo(0.f) {}
+  __host__ __device__ explicit DF(double x) : hi((float)x), lo((float)(x - (double)(float)x)) {}
+  __host__ __device__ explicit DF(long double x)
+      : hi((float)x), lo((float)(x - (long double)(float)x)) {}
+  __host__ __device__ explicit operator double() const { return (double)hi + (double)lo; }
+};
+
+__host__ __device__ __forceinline__ DF df_two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  const float e = (a - (s - bb)) + (b - bb);
+  return DF(s, e);
+}
+__host__ __device__ __forceinline__ DF df_fast_two_sum(float a, float b) {
+  const float s = a + b;
+  return DF(s, b - (s - a));
+}
+__host__ __device__ __forceinline__ DF operator+(DF a, DF b) {
+  const DF s = df_two_sum(a.hi, b.hi);
+  const float t = a.lo + b.lo;
+  return df_fast_two_sum(s.hi, s.lo + t);
+}
+__host__ __device__ __forceinline__ DF operator-(DF a) { return DF(-a.hi, -a.lo); }
+__host__ __device__ __forceinline__ DF operator-(DF a, DF b) { return a + (-b); }
+__host__ __device__ __forceinline__ DF operator*(DF a, DF b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return df_fast_two_sum(p, e);
+}
+__host__ __device__ __forceinline__ DF& operator+=(DF& a, DF b) { return a = a + b; }
+// |x| < e for e a power of two representable in float (exact on normalised pairs)
+__host__ __device__ __forceinline__ bool df_abs_lt(DF x, float e) {
+  const float h = fabsf(x.hi);
+  return h < e || (h == e && (x.hi > 0.f ? x.lo < 0.f : x.lo > 0.f));
+}
+
+// Storage <-> compute conversions (identity unless the compute type is DF).
+template <typename C, typename S>
+__host__ __device__ __forceinline__ C to_compute(S x) {
+  return (C)x;
+}
+template <>
+__host__ __device__ __forceinline__ DF to_compute<DF, double>(double x) {
+  return DF(x);
+}
+template <typename S, typename C>
+__host__ __device__ __forceinline__ S to_storage(C x) {
+  return (S)x;
+}
+template <>
+__host__ __device__ __forceinline__ double to_storage<double, DF>(DF x) {
+  return (double)x;
+}
+
 inline void cuda_check(cudaError_t e, const char* what) {
   if (e != cudaSuccess) {
     cudaGetLastError();  // a non-sticky error must not resurface at a later check
@@ -127,12 +196,14 @@ struct AngPlan {
   const int* pmap;                  // (mmax+1, 2mmax+1, K+1)
 };
 
-template <typename T>
-void launch_angl2proj(const AngPlan& P, const T* o, Cx<T>* p, bool from_xi,
+// S: storage type of the fields (double/float); C: arithmetic type
+// (double, float, or DF for the FP64 form on the FP32 pipes).
+template <typename S, typename C>
+void launch_angl2proj(const AngPlan& P, const S* o, Cx<S>* p, bool from_xi,
                       double rho0, cudaStream_t s);
-template <typename T>
-void launch_proj2angl(const AngPlan& P, const Cx<T>* p, T* o, cudaStream_t s);
-template <typename T>
+template <typename S, typename C>
+void launch_proj2angl(const AngPlan& P, const Cx<S>* p, S* o, cudaStream_t s);
+template <typename S, typename C>
 void ang_plan_finish(AngPlan& P);  // picks tiles / smem sizes, sets attributes
 
 // ---------------------------------------------------------------------------
@@ -151,10 +222,10 @@ struct FftAxis {
   const void* tw;  // (n) Cx<T> : exp(-2 pi i t / n)
 };
 bool fft_factor(int n, FftAxis& a);  // false if n has a prime factor > 13
-template <typename T>
+template <typename S, typename C>
 void fft_axis_finish(FftAxis& a);
-template <typename T>
-void launch_fft_axis(const FftAxis& a, Cx<T>* data, int sign, cudaStream_t s);
+template <typename S, typename C>
+void launch_fft_axis(const FftAxis& a, Cx<S>* data, int sign, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // Fused (q,-q) rotation + Ornstein-Zernike + rotation back.
@@ -185,13 +256,13 @@ struct OzPlan {
   const int* ia_start;     // (np) first OZ coefficient of each projection
   const void* rtab;        // (npairs_pad/32, nR, 32) Cx<T>: R(q) of 32 pairs, lane fastest
 };
-template <typename T>
+template <typename S, typename C>
 void oz_plan_finish(OzPlan& P);
 // Fills the R(q) table of the lane path (FP64 recursion, stored as T).
-template <typename T>
+template <typename C>
 void oz_build_rtab(const OzPlan& P, DevBuf& rtab);
-template <typename T>
-void launch_oz(const OzPlan& P, Cx<T>* p, cudaStream_t s);
+template <typename S, typename C>
+void launch_oz(const OzPlan& P, Cx<S>* p, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // Energy / gradient.

@@ -206,7 +206,7 @@ extern "C" int mdft_get_delta_f_noalloc(const void* xi, const void* vexc, const 
                                         void* stream) {
   using namespace mdft;
   try {
-    throw_if(precision != 0 && precision != 1, "precision must be MDFT_F64 or MDFT_F32");
+    throw_if(precision < 0 || precision > 2, "precision must be MDFT_F64, MDFT_F32 or MDFT_F64_DF");
     throw_if(no <= 0, "angular grid size must be positive");
     throw_if(!ff_dev, "NULL argument");
     throw_if(nxyz > 0 && (!xi || !vexc || !w || !delta_f), "NULL argument");
@@ -221,7 +221,7 @@ extern "C" int mdft_get_delta_f_noalloc(const void* xi, const void* vexc, const 
     // partials first, then the completion counter, which must start at zero
     unsigned char* counter = scratch + sizeof(double2) * nb;
     cuda_check(cudaMemsetAsync(counter, 0, sizeof(unsigned), s), "cudaMemsetAsync(fixed scratch counter)");
-    if (precision == 0)
+    if (precision != 1)  // MDFT_F64 and MDFT_F64_DF fields are double
       launch_delta_f<double>(static_cast<const double*>(xi), static_cast<const double*>(vexc), w,
                              static_cast<double*>(delta_f), ff_dev, nxyz, no, rho0, prefactor, scratch, s);
     else

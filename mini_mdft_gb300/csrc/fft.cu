@@ -8,9 +8,12 @@
 // transforms: it stages them in shared memory (for S > 1 the `cols`
 // transforms are adjacent in memory, so every row of the tile is one
 // contiguous run), runs a mixed-radix Stockham autosort FFT in shared memory
-// (radices 4, 2, 3, 5, 7, 11, 13; natural order in and out, no bit reversal)
-// and writes the tile back.  Forward uses exp(-2 pi i jk/n), backward
-// exp(+2 pi i jk/n); neither is normalised (KokkosFFT::Normalization::none).
+// (natural order in and out, no bit reversal) and writes the tile back.
+// Forward uses exp(-2 pi i jk/n), backward exp(+2 pi i jk/n); neither is
+// normalised (KokkosFFT::Normalization::none).
+//
+// S is the storage type of the array (double or float), C the arithmetic
+// type (the same, or double-float DF for the FP64 form on the FP32 pipes).
 #include "common.cuh"
 
 namespace mdft {
@@ -38,6 +41,15 @@ namespace {
 
 constexpr int kFftThreads = 256;
 
+template <typename C, typename S>
+__device__ __forceinline__ Cx<C> ld_c(const Cx<S>& z) {
+  return mkc<C>(to_compute<C>(z.re), to_compute<C>(z.im));
+}
+template <typename S, typename C>
+__device__ __forceinline__ Cx<S> st_c(const Cx<C>& z) {
+  return mkc<S>(to_storage<S>(z.re), to_storage<S>(z.im));
+}
+
 template <typename T>
 __device__ __forceinline__ Cx<T> twiddle(const Cx<T>* tw, int idx, int sign) {
   Cx<T> t = tw[idx];
@@ -45,7 +57,7 @@ __device__ __forceinline__ Cx<T> twiddle(const Cx<T>* tw, int idx, int sign) {
   return t;
 }
 
-// In-register DFT of length R on v[0..R-1] (R <= 13).
+// In-register DFT of length R on v[0..R-1] (R <= 13), runtime radix.
 template <typename T>
 __device__ __forceinline__ void small_dft(Cx<T>* v, int R, int sign, const Cx<T>* tw, int n) {
   if (R == 2) {
@@ -87,36 +99,37 @@ __device__ __forceinline__ void small_dft(Cx<T>* v, int R, int sign, const Cx<T>
   }
 }
 
-template <typename T>
+// Runtime-radix kernel: any length whose prime factors are <= 13.
+template <typename S, typename C>
 __global__ void __launch_bounds__(kFftThreads)
-fft_axis_kernel(const FftAxis A, Cx<T>* __restrict__ data, int sign) {
+fft_axis_kernel(const FftAxis A, Cx<S>* __restrict__ data, int sign) {
   extern __shared__ __align__(16) unsigned char sm[];
-  const int n = A.n, C = A.cols;
-  Cx<T>* buf0 = reinterpret_cast<Cx<T>*>(sm);
-  Cx<T>* buf1 = buf0 + (size_t)n * C;
-  Cx<T>* tw = buf1 + (size_t)n * C;
+  const int n = A.n, CL = A.cols;
+  Cx<C>* buf0 = reinterpret_cast<Cx<C>*>(sm);
+  Cx<C>* buf1 = buf0 + (size_t)n * CL;
+  Cx<C>* tw = buf1 + (size_t)n * CL;
   const int tid = threadIdx.x, bd = blockDim.x;
-  const long long c0 = (long long)blockIdx.x * C;
-  const int cc = (int)min((long long)C, A.ncols - c0);
-  const long long S = A.S;
+  const long long c0 = (long long)blockIdx.x * CL;
+  const int cc = (int)min((long long)CL, A.ncols - c0);
+  const long long S_ = A.S;
 
-  for (int i = tid; i < n; i += bd) tw[i] = static_cast<const Cx<T>*>(A.tw)[i];
-  if (S == 1) {
-    const Cx<T>* src = data + c0 * n;
+  for (int i = tid; i < n; i += bd) tw[i] = static_cast<const Cx<C>*>(A.tw)[i];
+  if (S_ == 1) {
+    const Cx<S>* src = data + c0 * n;
     for (int i = tid; i < n * cc; i += bd) {
       const int c = i / n, j = i % n;
-      buf0[j * C + c] = src[i];
+      buf0[j * CL + c] = ld_c<C>(src[i]);
     }
   } else {
     for (int i = tid; i < n * cc; i += bd) {
       const int j = i / cc, c = i % cc;
       const long long col = c0 + c;
-      const long long b = col / S, s = col % S;
-      buf0[j * C + c] = data[(b * n + j) * S + s];
+      const long long b = col / S_, s = col % S_;
+      buf0[j * CL + c] = ld_c<C>(data[(b * n + j) * S_ + s]);
     }
   }
-  Cx<T>* in = buf0;
-  Cx<T>* out = buf1;
+  Cx<C>* in = buf0;
+  Cx<C>* out = buf1;
   int Ns = 1;
   for (int st = 0; st < A.nr; ++st) {
     const int R = A.radix[st];
@@ -126,34 +139,34 @@ fft_axis_kernel(const FftAxis A, Cx<T>* __restrict__ data, int sign) {
     for (int w = tid; w < nR * cc; w += bd) {
       const int c = w % cc, j = w / cc;
       const int k = j % Ns;
-      Cx<T> v[13];
-      v[0] = in[j * C + c];
+      Cx<C> v[13];
+      v[0] = in[j * CL + c];
       for (int r = 1; r < R; ++r) {
-        const Cx<T> x = in[(j + r * nR) * C + c];
+        const Cx<C> x = in[(j + r * nR) * CL + c];
         v[r] = (k == 0) ? x : x * twiddle(tw, k * r * twstep, sign);
       }
       small_dft(v, R, sign, tw, n);
       const int d = (j / Ns) * Ns * R + k;
-      for (int r = 0; r < R; ++r) out[(d + r * Ns) * C + c] = v[r];
+      for (int r = 0; r < R; ++r) out[(d + r * Ns) * CL + c] = v[r];
     }
-    Cx<T>* t = in;
+    Cx<C>* t = in;
     in = out;
     out = t;
     Ns *= R;
   }
   __syncthreads();
-  if (S == 1) {
-    Cx<T>* dst = data + c0 * n;
+  if (S_ == 1) {
+    Cx<S>* dst = data + c0 * n;
     for (int i = tid; i < n * cc; i += bd) {
       const int c = i / n, j = i % n;
-      dst[i] = in[j * C + c];
+      dst[i] = st_c<S>(in[j * CL + c]);
     }
   } else {
     for (int i = tid; i < n * cc; i += bd) {
       const int j = i / cc, c = i % cc;
       const long long col = c0 + c;
-      const long long b = col / S, s = col % S;
-      data[(b * n + j) * S + s] = in[j * C + c];
+      const long long b = col / S_, s = col % S_;
+      data[(b * n + j) * S_ + s] = st_c<S>(in[j * CL + c]);
     }
   }
 }
@@ -234,8 +247,7 @@ __device__ __forceinline__ void dft_small(Cx<T>* v, const Cx<T>* tw, int n) {
 }
 
 template <typename T, int N, int LD, bool FWD, int Ns>
-__device__ __forceinline__ Cx<T>* stages(Cx<T>* in, Cx<T>* out, const Cx<T>* tw, int cols, int cc,
-                                         RList<>) {
+__device__ __forceinline__ Cx<T>* stages(Cx<T>* in, Cx<T>*, const Cx<T>*, int, int, RList<>) {
   return in;
 }
 
@@ -264,102 +276,103 @@ __device__ __forceinline__ Cx<T>* stages(Cx<T>* in, Cx<T>* out, const Cx<T>* tw,
   return stages<T, N, LD, FWD, Ns * R>(out, in, tw, cols, cc, RList<Rest...>{});
 }
 
-template <typename T, int N, int COLS, bool FWD>
+template <typename S, typename C, int N, int COLS, bool FWD>
 __global__ void __launch_bounds__(256)
-fft_fixed_kernel(const FftAxis A, Cx<T>* __restrict__ data) {
+fft_fixed_kernel(const FftAxis A, Cx<S>* __restrict__ data) {
   extern __shared__ __align__(16) unsigned char sm[];
   constexpr int LD = COLS + 1;  // padded column stride of the tile
-  Cx<T>* buf0 = reinterpret_cast<Cx<T>*>(sm);
-  Cx<T>* buf1 = buf0 + N * LD;
-  Cx<T>* tw = buf1 + N * LD;
+  Cx<C>* buf0 = reinterpret_cast<Cx<C>*>(sm);
+  Cx<C>* buf1 = buf0 + N * LD;
+  Cx<C>* tw = buf1 + N * LD;
   const int tid = threadIdx.x, bd = blockDim.x;
   const long long c0 = (long long)blockIdx.x * COLS;
   const int cc = (int)min((long long)COLS, A.ncols - c0);
-  const long long S = A.S;
-  for (int i = tid; i < N; i += bd) tw[i] = static_cast<const Cx<T>*>(A.tw)[i];
-  if (S == 1) {
-    const Cx<T>* src = data + c0 * N;
+  const long long S_ = A.S;
+  for (int i = tid; i < N; i += bd) tw[i] = static_cast<const Cx<C>*>(A.tw)[i];
+  if (S_ == 1) {
+    const Cx<S>* src = data + c0 * N;
     for (int i = tid; i < N * cc; i += bd) {
       const int c = i / N, j = i % N;
-      buf0[j * LD + c] = src[i];
+      buf0[j * LD + c] = ld_c<C>(src[i]);
     }
   } else {
-    const long long b = c0 / S, s0 = c0 % S;
-    if (s0 + cc <= S) {  // the tile's columns are one contiguous run per row
-      Cx<T>* base = data + b * N * S + s0;
+    const long long b = c0 / S_, s0 = c0 % S_;
+    if (s0 + cc <= S_) {  // the tile's columns are one contiguous run per row
+      const Cx<S>* base = data + b * N * S_ + s0;
       for (int i = tid; i < N * COLS; i += bd) {
         const int j = i / COLS, c = i % COLS;
-        if (c < cc) buf0[j * LD + c] = base[(long long)j * S + c];
+        if (c < cc) buf0[j * LD + c] = ld_c<C>(base[(long long)j * S_ + c]);
       }
     } else {
       for (int i = tid; i < N * COLS; i += bd) {
         const int j = i / COLS, c = i % COLS;
         if (c < cc) {
-          const long long col = c0 + c, bb = col / S, ss = col % S;
-          buf0[j * LD + c] = data[(bb * N + j) * S + ss];
+          const long long col = c0 + c, bb = col / S_, ss = col % S_;
+          buf0[j * LD + c] = ld_c<C>(data[(bb * N + j) * S_ + ss]);
         }
       }
     }
   }
-  Cx<T>* res = stages<T, N, LD, FWD, 1>(buf0, buf1, tw, COLS, cc, typename FftRadices<N>::type{});
+  Cx<C>* res = stages<C, N, LD, FWD, 1>(buf0, buf1, tw, COLS, cc, typename FftRadices<N>::type{});
   __syncthreads();
-  if (S == 1) {
-    Cx<T>* dst = data + c0 * N;
+  if (S_ == 1) {
+    Cx<S>* dst = data + c0 * N;
     for (int i = tid; i < N * cc; i += bd) {
       const int c = i / N, j = i % N;
-      dst[i] = res[j * LD + c];
+      dst[i] = st_c<S>(res[j * LD + c]);
     }
   } else {
-    const long long b = c0 / S, s0 = c0 % S;
-    if (s0 + cc <= S) {
-      Cx<T>* base = data + b * N * S + s0;
+    const long long b = c0 / S_, s0 = c0 % S_;
+    if (s0 + cc <= S_) {
+      Cx<S>* base = data + b * N * S_ + s0;
       for (int i = tid; i < N * COLS; i += bd) {
         const int j = i / COLS, c = i % COLS;
-        if (c < cc) base[(long long)j * S + c] = res[j * LD + c];
+        if (c < cc) base[(long long)j * S_ + c] = st_c<S>(res[j * LD + c]);
       }
     } else {
       for (int i = tid; i < N * COLS; i += bd) {
         const int j = i / COLS, c = i % COLS;
         if (c < cc) {
-          const long long col = c0 + c, bb = col / S, ss = col % S;
-          data[(bb * N + j) * S + ss] = res[j * LD + c];
+          const long long col = c0 + c, bb = col / S_, ss = col % S_;
+          data[(bb * N + j) * S_ + ss] = st_c<S>(res[j * LD + c]);
         }
       }
     }
   }
 }
 
-template <typename T>
+template <typename C>
 constexpr int fixed_cols() {
-  return sizeof(T) == 8 ? 16 : 32;
+  return sizeof(Cx<C>) == 16 ? 16 : 32;
 }
 
-template <typename T, int N>
+template <typename C, int N>
 size_t fixed_smem() {
-  constexpr int LD = fixed_cols<T>() + 1;
-  return sizeof(Cx<T>) * ((size_t)2 * N * LD + N);
+  constexpr int LD = fixed_cols<C>() + 1;
+  return sizeof(Cx<C>) * ((size_t)2 * N * LD + N);
 }
 
-template <typename T, int N>
+template <typename S, typename C, int N>
 void fixed_attr() {
-  allow_max_smem(fft_fixed_kernel<T, N, fixed_cols<T>(), true>, fixed_smem<T, N>(), "fft smem attribute");
-  allow_max_smem(fft_fixed_kernel<T, N, fixed_cols<T>(), false>, fixed_smem<T, N>(), "fft smem attribute");
+  allow_max_smem(fft_fixed_kernel<S, C, N, fixed_cols<C>(), true>, fixed_smem<C, N>(),
+                 "fft smem attribute");
+  allow_max_smem(fft_fixed_kernel<S, C, N, fixed_cols<C>(), false>, fixed_smem<C, N>(),
+                 "fft smem attribute");
 }
 
-template <typename T, int N>
-void fixed_launch(const FftAxis& a, Cx<T>* data, int sign, cudaStream_t s) {
-  constexpr int COLS = fixed_cols<T>();
+template <typename S, typename C, int N>
+void fixed_launch(const FftAxis& a, Cx<S>* data, int sign, cudaStream_t s) {
+  constexpr int COLS = fixed_cols<C>();
   const long long nb = (a.ncols + COLS - 1) / COLS;
   throw_if(nb > 0x7fffffffLL, "FFT batch too large", 4);
   if (sign < 0)
-    fft_fixed_kernel<T, N, COLS, true><<<(unsigned)nb, 256, fixed_smem<T, N>(), s>>>(a, data);
+    fft_fixed_kernel<S, C, N, COLS, true><<<(unsigned)nb, 256, fixed_smem<C, N>(), s>>>(a, data);
   else
-    fft_fixed_kernel<T, N, COLS, false><<<(unsigned)nb, 256, fixed_smem<T, N>(), s>>>(a, data);
+    fft_fixed_kernel<S, C, N, COLS, false><<<(unsigned)nb, 256, fixed_smem<C, N>(), s>>>(a, data);
 }
 
 #define MDFT_FIXED_SIZES(X) X(16) X(32) X(64) X(128) X(256) X(48) X(96) X(192) X(80) X(160)
 
-template <typename T>
 bool fixed_supported(int n) {
   switch (n) {
 #define X(N) case N:
@@ -370,36 +383,25 @@ bool fixed_supported(int n) {
   return false;
 }
 
-template <typename T>
-void fixed_setup(int n) {
+template <typename S, typename C>
+void fixed_setup(int n, size_t& smem) {
   switch (n) {
-#define X(N) \
-  case N:    \
-    fixed_attr<T, N>(); \
+#define X(N)                      \
+  case N:                         \
+    fixed_attr<S, C, N>();        \
+    smem = fixed_smem<C, N>();    \
     return;
     MDFT_FIXED_SIZES(X)
 #undef X
   }
 }
 
-template <typename T>
-size_t fixed_smem_of(int n) {
-  switch (n) {
-#define X(N) \
-  case N:    \
-    return fixed_smem<T, N>();
-    MDFT_FIXED_SIZES(X)
-#undef X
-  }
-  return 0;
-}
-
-template <typename T>
-void fixed_dispatch(const FftAxis& a, Cx<T>* data, int sign, cudaStream_t s) {
+template <typename S, typename C>
+void fixed_dispatch(const FftAxis& a, Cx<S>* data, int sign, cudaStream_t s) {
   switch (a.n) {
-#define X(N) \
-  case N:    \
-    fixed_launch<T, N>(a, data, sign, s); \
+#define X(N)                                   \
+  case N:                                      \
+    fixed_launch<S, C, N>(a, data, sign, s);   \
     return;
     MDFT_FIXED_SIZES(X)
 #undef X
@@ -409,13 +411,12 @@ void fixed_dispatch(const FftAxis& a, Cx<T>* data, int sign, cudaStream_t s) {
 
 }  // namespace
 
-template <typename T>
+template <typename S, typename C>
 void fft_axis_finish(FftAxis& a) {
-  if (fixed_supported<T>(a.n)) {
+  if (fixed_supported(a.n)) {
     a.fixed = 1;
-    a.cols = fixed_cols<T>();
-    a.smem = fixed_smem_of<T>(a.n);
-    fixed_setup<T>(a.n);
+    a.cols = fixed_cols<C>();
+    fixed_setup<S, C>(a.n, a.smem);
     return;
   }
   a.fixed = 0;
@@ -429,30 +430,31 @@ void fft_axis_finish(FftAxis& a) {
   }
   if (cols < 1) cols = 1;
   a.cols = cols;
-  a.smem = sizeof(Cx<T>) * ((size_t)2 * a.n * cols + a.n);
+  a.smem = sizeof(Cx<C>) * ((size_t)2 * a.n * cols + a.n);
   throw_if(a.smem > 200 * 1024, "FFT length too large for the shared-memory tile", 4);
-  allow_max_smem(fft_axis_kernel<T>, a.smem, "fft smem attribute");
+  allow_max_smem(fft_axis_kernel<S, C>, a.smem, "fft smem attribute");
 }
 
-template <typename T>
-void launch_fft_axis(const FftAxis& a, Cx<T>* data, int sign, cudaStream_t s) {
+template <typename S, typename C>
+void launch_fft_axis(const FftAxis& a, Cx<S>* data, int sign, cudaStream_t s) {
   if (a.n <= 1 || a.ncols == 0) return;
+  clear_stale_error();
   if (a.fixed) {
-    clear_stale_error();
-    fixed_dispatch<T>(a, data, sign, s);
+    fixed_dispatch<S, C>(a, data, sign, s);
     launch_check("fft kernel launch");
     return;
   }
   const long long nb = (a.ncols + a.cols - 1) / a.cols;
   throw_if(nb > 0x7fffffffLL, "FFT batch too large", 4);
-  clear_stale_error();
-  fft_axis_kernel<T><<<(unsigned)nb, kFftThreads, a.smem, s>>>(a, data, sign);
+  fft_axis_kernel<S, C><<<(unsigned)nb, kFftThreads, a.smem, s>>>(a, data, sign);
   launch_check("fft kernel launch");
 }
 
-template void fft_axis_finish<double>(FftAxis&);
-template void fft_axis_finish<float>(FftAxis&);
-template void launch_fft_axis<double>(const FftAxis&, Cx<double>*, int, cudaStream_t);
-template void launch_fft_axis<float>(const FftAxis&, Cx<float>*, int, cudaStream_t);
+template void fft_axis_finish<double, double>(FftAxis&);
+template void fft_axis_finish<float, float>(FftAxis&);
+template void fft_axis_finish<double, DF>(FftAxis&);
+template void launch_fft_axis<double, double>(const FftAxis&, Cx<double>*, int, cudaStream_t);
+template void launch_fft_axis<float, float>(const FftAxis&, Cx<float>*, int, cudaStream_t);
+template void launch_fft_axis<double, DF>(const FftAxis&, Cx<double>*, int, cudaStream_t);
 
 }  // namespace mdft

@@ -17,6 +17,7 @@
 // Pairs are visited sorted by the linear index of q, so neighbouring warps
 // touch neighbouring addresses of each projection plane.
 #include <cfloat>
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -58,6 +59,13 @@ __device__ __forceinline__ Cx<T> chop(Cx<T> x) {
   const T e = (T)DBL_EPSILON;
   if (fabs(x.re) < e) x.re = T(0);
   if (fabs(x.im) < e) x.im = T(0);
+  return x;
+}
+
+__device__ __forceinline__ Cx<DF> chop(Cx<DF> x) {
+  const float e = 2.220446049250313e-16f;  // DBL_EPSILON = 2^-52, exact in float
+  if (df_abs_lt(x.re, e)) x.re = DF(0);
+  if (df_abs_lt(x.im, e)) x.im = DF(0);
   return x;
 }
 
@@ -450,10 +458,11 @@ __global__ void rot_table_kernel(const OzPlan P, Cx<double>* __restrict__ rt64) 
   rot_recursion(q0, q1, q2, P.mmax, A, B, Cc, D, R);
 }
 
-__global__ void rot_table_to_f32(const Cx<double>* __restrict__ a, Cx<float>* __restrict__ b, long long n) {
+template <typename C>
+__global__ void rot_table_convert(const Cx<double>* __restrict__ a, Cx<C>* __restrict__ b, long long n) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
-    b[i] = mkc<float>((float)a[i].re, (float)a[i].im);
+    b[i] = mkc<C>(to_compute<C>(a[i].re), to_compute<C>(a[i].im));
 }
 
 // Projection index of (m, mup, mu2) in OrientationProjectionMap order
@@ -466,9 +475,9 @@ struct PIndex {
   }
 };
 
-template <typename T, int MMAX>
+template <typename S, typename C, int MMAX>
 __global__ void __launch_bounds__(256)
-oz_lane_kernel(const OzPlan P, Cx<T>* __restrict__ p) {
+oz_lane_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
   extern __shared__ __align__(16) unsigned char sm[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const long long blk = (long long)blockIdx.x * P.warps_per_cta + wib;
@@ -476,8 +485,8 @@ oz_lane_kernel(const OzPlan P, Cx<T>* __restrict__ p) {
   const long long pair = blk * 32 + lane;
   const bool valid = pair < P.npairs;
   const int np = P.np, mrso = P.mrso;
-  Cx<T>* Dq = reinterpret_cast<Cx<T>*>(sm + (size_t)wib * 2 * np * 32 * sizeof(Cx<T>));
-  Cx<T>* Dmq = Dq + (size_t)np * 32;
+  Cx<C>* Dq = reinterpret_cast<Cx<C>*>(sm + (size_t)wib * 2 * np * 32 * sizeof(Cx<C>));
+  Cx<C>* Dmq = Dq + (size_t)np * 32;
   PIndex ipx;
   ipx.mrso = mrso;
   {
@@ -490,23 +499,24 @@ oz_lane_kernel(const OzPlan P, Cx<T>* __restrict__ p) {
   }
   const int4 info = P.pinfo[pair];
   const long long N = P.N, lq = info.x, lmq = info.y;
-  const Cx<T>* Rt = static_cast<const Cx<T>*>(P.rtab) + blk * (long long)P.nR * 32 + lane;
+  const Cx<C>* Rt = static_cast<const Cx<C>*>(P.rtab) + blk * (long long)P.nR * 32 + lane;
 #define RT(l, m, m1) Rt[(roff(l) + ((m) + (l)) * (2 * (l) + 1) + ((m1) + (l))) * 32]
 
   // rotation to the q frame (MDFT_Convolution.hpp:427-443), block by block
 #pragma unroll
   for (int m = 0; m <= MMAX; ++m) {
     for (int mu2 = 0; mu2 <= m / mrso; ++mu2) {
-      Cx<T> gq[2 * MMAX + 1], gmq[2 * MMAX + 1];
+      Cx<C> gq[2 * MMAX + 1], gmq[2 * MMAX + 1];
 #pragma unroll
       for (int a = 0; a <= 2 * m; ++a) {
         const long long off = (long long)ipx(m, a - m, mu2) * N;
-        gq[a] = p[off + lq];
-        gmq[a] = p[off + lmq];
+        const Cx<S> u = p[off + lq], v = p[off + lmq];
+        gq[a] = mkc<C>(to_compute<C>(u.re), to_compute<C>(u.im));
+        gmq[a] = mkc<C>(to_compute<C>(v.re), to_compute<C>(v.im));
       }
 #pragma unroll 1
       for (int k = -m; k <= m; ++k) {
-        Cx<T> x = mkc<T>(0, 0), y = mkc<T>(0, 0);
+        Cx<C> x = mkc<C>(C(0), C(0)), y = mkc<C>(C(0), C(0));
 #pragma unroll
         for (int a = 0; a <= 2 * m; ++a) {
           x = cmac(x, gq[a], RT(m, a - m, k));
@@ -514,7 +524,7 @@ oz_lane_kernel(const OzPlan P, Cx<T>* __restrict__ p) {
         }
         const int j = ipx(m, k, mu2) * 32 + lane;
         Dq[j] = x;
-        Dmq[j] = (m & 1) ? mkc<T>(-y.re, -y.im) : y;
+        Dmq[j] = (m & 1) ? mkc<C>(-y.re, -y.im) : y;
       }
     }
   }
@@ -522,24 +532,24 @@ oz_lane_kernel(const OzPlan P, Cx<T>* __restrict__ p) {
   // rotation back (:518-536) and the stores (:538-541)
   const int iq = info.z;
   const bool singular = info.w != 0;
-  const T alpha = static_cast<const T*>(P.palpha)[pair];
-  const T beta = T(1) - alpha;
-  const Cx<T>* clo = static_cast<const Cx<T>*>(P.ctab) + (size_t)iq * P.np_new;
-  const Cx<T>* chi = clo + P.np_new;
+  const C alpha = static_cast<const C*>(P.palpha)[pair];
+  const C beta = C(1) - alpha;
+  const Cx<C>* clo = static_cast<const Cx<C>*>(P.ctab) + (size_t)iq * P.np_new;
+  const Cx<C>* chi = clo + P.np_new;
 #pragma unroll
   for (int m = 0; m <= MMAX; ++m) {
     for (int mu2 = 0; mu2 <= m / mrso; ++mu2) {
-      Cx<T> gq[2 * MMAX + 1], gmq[2 * MMAX + 1];
+      Cx<C> gq[2 * MMAX + 1], gmq[2 * MMAX + 1];
 #pragma unroll
       for (int k = -m; k <= m; ++k) {
         int ia = P.ia_start[ipx(m, k, mu2)];
-        Cx<T> sq = mkc<T>(0, 0), smq = mkc<T>(0, 0);
+        Cx<C> sq = mkc<C>(C(0), C(0)), smq = mkc<C>(C(0), C(0));
 #pragma unroll
         for (int n = (k < 0 ? -k : k); n <= MMAX; ++n) {
           const int nn = n / mrso;
           for (int nu2 = -nn; nu2 <= nn; ++nu2, ++ia) {
-            const Cx<T> h = chi[ia], lo = clo[ia];
-            const Cx<T> c = mkc<T>(alpha * h.re + beta * lo.re, alpha * h.im + beta * lo.im);
+            const Cx<C> h = chi[ia], lo = clo[ia];
+            const Cx<C> c = mkc<C>(alpha * h.re + beta * lo.re, alpha * h.im + beta * lo.im);
             if (nu2 < 0) {
               const int j = ipx(n, k, -nu2) * 32 + lane;
               sq = cmac(sq, c, Dq[j]);
@@ -556,17 +566,18 @@ oz_lane_kernel(const OzPlan P, Cx<T>* __restrict__ p) {
       }
 #pragma unroll 1
       for (int a = -m; a <= m; ++a) {
-        Cx<T> x = mkc<T>(0, 0), y = mkc<T>(0, 0);
+        Cx<C> x = mkc<C>(C(0), C(0)), y = mkc<C>(C(0), C(0));
 #pragma unroll
         for (int k = -m; k <= m; ++k) {
           x = cmac(x, gq[k + m], conj(RT(m, a, k)));
           y = cmac(y, gmq[k + m], conj(RT(m, a, -k)));
         }
-        if (m & 1) y = mkc<T>(-y.re, -y.im);
+        if (m & 1) y = mkc<C>(-y.re, -y.im);
         if (valid) {
           const long long off = (long long)ipx(m, a, mu2) * N;
-          p[off + lq] = x;
-          p[off + lmq] = singular ? conj(y) : y;
+          const Cx<C> yy = singular ? conj(y) : y;
+          p[off + lq] = mkc<S>(to_storage<S>(x.re), to_storage<S>(x.im));
+          p[off + lmq] = mkc<S>(to_storage<S>(yy.re), to_storage<S>(yy.im));
         }
       }
     }
@@ -576,60 +587,61 @@ oz_lane_kernel(const OzPlan P, Cx<T>* __restrict__ p) {
 
 constexpr int kLaneMaxMmax = 6;
 
-template <typename T>
+template <typename C>
 size_t lane_smem_per_warp(int np) {
-  return (size_t)2 * np * 32 * sizeof(Cx<T>);
+  return (size_t)2 * np * 32 * sizeof(Cx<C>);
 }
 
 }  // namespace
 
-template <typename T>
+template <typename S, typename C>
 void oz_plan_finish(OzPlan& P) {
   // Lane path when one warp's shared columns fit with room for a few warps
   // per SM; otherwise the warp-per-pair kernel (R computed on the fly).
-  const size_t per_warp = lane_smem_per_warp<T>(P.np);
+  const size_t per_warp = lane_smem_per_warp<C>(P.np);
   P.lane_path = (P.mmax <= kLaneMaxMmax && per_warp <= 64 * 1024 && P.N < (1LL << 31)) ? 1 : 0;
   if (P.lane_path) {
     int w = (int)((200 * 1024) / per_warp);
     P.warps_per_cta = w < 1 ? 1 : (w > 8 ? 8 : w);
     P.smem = per_warp * P.warps_per_cta;
     switch (P.mmax) {
-      case 1: allow_max_smem(oz_lane_kernel<T, 1>, P.smem, "oz smem attribute"); break;
-      case 2: allow_max_smem(oz_lane_kernel<T, 2>, P.smem, "oz smem attribute"); break;
-      case 3: allow_max_smem(oz_lane_kernel<T, 3>, P.smem, "oz smem attribute"); break;
-      case 4: allow_max_smem(oz_lane_kernel<T, 4>, P.smem, "oz smem attribute"); break;
-      case 5: allow_max_smem(oz_lane_kernel<T, 5>, P.smem, "oz smem attribute"); break;
-      case 6: allow_max_smem(oz_lane_kernel<T, 6>, P.smem, "oz smem attribute"); break;
+      case 1: allow_max_smem(oz_lane_kernel<S, C, 1>, P.smem, "oz smem attribute"); break;
+      case 2: allow_max_smem(oz_lane_kernel<S, C, 2>, P.smem, "oz smem attribute"); break;
+      case 3: allow_max_smem(oz_lane_kernel<S, C, 3>, P.smem, "oz smem attribute"); break;
+      case 4: allow_max_smem(oz_lane_kernel<S, C, 4>, P.smem, "oz smem attribute"); break;
+      case 5: allow_max_smem(oz_lane_kernel<S, C, 5>, P.smem, "oz smem attribute"); break;
+      case 6: allow_max_smem(oz_lane_kernel<S, C, 6>, P.smem, "oz smem attribute"); break;
     }
     return;
   }
-  const OzSmem<T> L(P.mmax, P.np);
+  const OzSmem<S> L(P.mmax, P.np);
   P.warps_per_cta = 8;
   P.smem = L.per_warp * P.warps_per_cta;
   throw_if(P.smem > 200 * 1024, "mmax too large for the OZ kernel", 4);
-  allow_max_smem(oz_kernel<T>, P.smem, "oz smem attribute");
+  allow_max_smem(oz_kernel<S>, P.smem, "oz smem attribute");
 }
 
-template <typename T>
+template <typename C>
 void oz_build_rtab(const OzPlan& P, DevBuf& rtab) {
   const long long n = P.npairs_pad * (long long)P.nR;
+  constexpr bool keep64 = std::is_same<C, double>::value;
   DevBuf rt64;
-  DevBuf& target64 = sizeof(T) == sizeof(double) ? rtab : rt64;
+  DevBuf& target64 = keep64 ? rtab : rt64;
   target64.alloc(sizeof(Cx<double>) * (size_t)n);
   const long long nb = (P.npairs_pad + 127) / 128;
   clear_stale_error();
   rot_table_kernel<<<(unsigned)nb, 128>>>(P, target64.as<Cx<double>>());
   launch_check("R(q) table kernel launch");
-  if (sizeof(T) != sizeof(double)) {
-    rtab.alloc(sizeof(Cx<float>) * (size_t)n);
-    rot_table_to_f32<<<152 * 8, 256>>>(rt64.as<Cx<double>>(), rtab.as<Cx<float>>(), n);
+  if (!keep64) {
+    rtab.alloc(sizeof(Cx<C>) * (size_t)n);
+    rot_table_convert<C><<<152 * 8, 256>>>(rt64.as<Cx<double>>(), rtab.as<Cx<C>>(), n);
     launch_check("R(q) table conversion launch");
   }
   cuda_check(cudaDeviceSynchronize(), "R(q) table build");
 }
 
-template <typename T>
-void launch_oz(const OzPlan& P, Cx<T>* p, cudaStream_t s) {
+template <typename S, typename C>
+void launch_oz(const OzPlan& P, Cx<S>* p, cudaStream_t s) {
   if (P.npairs == 0) return;
   clear_stale_error();
   if (P.lane_path) {
@@ -638,27 +650,30 @@ void launch_oz(const OzPlan& P, Cx<T>* p, cudaStream_t s) {
     throw_if(nb > 0x7fffffffLL, "too many k-space pairs", 4);
     const dim3 grid((unsigned)nb), block(32 * P.warps_per_cta);
     switch (P.mmax) {
-      case 1: oz_lane_kernel<T, 1><<<grid, block, P.smem, s>>>(P, p); break;
-      case 2: oz_lane_kernel<T, 2><<<grid, block, P.smem, s>>>(P, p); break;
-      case 3: oz_lane_kernel<T, 3><<<grid, block, P.smem, s>>>(P, p); break;
-      case 4: oz_lane_kernel<T, 4><<<grid, block, P.smem, s>>>(P, p); break;
-      case 5: oz_lane_kernel<T, 5><<<grid, block, P.smem, s>>>(P, p); break;
-      case 6: oz_lane_kernel<T, 6><<<grid, block, P.smem, s>>>(P, p); break;
+      case 1: oz_lane_kernel<S, C, 1><<<grid, block, P.smem, s>>>(P, p); break;
+      case 2: oz_lane_kernel<S, C, 2><<<grid, block, P.smem, s>>>(P, p); break;
+      case 3: oz_lane_kernel<S, C, 3><<<grid, block, P.smem, s>>>(P, p); break;
+      case 4: oz_lane_kernel<S, C, 4><<<grid, block, P.smem, s>>>(P, p); break;
+      case 5: oz_lane_kernel<S, C, 5><<<grid, block, P.smem, s>>>(P, p); break;
+      case 6: oz_lane_kernel<S, C, 6><<<grid, block, P.smem, s>>>(P, p); break;
       default: throw Error(4, "mmax outside the lane kernel's range");
     }
     launch_check("oz lane kernel launch");
     return;
   }
   const long long nb = (P.npairs + P.warps_per_cta - 1) / P.warps_per_cta;
-  oz_kernel<T><<<(unsigned)nb, 32 * P.warps_per_cta, P.smem, s>>>(P, p);
+  oz_kernel<S><<<(unsigned)nb, 32 * P.warps_per_cta, P.smem, s>>>(P, p);
   launch_check("oz kernel launch");
 }
 
-template void oz_plan_finish<double>(OzPlan&);
-template void oz_plan_finish<float>(OzPlan&);
+template void oz_plan_finish<double, double>(OzPlan&);
+template void oz_plan_finish<float, float>(OzPlan&);
+template void oz_plan_finish<double, DF>(OzPlan&);
 template void oz_build_rtab<double>(const OzPlan&, DevBuf&);
 template void oz_build_rtab<float>(const OzPlan&, DevBuf&);
-template void launch_oz<double>(const OzPlan&, Cx<double>*, cudaStream_t);
-template void launch_oz<float>(const OzPlan&, Cx<float>*, cudaStream_t);
+template void oz_build_rtab<DF>(const OzPlan&, DevBuf&);
+template void launch_oz<double, double>(const OzPlan&, Cx<double>*, cudaStream_t);
+template void launch_oz<float, float>(const OzPlan&, Cx<float>*, cudaStream_t);
+template void launch_oz<double, DF>(const OzPlan&, Cx<double>*, cudaStream_t);
 
 }  // namespace mdft

@@ -33,7 +33,15 @@ def _np(t):
 
 def _dtypes(prec):
     import torch
-    return (torch.float64, torch.complex128) if prec == "f64" else (torch.float32, torch.complex64)
+    return (torch.float32, torch.complex64) if prec == "f32" else (torch.float64, torch.complex128)
+
+
+def _tol(prec):
+    # f64 and f64df (FP64 fields, double-float arithmetic) share the 1e-12 bound
+    return TOL32 if prec == "f32" else TOL64
+
+
+PRECS = ["f64", "f32", "f64df"]
 
 
 OPT_CASES = [((2, 2, 2), 10, 10), ((3, 2, 2), 3, 2), ((2, 2, 1), 5, 1), ((2, 1, 2), 4, 3),
@@ -41,7 +49,7 @@ OPT_CASES = [((2, 2, 2), 10, 10), ((3, 2, 2), 3, 2), ((2, 2, 1), 5, 1), ((2, 1, 
              ((9, 7, 5), 4, 2), ((4, 4, 4), 6, 1)]
 
 
-@pytest.mark.parametrize("prec", ["f64", "f32"])
+@pytest.mark.parametrize("prec", PRECS)
 @pytest.mark.parametrize("n,mmax,mrso", OPT_CASES)
 def test_angl2proj(gpu_lib, n, mmax, mrso, prec):
     import torch
@@ -56,15 +64,15 @@ def test_angl2proj(gpu_lib, n, mmax, mrso, prec):
     xo = _t(x, rd)
     p = torch.zeros((o.np,) + tuple(n), dtype=cd, device="cuda")
     opt.angl2proj(xo, p)
-    assert rel_err(_np(p), ref) < (TOL64 if prec == "f64" else TOL32)
+    assert rel_err(_np(p), ref) < _tol(prec)
     # get_delta_rho fused into the load
     rho0 = 0.3
     opt.angl2proj_from_xi(xo, rho0, p)
     ref2 = o.angl2proj(O.delta_rho(x, rho0))
-    assert rel_err(_np(p), ref2) < (TOL64 if prec == "f64" else TOL32)
+    assert rel_err(_np(p), ref2) < _tol(prec)
 
 
-@pytest.mark.parametrize("prec", ["f64", "f32"])
+@pytest.mark.parametrize("prec", PRECS)
 @pytest.mark.parametrize("n,mmax,mrso", OPT_CASES)
 def test_proj2angl(gpu_lib, n, mmax, mrso, prec):
     import torch
@@ -80,7 +88,7 @@ def test_proj2angl(gpu_lib, n, mmax, mrso, prec):
     out = torch.zeros((o.N, o.ntheta, o.nphi, o.npsi), dtype=rd, device="cuda")
     pt = _t(p, cd)
     opt.proj2angl(pt, out)
-    assert rel_err(_np(out), ref) < (TOL64 if prec == "f64" else TOL32)
+    assert rel_err(_np(out), ref) < _tol(prec)
     # p is read only
     assert np.array_equal(_np(pt), p.astype(_np(pt).dtype))
 
@@ -115,7 +123,7 @@ FFT_SHAPES = [(2, 4, 5), (8, 8, 8), (6, 10, 12), (3, 5, 7), (32, 48, 5), (16, 16
               (80, 2, 3)]
 
 
-@pytest.mark.parametrize("prec", ["f64", "f32"])
+@pytest.mark.parametrize("prec", PRECS)
 @pytest.mark.parametrize("n", FFT_SHAPES)
 def test_fft3d_vs_numpy_and_cufft(gpu_lib, n, prec):
     import torch
@@ -128,7 +136,7 @@ def test_fft3d_vs_numpy_and_cufft(gpu_lib, n, prec):
     shp = (ag.m_np,) + tuple(n)
     x = rng.standard_normal(shp) + 1j * rng.standard_normal(shp)
     rd, cd = _dtypes(prec)
-    tol = 1e-13 if prec == "f64" else 2e-6
+    tol = {"f64": 1e-13, "f64df": 1e-13, "f32": 2e-6}[prec]
     for sign in (-1, 1):
         t = _t(x, cd)
         conv.fft(t, sign)
@@ -159,7 +167,7 @@ def _conv_pair(M, n, box, mmax, mrso, prec):
     return o, conv, idx, tab
 
 
-@pytest.mark.parametrize("prec", ["f64", "f32"])
+@pytest.mark.parametrize("prec", PRECS)
 @pytest.mark.parametrize("n,box,mmax,mrso", CONV_CASES)
 def test_conv_execute(gpu_lib, n, box, mmax, mrso, prec):
     M = gpu_lib
@@ -171,7 +179,7 @@ def test_conv_execute(gpu_lib, n, box, mmax, mrso, prec):
     rd, cd = _dtypes(prec)
     t = _t(p, cd)
     conv.execute(t)
-    assert rel_err(_np(t), ref) < (TOL64 if prec == "f64" else TOL32)
+    assert rel_err(_np(t), ref) < _tol(prec)
 
 
 def test_conv_tables_match_oracle(gpu_lib):
@@ -246,7 +254,7 @@ def test_energy(gpu_lib, prec):
             assert abs(ff - ff_ref32) <= 1e-12 * abs(ff_ref32)
 
 
-@pytest.mark.parametrize("prec", ["f64", "f32"])
+@pytest.mark.parametrize("prec", PRECS)
 def test_energy_cproj_pipeline_32cubed(gpu_lib, prec):
     """The five stages of Solver::energy_cproj_mrso (src/mini-mdft.hpp:137-183)
     on the 32^3 / 20 A / mmax 3 / mrso 2 configuration, against the oracle:
@@ -274,7 +282,7 @@ def test_energy_cproj_pipeline_32cubed(gpu_lib, prec):
     M.get_delta_rho(xt, drt, rho0)
     p = torch.zeros((o.np,) + n, dtype=cd, device="cuda")
     opt.angl2proj(drt, p)
-    tol = TOL64 if prec == "f64" else TOL32
+    tol = _tol(prec)
     assert rel_err(_np(p), p_ref) < tol
     conv.execute(p)
     assert rel_err(_np(p), pc_ref) < tol
@@ -284,4 +292,4 @@ def test_energy_cproj_pipeline_32cubed(gpu_lib, prec):
     df = torch.zeros_like(xt)
     ff = M.get_delta_f(xt, vexc, torch.from_numpy(w), df, rho0, pref)
     assert rel_err(_np(df), df_ref) < tol
-    assert abs(ff - ff_ref) <= (1e-12 if prec == "f64" else 1e-6) * abs(ff_ref)
+    assert abs(ff - ff_ref) <= (1e-6 if prec == "f32" else 1e-12) * abs(ff_ref)
