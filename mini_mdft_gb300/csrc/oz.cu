@@ -476,17 +476,21 @@ struct PIndex {
 };
 
 template <typename S, typename C, int MMAX>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 2)
 oz_lane_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
   extern __shared__ __align__(16) unsigned char sm[];
+  // Two lanes per pair: lane i (< 16) carries the q side of pair i of the
+  // warp's 16, lane i + 16 its -q side.  Each lane keeps its rotated
+  // projections in its own shared column; the OZ product reads the partner's
+  // column for the conjugated terms.
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const long long blk = (long long)blockIdx.x * P.warps_per_cta + wib;
-  if (blk * 32 >= P.npairs) return;  // whole warp exits together
-  const long long pair = blk * 32 + lane;
+  const int side = lane >> 4;
+  const long long grp = (long long)blockIdx.x * P.warps_per_cta + wib;
+  if (grp * 16 >= P.npairs) return;  // whole warp exits together
+  const long long pair = grp * 16 + (lane & 15);
   const bool valid = pair < P.npairs;
   const int np = P.np, mrso = P.mrso;
-  Cx<C>* Dq = reinterpret_cast<Cx<C>*>(sm + (size_t)wib * 2 * np * 32 * sizeof(Cx<C>));
-  Cx<C>* Dmq = Dq + (size_t)np * 32;
+  Cx<C>* D = reinterpret_cast<Cx<C>*>(sm + (size_t)wib * np * 32 * sizeof(Cx<C>));
   PIndex ipx;
   ipx.mrso = mrso;
   {
@@ -498,36 +502,35 @@ oz_lane_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
     }
   }
   const int4 info = P.pinfo[pair];
-  const long long N = P.N, lq = info.x, lmq = info.y;
-  const Cx<C>* Rt = static_cast<const Cx<C>*>(P.rtab) + blk * (long long)P.nR * 32 + lane;
+  const long long N = P.N;
+  const long long lown = side ? info.y : info.x;
+  // the q side does not store at self-paired k-points: the -q store wins
+  const bool store = valid && (side == 1 || info.x != info.y);
+  const int ks = side ? -1 : 1;  // R(m, mup, +-khi)
+  const Cx<C>* Rt = static_cast<const Cx<C>*>(P.rtab) + (pair >> 5) * (long long)P.nR * 32 + (pair & 31);
 #define RT(l, m, m1) Rt[(roff(l) + ((m) + (l)) * (2 * (l) + 1) + ((m1) + (l))) * 32]
 
   // rotation to the q frame (MDFT_Convolution.hpp:427-443), block by block
 #pragma unroll
   for (int m = 0; m <= MMAX; ++m) {
     for (int mu2 = 0; mu2 <= m / mrso; ++mu2) {
-      Cx<C> gq[2 * MMAX + 1], gmq[2 * MMAX + 1];
+      Cx<C> g[2 * MMAX + 1];
 #pragma unroll
       for (int a = 0; a <= 2 * m; ++a) {
-        const long long off = (long long)ipx(m, a - m, mu2) * N;
-        const Cx<S> u = p[off + lq], v = p[off + lmq];
-        gq[a] = mkc<C>(to_compute<C>(u.re), to_compute<C>(u.im));
-        gmq[a] = mkc<C>(to_compute<C>(v.re), to_compute<C>(v.im));
+        const Cx<S> u = p[(long long)ipx(m, a - m, mu2) * N + lown];
+        g[a] = mkc<C>(to_compute<C>(u.re), to_compute<C>(u.im));
       }
 #pragma unroll 1
       for (int k = -m; k <= m; ++k) {
-        Cx<C> x = mkc<C>(C(0), C(0)), y = mkc<C>(C(0), C(0));
+        Cx<C> x = mkc<C>(C(0), C(0));
 #pragma unroll
-        for (int a = 0; a <= 2 * m; ++a) {
-          x = cmac(x, gq[a], RT(m, a - m, k));
-          y = cmac(y, gmq[a], RT(m, a - m, -k));
-        }
-        const int j = ipx(m, k, mu2) * 32 + lane;
-        Dq[j] = x;
-        Dmq[j] = (m & 1) ? mkc<C>(-y.re, -y.im) : y;
+        for (int a = 0; a <= 2 * m; ++a) x = cmac(x, g[a], RT(m, a - m, ks * k));
+        if (side && (m & 1)) x = mkc<C>(-x.re, -x.im);
+        D[ipx(m, k, mu2) * 32 + lane] = x;
       }
     }
   }
+  __syncwarp();
   // OZ with c(|q|) interpolated on the fly (:449-496), chop (:514-517),
   // rotation back (:518-536) and the stores (:538-541)
   const int iq = info.z;
@@ -536,49 +539,37 @@ oz_lane_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
   const C beta = C(1) - alpha;
   const Cx<C>* clo = static_cast<const Cx<C>*>(P.ctab) + (size_t)iq * P.np_new;
   const Cx<C>* chi = clo + P.np_new;
+  const int other = lane ^ 16;
 #pragma unroll
   for (int m = 0; m <= MMAX; ++m) {
     for (int mu2 = 0; mu2 <= m / mrso; ++mu2) {
-      Cx<C> gq[2 * MMAX + 1], gmq[2 * MMAX + 1];
+      Cx<C> g[2 * MMAX + 1];
 #pragma unroll
       for (int k = -m; k <= m; ++k) {
         int ia = P.ia_start[ipx(m, k, mu2)];
-        Cx<C> sq = mkc<C>(C(0), C(0)), smq = mkc<C>(C(0), C(0));
+        Cx<C> sacc = mkc<C>(C(0), C(0));
 #pragma unroll
         for (int n = (k < 0 ? -k : k); n <= MMAX; ++n) {
           const int nn = n / mrso;
           for (int nu2 = -nn; nu2 <= nn; ++nu2, ++ia) {
             const Cx<C> h = chi[ia], lo = clo[ia];
             const Cx<C> c = mkc<C>(alpha * h.re + beta * lo.re, alpha * h.im + beta * lo.im);
-            if (nu2 < 0) {
-              const int j = ipx(n, k, -nu2) * 32 + lane;
-              sq = cmac(sq, c, Dq[j]);
-              smq = cmac(smq, c, Dmq[j]);
-            } else {
-              const int j = ipx(n, k, nu2) * 32 + lane;
-              sq = cmac(sq, c, conj(Dmq[j]));
-              smq = cmac(smq, c, conj(Dq[j]));
-            }
+            if (nu2 < 0)
+              sacc = cmac(sacc, c, D[ipx(n, k, -nu2) * 32 + lane]);
+            else
+              sacc = cmac(sacc, c, conj(D[ipx(n, k, nu2) * 32 + other]));
           }
         }
-        gq[k + m] = chop(sq);
-        gmq[k + m] = chop(smq);
+        g[k + m] = chop(sacc);
       }
 #pragma unroll 1
       for (int a = -m; a <= m; ++a) {
-        Cx<C> x = mkc<C>(C(0), C(0)), y = mkc<C>(C(0), C(0));
+        Cx<C> x = mkc<C>(C(0), C(0));
 #pragma unroll
-        for (int k = -m; k <= m; ++k) {
-          x = cmac(x, gq[k + m], conj(RT(m, a, k)));
-          y = cmac(y, gmq[k + m], conj(RT(m, a, -k)));
-        }
-        if (m & 1) y = mkc<C>(-y.re, -y.im);
-        if (valid) {
-          const long long off = (long long)ipx(m, a, mu2) * N;
-          const Cx<C> yy = singular ? conj(y) : y;
-          p[off + lq] = mkc<S>(to_storage<S>(x.re), to_storage<S>(x.im));
-          p[off + lmq] = mkc<S>(to_storage<S>(yy.re), to_storage<S>(yy.im));
-        }
+        for (int k = -m; k <= m; ++k) x = cmac(x, g[k + m], conj(RT(m, a, ks * k)));
+        if (side && (m & 1)) x = mkc<C>(-x.re, -x.im);
+        if (side && singular) x = conj(x);
+        if (store) p[(long long)ipx(m, a, mu2) * N + lown] = mkc<S>(to_storage<S>(x.re), to_storage<S>(x.im));
       }
     }
   }
@@ -589,7 +580,7 @@ constexpr int kLaneMaxMmax = 6;
 
 template <typename C>
 size_t lane_smem_per_warp(int np) {
-  return (size_t)2 * np * 32 * sizeof(Cx<C>);
+  return (size_t)np * 32 * sizeof(Cx<C>);  // 16 pairs x 2 sides per warp
 }
 
 }  // namespace
@@ -599,9 +590,10 @@ void oz_plan_finish(OzPlan& P) {
   // Lane path when one warp's shared columns fit with room for a few warps
   // per SM; otherwise the warp-per-pair kernel (R computed on the fly).
   const size_t per_warp = lane_smem_per_warp<C>(P.np);
-  P.lane_path = (P.mmax <= kLaneMaxMmax && per_warp <= 64 * 1024 && P.N < (1LL << 31)) ? 1 : 0;
+  P.lane_path = (P.mmax <= kLaneMaxMmax && per_warp <= 48 * 1024 && P.N < (1LL << 31)) ? 1 : 0;
   if (P.lane_path) {
-    int w = (int)((200 * 1024) / per_warp);
+    // at most ~100 KB per CTA so that two CTAs share an SM
+    int w = (int)((100 * 1024) / per_warp);
     P.warps_per_cta = w < 1 ? 1 : (w > 8 ? 8 : w);
     P.smem = per_warp * P.warps_per_cta;
     switch (P.mmax) {
@@ -645,8 +637,8 @@ void launch_oz(const OzPlan& P, Cx<S>* p, cudaStream_t s) {
   if (P.npairs == 0) return;
   clear_stale_error();
   if (P.lane_path) {
-    const long long nblk = P.npairs_pad / 32;
-    const long long nb = (nblk + P.warps_per_cta - 1) / P.warps_per_cta;
+    const long long ngrp = (P.npairs + 15) / 16;  // 16 pairs per warp
+    const long long nb = (ngrp + P.warps_per_cta - 1) / P.warps_per_cta;
     throw_if(nb > 0x7fffffffLL, "too many k-space pairs", 4);
     const dim3 grid((unsigned)nb), block(32 * P.warps_per_cta);
     switch (P.mmax) {
