@@ -101,6 +101,46 @@ __host__ __device__ __forceinline__ bool df_abs_lt(DF x, float e) {
   return h < e || (h == e && (x.hi > 0.f ? x.lo < 0.f : x.lo > 0.f));
 }
 
+// double <-> double-float conversions built from the IEEE bit fields, so
+// that they run on the integer and FP32 pipes: the hardware double<->float
+// conversions and the FP64 add they need share this GPU's narrow FP64 pipe.
+#ifdef __CUDA_ARCH__
+__device__ __forceinline__ DF df_from_double_dev(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi32 = (unsigned)(b >> 32), lo32 = (unsigned)b;
+  const unsigned e = (hi32 >> 20) & 0x7ffu;  // biased exponent
+  const unsigned sign = hi32 & 0x80000000u;
+  if ((b << 1) == 0) return DF(__uint_as_float(sign), 0.f);  // +-0
+  // 2^-73 <= |x| < 2^128: hi (x truncated to 24 bits) and lo (the rest,
+  // truncated to 24 bits) are normal floats
+  if (e >= 950u && e <= 1150u) {
+    const unsigned m23 = ((hi32 & 0x000fffffu) << 3) | (lo32 >> 29);
+    const float h = __uint_as_float(sign | ((e - 896u) << 23) | m23);
+    const unsigned r = lo32 & 0x1fffffffu;  // remaining 29 mantissa bits
+    float l = 0.f;
+    if (r) {
+      const int top = 31 - __clz(r);  // leading bit, 0..28
+      const unsigned mr = top >= 23 ? (r >> (top - 23)) : (r << (23 - top));
+      const unsigned lexp = e - 948u + (unsigned)top;  // biased exponent of lo, 2..230
+      l = __uint_as_float(sign | (lexp << 23) | (mr & 0x7fffffu));
+    }
+    return df_fast_two_sum(h, l);
+  }
+  return DF(x);  // tiny, huge, inf, nan: hardware conversions
+}
+__device__ __forceinline__ double f2d_bits(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned ex = (u >> 23) & 0xffu;
+  if ((u << 1) == 0) return __longlong_as_double((long long)((unsigned long long)u << 32));  // +-0
+  if (ex == 0u || ex == 0xffu) return (double)f;  // denormal, inf, nan
+  const unsigned long long bits = ((unsigned long long)(u & 0x80000000u) << 32) |
+                                  ((unsigned long long)(ex + 896u) << 52) |
+                                  ((unsigned long long)(u & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+__device__ __forceinline__ double df_to_double_dev(DF a) { return f2d_bits(a.hi) + f2d_bits(a.lo); }
+#endif
+
 // Storage <-> compute conversions (identity unless the compute type is DF).
 template <typename C, typename S>
 __host__ __device__ __forceinline__ C to_compute(S x) {
@@ -108,7 +148,11 @@ __host__ __device__ __forceinline__ C to_compute(S x) {
 }
 template <>
 __host__ __device__ __forceinline__ DF to_compute<DF, double>(double x) {
+#ifdef __CUDA_ARCH__
+  return df_from_double_dev(x);
+#else
   return DF(x);
+#endif
 }
 template <typename S, typename C>
 __host__ __device__ __forceinline__ S to_storage(C x) {
@@ -116,7 +160,11 @@ __host__ __device__ __forceinline__ S to_storage(C x) {
 }
 template <>
 __host__ __device__ __forceinline__ double to_storage<double, DF>(DF x) {
+#ifdef __CUDA_ARCH__
+  return df_to_double_dev(x);
+#else
   return (double)x;
+#endif
 }
 
 inline void cuda_check(cudaError_t e, const char* what) {

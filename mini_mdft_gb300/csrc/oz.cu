@@ -576,11 +576,130 @@ oz_lane_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
 #undef RT
 }
 
+// One lane per pair (both sides in one thread): used for FP64 arithmetic,
+// where the FP64 pipe, not latency, bounds the kernel and splitting the pair
+// would repeat the interpolation of c(|q|) on both lanes.
+template <typename S, typename C, int MMAX>
+__global__ void __launch_bounds__(256)
+oz_lane1_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const long long blk = (long long)blockIdx.x * P.warps_per_cta + wib;
+  if (blk * 32 >= P.npairs) return;  // whole warp exits together
+  const long long pair = blk * 32 + lane;
+  const bool valid = pair < P.npairs;
+  const int np = P.np, mrso = P.mrso;
+  Cx<C>* Dq = reinterpret_cast<Cx<C>*>(sm + (size_t)wib * 2 * np * 32 * sizeof(Cx<C>));
+  Cx<C>* Dmq = Dq + (size_t)np * 32;
+  PIndex ipx;
+  ipx.mrso = mrso;
+  {
+    int b = 0;
+#pragma unroll
+    for (int m = 0; m <= MMAX; ++m) {
+      ipx.base[m] = b;
+      b += (2 * m + 1) * (m / mrso + 1);
+    }
+  }
+  const int4 info = P.pinfo[pair];
+  const long long N = P.N, lq = info.x, lmq = info.y;
+  const Cx<C>* Rt = static_cast<const Cx<C>*>(P.rtab) + blk * (long long)P.nR * 32 + lane;
+#define RT(l, m, m1) Rt[(roff(l) + ((m) + (l)) * (2 * (l) + 1) + ((m1) + (l))) * 32]
+
+  // rotation to the q frame (MDFT_Convolution.hpp:427-443), block by block
+#pragma unroll
+  for (int m = 0; m <= MMAX; ++m) {
+    for (int mu2 = 0; mu2 <= m / mrso; ++mu2) {
+      Cx<C> gq[2 * MMAX + 1], gmq[2 * MMAX + 1];
+#pragma unroll
+      for (int a = 0; a <= 2 * m; ++a) {
+        const long long off = (long long)ipx(m, a - m, mu2) * N;
+        const Cx<S> u = p[off + lq], v = p[off + lmq];
+        gq[a] = mkc<C>(to_compute<C>(u.re), to_compute<C>(u.im));
+        gmq[a] = mkc<C>(to_compute<C>(v.re), to_compute<C>(v.im));
+      }
+#pragma unroll 1
+      for (int k = -m; k <= m; ++k) {
+        Cx<C> x = mkc<C>(C(0), C(0)), y = mkc<C>(C(0), C(0));
+#pragma unroll
+        for (int a = 0; a <= 2 * m; ++a) {
+          x = cmac(x, gq[a], RT(m, a - m, k));
+          y = cmac(y, gmq[a], RT(m, a - m, -k));
+        }
+        const int j = ipx(m, k, mu2) * 32 + lane;
+        Dq[j] = x;
+        Dmq[j] = (m & 1) ? mkc<C>(-y.re, -y.im) : y;
+      }
+    }
+  }
+  // OZ with c(|q|) interpolated on the fly (:449-496), chop (:514-517),
+  // rotation back (:518-536) and the stores (:538-541)
+  const int iq = info.z;
+  const bool singular = info.w != 0;
+  const C alpha = static_cast<const C*>(P.palpha)[pair];
+  const C beta = C(1) - alpha;
+  const Cx<C>* clo = static_cast<const Cx<C>*>(P.ctab) + (size_t)iq * P.np_new;
+  const Cx<C>* chi = clo + P.np_new;
+#pragma unroll
+  for (int m = 0; m <= MMAX; ++m) {
+    for (int mu2 = 0; mu2 <= m / mrso; ++mu2) {
+      Cx<C> gq[2 * MMAX + 1], gmq[2 * MMAX + 1];
+#pragma unroll
+      for (int k = -m; k <= m; ++k) {
+        int ia = P.ia_start[ipx(m, k, mu2)];
+        Cx<C> sq = mkc<C>(C(0), C(0)), smq = mkc<C>(C(0), C(0));
+#pragma unroll
+        for (int n = (k < 0 ? -k : k); n <= MMAX; ++n) {
+          const int nn = n / mrso;
+          for (int nu2 = -nn; nu2 <= nn; ++nu2, ++ia) {
+            const Cx<C> h = chi[ia], lo = clo[ia];
+            const Cx<C> c = mkc<C>(alpha * h.re + beta * lo.re, alpha * h.im + beta * lo.im);
+            if (nu2 < 0) {
+              const int j = ipx(n, k, -nu2) * 32 + lane;
+              sq = cmac(sq, c, Dq[j]);
+              smq = cmac(smq, c, Dmq[j]);
+            } else {
+              const int j = ipx(n, k, nu2) * 32 + lane;
+              sq = cmac(sq, c, conj(Dmq[j]));
+              smq = cmac(smq, c, conj(Dq[j]));
+            }
+          }
+        }
+        gq[k + m] = chop(sq);
+        gmq[k + m] = chop(smq);
+      }
+#pragma unroll 1
+      for (int a = -m; a <= m; ++a) {
+        Cx<C> x = mkc<C>(C(0), C(0)), y = mkc<C>(C(0), C(0));
+#pragma unroll
+        for (int k = -m; k <= m; ++k) {
+          x = cmac(x, gq[k + m], conj(RT(m, a, k)));
+          y = cmac(y, gmq[k + m], conj(RT(m, a, -k)));
+        }
+        if (m & 1) y = mkc<C>(-y.re, -y.im);
+        if (valid) {
+          const long long off = (long long)ipx(m, a, mu2) * N;
+          const Cx<C> yy = singular ? conj(y) : y;
+          p[off + lq] = mkc<S>(to_storage<S>(x.re), to_storage<S>(x.im));
+          p[off + lmq] = mkc<S>(to_storage<S>(yy.re), to_storage<S>(yy.im));
+        }
+      }
+    }
+  }
+#undef RT
+}
+
 constexpr int kLaneMaxMmax = 6;
 
 template <typename C>
+constexpr bool split_pairs() {
+  return !std::is_same<C, double>::value;
+}
+
+template <typename C>
 size_t lane_smem_per_warp(int np) {
-  return (size_t)np * 32 * sizeof(Cx<C>);  // 16 pairs x 2 sides per warp
+  // split: 16 pairs x 2 sides per warp; unsplit: 32 pairs x (q, -q)
+  return (size_t)np * 32 * sizeof(Cx<C>) * (split_pairs<C>() ? 1 : 2);
 }
 
 }  // namespace
@@ -590,20 +709,26 @@ void oz_plan_finish(OzPlan& P) {
   // Lane path when one warp's shared columns fit with room for a few warps
   // per SM; otherwise the warp-per-pair kernel (R computed on the fly).
   const size_t per_warp = lane_smem_per_warp<C>(P.np);
-  P.lane_path = (P.mmax <= kLaneMaxMmax && per_warp <= 48 * 1024 && P.N < (1LL << 31)) ? 1 : 0;
+  P.lane_path = (P.mmax <= kLaneMaxMmax && per_warp <= 64 * 1024 && P.N < (1LL << 31)) ? 1 : 0;
   if (P.lane_path) {
-    // at most ~100 KB per CTA so that two CTAs share an SM
-    int w = (int)((100 * 1024) / per_warp);
+    // split: at most ~100 KB per CTA so that two CTAs share an SM
+    int w = (int)(((split_pairs<C>() ? 100 : 200) * 1024) / per_warp);
     P.warps_per_cta = w < 1 ? 1 : (w > 8 ? 8 : w);
     P.smem = per_warp * P.warps_per_cta;
+#define MDFT_OZ_ATTR(K)                                                              \
+  if constexpr (split_pairs<C>())                                                  \
+    allow_max_smem(oz_lane_kernel<S, C, K>, P.smem, "oz smem attribute");          \
+  else                                                                             \
+    allow_max_smem(oz_lane1_kernel<S, C, K>, P.smem, "oz smem attribute");
     switch (P.mmax) {
-      case 1: allow_max_smem(oz_lane_kernel<S, C, 1>, P.smem, "oz smem attribute"); break;
-      case 2: allow_max_smem(oz_lane_kernel<S, C, 2>, P.smem, "oz smem attribute"); break;
-      case 3: allow_max_smem(oz_lane_kernel<S, C, 3>, P.smem, "oz smem attribute"); break;
-      case 4: allow_max_smem(oz_lane_kernel<S, C, 4>, P.smem, "oz smem attribute"); break;
-      case 5: allow_max_smem(oz_lane_kernel<S, C, 5>, P.smem, "oz smem attribute"); break;
-      case 6: allow_max_smem(oz_lane_kernel<S, C, 6>, P.smem, "oz smem attribute"); break;
+      case 1: MDFT_OZ_ATTR(1) break;
+      case 2: MDFT_OZ_ATTR(2) break;
+      case 3: MDFT_OZ_ATTR(3) break;
+      case 4: MDFT_OZ_ATTR(4) break;
+      case 5: MDFT_OZ_ATTR(5) break;
+      case 6: MDFT_OZ_ATTR(6) break;
     }
+#undef MDFT_OZ_ATTR
     return;
   }
   const OzSmem<S> L(P.mmax, P.np);
@@ -637,19 +762,26 @@ void launch_oz(const OzPlan& P, Cx<S>* p, cudaStream_t s) {
   if (P.npairs == 0) return;
   clear_stale_error();
   if (P.lane_path) {
-    const long long ngrp = (P.npairs + 15) / 16;  // 16 pairs per warp
+    const int per_warp_pairs = split_pairs<C>() ? 16 : 32;
+    const long long ngrp = (P.npairs + per_warp_pairs - 1) / per_warp_pairs;
     const long long nb = (ngrp + P.warps_per_cta - 1) / P.warps_per_cta;
     throw_if(nb > 0x7fffffffLL, "too many k-space pairs", 4);
     const dim3 grid((unsigned)nb), block(32 * P.warps_per_cta);
+#define MDFT_OZ_LAUNCH(K)                                             \
+  if constexpr (split_pairs<C>())                                   \
+    oz_lane_kernel<S, C, K><<<grid, block, P.smem, s>>>(P, p);      \
+  else                                                              \
+    oz_lane1_kernel<S, C, K><<<grid, block, P.smem, s>>>(P, p);
     switch (P.mmax) {
-      case 1: oz_lane_kernel<S, C, 1><<<grid, block, P.smem, s>>>(P, p); break;
-      case 2: oz_lane_kernel<S, C, 2><<<grid, block, P.smem, s>>>(P, p); break;
-      case 3: oz_lane_kernel<S, C, 3><<<grid, block, P.smem, s>>>(P, p); break;
-      case 4: oz_lane_kernel<S, C, 4><<<grid, block, P.smem, s>>>(P, p); break;
-      case 5: oz_lane_kernel<S, C, 5><<<grid, block, P.smem, s>>>(P, p); break;
-      case 6: oz_lane_kernel<S, C, 6><<<grid, block, P.smem, s>>>(P, p); break;
+      case 1: MDFT_OZ_LAUNCH(1) break;
+      case 2: MDFT_OZ_LAUNCH(2) break;
+      case 3: MDFT_OZ_LAUNCH(3) break;
+      case 4: MDFT_OZ_LAUNCH(4) break;
+      case 5: MDFT_OZ_LAUNCH(5) break;
+      case 6: MDFT_OZ_LAUNCH(6) break;
       default: throw Error(4, "mmax outside the lane kernel's range");
     }
+#undef MDFT_OZ_LAUNCH
     launch_check("oz lane kernel launch");
     return;
   }
