@@ -65,7 +65,7 @@ struct DF {
   __host__ __device__ constexpr DF(float h, float l) : hi(h), lo(l) {}
   __host__ __device__ constexpr DF(int v) : hi((float)v), lo(0.f) {}
   __host__ __device__ explicit DF(double x) : hi((float)x), lo((float)(x - (double)(float)x)) {}
-  __host__ __device__ explicit DF(long double x)
+  __host__ explicit DF(long double x)
       : hi((float)x), lo((float)(x - (long double)(float)x)) {}
   __host__ __device__ explicit operator double() const { return (double)hi + (double)lo; }
 };
