@@ -234,6 +234,8 @@ proj2angl_kernel(const AngPlan P, const Cx<S>* __restrict__ p, S* __restrict__ o
 
 template <typename S, typename C>
 void ang_plan_finish(AngPlan& P) {
+  P.fast = ang_fast_supported(P.mmax, P.mrso) ? 1 : 0;
+  if (P.fast) ang_fast_setup<S, C>(P);
   const size_t budget = 100 * 1024;
   int tp = 64;
   while (tp > 1 && A2PSmem<C>(P, tp).total > budget) tp /= 2;
@@ -254,6 +256,12 @@ template <typename S, typename C>
 void launch_angl2proj(const AngPlan& P, const S* o, Cx<S>* p, bool from_xi,
                       double rho0, cudaStream_t s) {
   if (P.N == 0) return;
+  if (P.fast) {
+    clear_stale_error();
+    ang_fast_a2p<S, C>(P, o, p, from_xi, rho0, s);
+    launch_check("angl2proj kernel launch");
+    return;
+  }
   const long long nb = (P.N + P.tile_a2p - 1) / P.tile_a2p;
   throw_if(nb > 0x7fffffffLL, "grid too large", 4);
   clear_stale_error();
@@ -267,6 +275,12 @@ void launch_angl2proj(const AngPlan& P, const S* o, Cx<S>* p, bool from_xi,
 template <typename S, typename C>
 void launch_proj2angl(const AngPlan& P, const Cx<S>* p, S* o, cudaStream_t s) {
   if (P.N == 0) return;
+  if (P.fast) {
+    clear_stale_error();
+    ang_fast_p2a<S, C>(P, p, o, s);
+    launch_check("proj2angl kernel launch");
+    return;
+  }
   const long long nb = (P.N + P.tile_p2a - 1) / P.tile_p2a;
   throw_if(nb > 0x7fffffffLL, "grid too large", 4);
   clear_stale_error();

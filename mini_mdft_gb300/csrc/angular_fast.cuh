@@ -1,0 +1,398 @@
+// angular_fast.cuh -- orientation <-> projection transforms specialised at
+// compile time for the angular grids of the workloads (mrso = 2, mmax 1..5).
+//
+// Same mathematics as angular.cu (angl2proj:
+// common/MDFT_OrientationProjectionTransform.hpp:270-380, proj2angl:
+// :391-484), restructured so that every loop bound and table index is a
+// compile-time constant:
+//   * one thread per (grid point, theta) runs the psi and phi DFTs in
+//     registers, using the input symmetries: the psi DFT has real input, so
+//     only kpsi = 0..K is formed with the (x_j +- x_{n-j}) pairing; the phi
+//     DFT of the real kpsi = 0 column forms half the outputs and conjugates
+//     the rest; the complex columns pair k with n - k;
+//   * one thread per (grid point, projection) forms the theta contraction,
+//     writing p in (np, N) layout with consecutive threads on consecutive
+//     points;
+//   * the point-major orientation tile is staged with one word of padding
+//     per point so that the per-thread rows are read bank-conflict-free.
+// S is the storage type of the fields, C the arithmetic type.
+#pragma once
+#include "common.cuh"
+
+namespace mdft {
+
+namespace {
+
+constexpr int np_of(int mmax, int mrso) {
+  int n = 0;
+  for (int m = 0; m <= mmax; ++m) n += (2 * m + 1) * (m / mrso + 1);
+  return n;
+}
+
+template <int MMAX, int MRSO>
+struct Shape {
+  static constexpr int NT = MMAX + 1;
+  static constexpr int NPHI = 2 * MMAX + 1;
+  static constexpr int K = MMAX / MRSO;
+  static constexpr int NPSI = 2 * K + 1;
+  static constexpr int ROW = NPHI * NPSI;  // values per (point, theta)
+  static constexpr int NO = NT * ROW;
+  static constexpr int NP = np_of(MMAX, MRSO);
+  static constexpr int LDO = NO + 1;  // padded point stride of the o tile
+  // projection index of (m, mup, mu2) in OrientationProjectionMap order
+  static constexpr int ip(int m, int mup, int mu2) {
+    return np_of(m - 1, MRSO) + (mup + m) * (m / MRSO + 1) + mu2;
+  }
+};
+
+template <typename C>
+constexpr int a2p_threads() {
+  return 256;
+}
+
+// points per CTA: keep the CTA's shared memory near 100 KB
+template <typename C, int MMAX, int MRSO>
+constexpr int pts_per_cta() {
+  using Sh = Shape<MMAX, MRSO>;
+  int pts = 128;
+  while (pts > 16) {
+    const long long bytes = (long long)pts * Sh::LDO * sizeof(C) +
+                            (long long)Sh::NT * (Sh::K + 1) * Sh::NPHI * pts * sizeof(Cx<C>);
+    if (bytes <= 104 * 1024) break;
+    pts /= 2;
+  }
+  return pts;
+}
+
+template <typename C, int MMAX, int MRSO>
+constexpr size_t fast_smem() {
+  using Sh = Shape<MMAX, MRSO>;
+  constexpr int PTS = pts_per_cta<C, MMAX, MRSO>();
+  const size_t a = ((size_t)PTS * Sh::LDO * sizeof(C) + 15) & ~size_t(15);
+  const size_t z = (size_t)Sh::NT * (Sh::K + 1) * Sh::NPHI * PTS * sizeof(Cx<C>);
+  return a + z;
+}
+
+template <typename C>
+__device__ __forceinline__ Cx<C> ldtw(const void* t, int i) {
+  return static_cast<const Cx<C>*>(t)[i];
+}
+
+template <typename S, typename C, int MMAX, int MRSO, bool FROM_XI>
+__global__ void __launch_bounds__(256)
+angl2proj_fast_kernel(const AngPlan P, const S* __restrict__ o, Cx<S>* __restrict__ p, C rho0) {
+  using Sh = Shape<MMAX, MRSO>;
+  constexpr int PTS = pts_per_cta<C, MMAX, MRSO>();
+  constexpr int NT = Sh::NT, NPHI = Sh::NPHI, NPSI = Sh::NPSI, K = Sh::K, NO = Sh::NO;
+  constexpr int LDO = Sh::LDO, NP = Sh::NP;
+  constexpr int HPHI = (NPHI - 1) / 2, HPSI = (NPSI - 1) / 2;
+  extern __shared__ __align__(16) unsigned char sm[];
+  C* ot = reinterpret_cast<C*>(sm);
+  Cx<C>* Zs = reinterpret_cast<Cx<C>*>(sm + (((size_t)PTS * LDO * sizeof(C) + 15) & ~size_t(15)));
+  const int tid = threadIdx.x;
+  const long long pt0 = (long long)blockIdx.x * PTS;
+  const int cnt = (int)min((long long)PTS, P.N - pt0);
+
+  // stage the contiguous o tile (and fold in get_delta_rho if asked)
+  const S* src = o + pt0 * NO;
+  for (int i = tid; i < cnt * NO; i += blockDim.x) {
+    const int q = i / NO, j = i - q * NO;
+    C v = to_compute<C>(src[i]);
+    if (FROM_XI) v = rho0 * (v * v - C(1));
+    ot[q * LDO + j] = v;
+  }
+  __syncthreads();
+
+  // psi and phi DFTs, one thread per (point, theta)
+  for (int w = tid; w < NT * PTS; w += blockDim.x) {
+    const int th = w / PTS, q = w - th * PTS;
+    if (q >= cnt) continue;
+    const C* x = ot + q * LDO + th * NPHI * NPSI;
+    Cx<C> Y[NPHI][K + 1];
+#pragma unroll
+    for (int f = 0; f < NPHI; ++f) {
+      const C* r = x + f * NPSI;
+      C s0 = r[0];
+#pragma unroll
+      for (int j = 1; j < NPSI; ++j) s0 = s0 + r[j];
+      Y[f][0] = mkc<C>(s0, C(0));
+#pragma unroll
+      for (int k = 1; k <= K; ++k) {
+        C re = r[0], im = C(0);
+#pragma unroll
+        for (int j = 1; j <= HPSI; ++j) {
+          const Cx<C> t = ldtw<C>(P.tw_psi, (k * j) % NPSI);
+          re = re + (r[j] + r[NPSI - j]) * t.re;
+          im = im + (r[j] - r[NPSI - j]) * t.im;
+        }
+        Y[f][k] = mkc<C>(re, im);
+      }
+    }
+    Cx<C>* zt = Zs + (size_t)th * (K + 1) * NPHI * PTS + q;
+    // kpsi = 0: real input, X(n-k) = conj(X(k))
+    {
+      C s0 = Y[0][0].re;
+#pragma unroll
+      for (int j = 1; j < NPHI; ++j) s0 = s0 + Y[j][0].re;
+      zt[(0 + MMAX) * PTS] = mkc<C>(s0, C(0));
+#pragma unroll
+      for (int k = 1; k <= HPHI; ++k) {
+        C re = Y[0][0].re, im = C(0);
+#pragma unroll
+        for (int j = 1; j <= HPHI; ++j) {
+          const Cx<C> t = ldtw<C>(P.tw_phi, (k * j) % NPHI);
+          re = re + (Y[j][0].re + Y[NPHI - j][0].re) * t.re;
+          im = im + (Y[j][0].re - Y[NPHI - j][0].re) * t.im;
+        }
+        // s_f(mup) = conj(o_hat(mup mod nphi)); mup = k and mup = -k
+        zt[(k + MMAX) * PTS] = mkc<C>(re, -im);
+        zt[(-k + MMAX) * PTS] = mkc<C>(re, im);
+      }
+    }
+    // kpsi >= 1: complex input, pair k with n - k
+#pragma unroll
+    for (int kp = 1; kp <= K; ++kp) {
+      Cx<C>* zk = zt + (size_t)kp * NPHI * PTS;
+      Cx<C> s0 = Y[0][kp];
+#pragma unroll
+      for (int j = 1; j < NPHI; ++j) s0 = s0 + Y[j][kp];
+      zk[(0 + MMAX) * PTS] = conj(s0);
+#pragma unroll
+      for (int k = 1; k <= HPHI; ++k) {
+        Cx<C> Pk = Y[0][kp], Qk = mkc<C>(C(0), C(0));
+#pragma unroll
+        for (int j = 1; j <= HPHI; ++j) {
+          const Cx<C> t = ldtw<C>(P.tw_phi, (k * j) % NPHI);  // (cos, -sin)
+          const Cx<C> A = Y[j][kp] + Y[NPHI - j][kp], B = Y[j][kp] - Y[NPHI - j][kp];
+          Pk = mkc<C>(Pk.re + A.re * t.re, Pk.im + A.im * t.re);
+          Qk = mkc<C>(Qk.re + B.re * t.im, Qk.im + B.im * t.im);
+        }
+        // X(k) = P + i Q', X(n-k) = P - i Q' with Q' = sum B (-sin) = Qk
+        const Cx<C> Xk = mkc<C>(Pk.re - Qk.im, Pk.im + Qk.re);
+        const Cx<C> Xn = mkc<C>(Pk.re + Qk.im, Pk.im - Qk.re);
+        zk[(k + MMAX) * PTS] = conj(Xk);
+        zk[(-k + MMAX) * PTS] = conj(Xn);
+      }
+    }
+  }
+  __syncthreads();
+
+  // theta contraction, one thread per (point, projection)
+  const C* coef = static_cast<const C*>(P.coef_a2p);
+  for (int w = tid; w < NP * PTS; w += blockDim.x) {
+    const int ip = w / PTS, q = w - ip * PTS;
+    if (q >= cnt) continue;
+    const int mupi = P.ip_mup[ip] + MMAX, mu2 = P.ip_mu2[ip];
+    const Cx<C>* z = Zs + ((size_t)mu2 * NPHI + mupi) * PTS + q;
+    Cx<C> sum = mkc<C>(C(0), C(0));
+#pragma unroll
+    for (int th = 0; th < NT; ++th) {
+      const Cx<C> v = z[(size_t)th * (K + 1) * NPHI * PTS];
+      const C c = coef[th * NP + ip];
+      sum = mkc<C>(sum.re + v.re * c, sum.im + v.im * c);
+    }
+    p[(long long)ip * P.N + pt0 + q] = mkc<S>(to_storage<S>(sum.re), to_storage<S>(sum.im));
+  }
+}
+
+template <typename S, typename C, int MMAX, int MRSO>
+__global__ void __launch_bounds__(256)
+proj2angl_fast_kernel(const AngPlan P, const Cx<S>* __restrict__ p, S* __restrict__ o) {
+  using Sh = Shape<MMAX, MRSO>;
+  constexpr int PTS = pts_per_cta<C, MMAX, MRSO>();
+  constexpr int NT = Sh::NT, NPHI = Sh::NPHI, NPSI = Sh::NPSI, K = Sh::K, NO = Sh::NO;
+  constexpr int LDO = Sh::LDO, NP = Sh::NP;
+  constexpr int HPHI = (NPHI - 1) / 2;
+  extern __shared__ __align__(16) unsigned char sm[];
+  C* ot = reinterpret_cast<C*>(sm);
+  Cx<C>* Ps = reinterpret_cast<Cx<C>*>(sm + (((size_t)PTS * LDO * sizeof(C) + 15) & ~size_t(15)));
+  const int tid = threadIdx.x;
+  const long long pt0 = (long long)blockIdx.x * PTS;
+  const int cnt = (int)min((long long)PTS, P.N - pt0);
+
+  // stage p(ip, pt0 .. pt0 + cnt) as Ps[ip][point]
+  for (int w = tid; w < NP * PTS; w += blockDim.x) {
+    const int ip = w / PTS, q = w - ip * PTS;
+    if (q >= cnt) continue;
+    const Cx<S> v = p[(long long)ip * P.N + pt0 + q];
+    Ps[w] = mkc<C>(to_compute<C>(v.re), to_compute<C>(v.im));
+  }
+  __syncthreads();
+
+  const C* coef = static_cast<const C*>(P.coef_p2a);
+  for (int w = tid; w < NT * PTS; w += blockDim.x) {
+    const int th = w / PTS, q = w - th * PTS;
+    if (q >= cnt) continue;
+    // synthesis over m (OPT:435-449) into FFT order: oh[kf][kp]
+    Cx<C> oh[NPHI][K + 1];
+#pragma unroll
+    for (int mup = -MMAX; mup <= MMAX; ++mup) {
+#pragma unroll
+      for (int kp = 0; kp <= K; ++kp) {
+        Cx<C> s = mkc<C>(C(0), C(0));
+        const int a = mup < 0 ? -mup : mup, b = MRSO * kp;
+        const int m0 = a > b ? a : b;
+#pragma unroll
+        for (int m = m0; m <= MMAX; ++m) {
+          const int ip = Sh::ip(m, mup, kp);
+          const Cx<C> v = Ps[ip * PTS + q];
+          const C c = coef[th * NP + ip];
+          s = mkc<C>(s.re + v.re * c, s.im + v.im * c);
+        }
+        const int kf = mup >= 0 ? mup : mup + NPHI;
+        oh[kf][kp] = conj(s);
+      }
+    }
+    // inverse phi DFT; for kpsi = 0 only the real part is used (C2R)
+    C u0[NPHI];
+    {
+      C s0 = oh[0][0].re;
+#pragma unroll
+      for (int k = 1; k < NPHI; ++k) s0 = s0 + oh[k][0].re;
+      u0[0] = s0;
+#pragma unroll
+      for (int f = 1; f <= HPHI; ++f) {
+        // Re sum_k oh(k) e^{+i 2 pi k f / n}, pairing k with n - k
+        C ca = oh[0][0].re, cb = C(0);
+#pragma unroll
+        for (int k = 1; k <= HPHI; ++k) {
+          const Cx<C> t = ldtw<C>(P.tw_phi, (k * f) % NPHI);  // (cos, -sin)
+          ca = ca + (oh[k][0].re + oh[NPHI - k][0].re) * t.re;
+          cb = cb + (oh[k][0].im - oh[NPHI - k][0].im) * t.im;
+        }
+        // Re(f) = ca + sum (im_k - im_{n-k}) sin = ca - cb ; Re(n-f) = ca + cb
+        u0[f] = ca + cb;
+        u0[NPHI - f] = ca - cb;
+      }
+    }
+    Cx<C> u[NPHI][K + 1 > 1 ? K + 1 : 2];
+#pragma unroll
+    for (int kp = 1; kp <= K; ++kp) {
+      Cx<C> s0 = oh[0][kp];
+#pragma unroll
+      for (int k = 1; k < NPHI; ++k) s0 = s0 + oh[k][kp];
+      u[0][kp] = s0;
+#pragma unroll
+      for (int f = 1; f <= HPHI; ++f) {
+        Cx<C> Pf = oh[0][kp], Qf = mkc<C>(C(0), C(0));
+#pragma unroll
+        for (int k = 1; k <= HPHI; ++k) {
+          const Cx<C> t = ldtw<C>(P.tw_phi, (k * f) % NPHI);
+          const Cx<C> A = oh[k][kp] + oh[NPHI - k][kp], B = oh[k][kp] - oh[NPHI - k][kp];
+          Pf = mkc<C>(Pf.re + A.re * t.re, Pf.im + A.im * t.re);
+          Qf = mkc<C>(Qf.re + B.re * t.im, Qf.im + B.im * t.im);
+        }
+        // backward: X(f) = P - i Q', X(n-f) = P + i Q', Q' = sum B (-sin) = Qf
+        u[f][kp] = mkc<C>(Pf.re + Qf.im, Pf.im - Qf.re);
+        u[NPHI - f][kp] = mkc<C>(Pf.re - Qf.im, Pf.im + Qf.re);
+      }
+    }
+    // C2R along psi: o = Re U0 + 2 sum_k Re(U_k e^{+2 pi i k psi/npsi})
+    C* out = ot + q * LDO + th * NPHI * NPSI;
+#pragma unroll
+    for (int f = 0; f < NPHI; ++f) {
+#pragma unroll
+      for (int j = 0; j < NPSI; ++j) {
+        C v = u0[f];
+#pragma unroll
+        for (int kp = 1; kp <= K; ++kp) {
+          const Cx<C> e = ldtw<C>(P.tw_psi, (kp * j) % NPSI);  // (cos, -sin)
+          v = v + C(2) * (u[f][kp].re * e.re + u[f][kp].im * e.im);
+        }
+        out[f * NPSI + j] = v;
+      }
+    }
+  }
+  __syncthreads();
+  S* dst = o + pt0 * NO;
+  for (int i = tid; i < cnt * NO; i += blockDim.x) {
+    const int q = i / NO, j = i - q * NO;
+    dst[i] = to_storage<S>(ot[q * LDO + j]);
+  }
+}
+
+template <typename S, typename C, int MMAX, int MRSO>
+void fast_attr() {
+  constexpr size_t sm = fast_smem<C, MMAX, MRSO>();
+  allow_max_smem(angl2proj_fast_kernel<S, C, MMAX, MRSO, false>, sm, "angl2proj smem attribute");
+  allow_max_smem(angl2proj_fast_kernel<S, C, MMAX, MRSO, true>, sm, "angl2proj smem attribute");
+  // proj2angl's second buffer holds NP complex per point instead of the Z tile
+  using Sh = Shape<MMAX, MRSO>;
+  constexpr int PTS = pts_per_cta<C, MMAX, MRSO>();
+  constexpr size_t sm2 = (((size_t)PTS * Sh::LDO * sizeof(C) + 15) & ~size_t(15)) +
+                         (size_t)Sh::NP * PTS * sizeof(Cx<C>);
+  allow_max_smem(proj2angl_fast_kernel<S, C, MMAX, MRSO>, sm2, "proj2angl smem attribute");
+}
+
+template <typename S, typename C, int MMAX, int MRSO>
+void fast_a2p(const AngPlan& P, const S* o, Cx<S>* p, bool from_xi, double rho0, cudaStream_t s) {
+  constexpr int PTS = pts_per_cta<C, MMAX, MRSO>();
+  constexpr size_t sm = fast_smem<C, MMAX, MRSO>();
+  const long long nb = (P.N + PTS - 1) / PTS;
+  throw_if(nb > 0x7fffffffLL, "grid too large", 4);
+  if (from_xi)
+    angl2proj_fast_kernel<S, C, MMAX, MRSO, true><<<(unsigned)nb, 256, sm, s>>>(P, o, p, C(rho0));
+  else
+    angl2proj_fast_kernel<S, C, MMAX, MRSO, false><<<(unsigned)nb, 256, sm, s>>>(P, o, p, C(rho0));
+}
+
+template <typename S, typename C, int MMAX, int MRSO>
+void fast_p2a(const AngPlan& P, const Cx<S>* p, S* o, cudaStream_t s) {
+  using Sh = Shape<MMAX, MRSO>;
+  constexpr int PTS = pts_per_cta<C, MMAX, MRSO>();
+  constexpr size_t sm2 = (((size_t)PTS * Sh::LDO * sizeof(C) + 15) & ~size_t(15)) +
+                         (size_t)Sh::NP * PTS * sizeof(Cx<C>);
+  const long long nb = (P.N + PTS - 1) / PTS;
+  throw_if(nb > 0x7fffffffLL, "grid too large", 4);
+  proj2angl_fast_kernel<S, C, MMAX, MRSO><<<(unsigned)nb, 256, sm2, s>>>(P, p, o);
+}
+
+}  // namespace
+
+#define MDFT_ANG_FAST_CASES(X) X(1, 2) X(2, 2) X(3, 2) X(4, 2) X(5, 2)
+
+inline bool ang_fast_supported_impl(int mmax, int mrso) {
+#define X(M, R) \
+  if (mmax == M && mrso == R) return true;
+  MDFT_ANG_FAST_CASES(X)
+#undef X
+  return false;
+}
+
+template <typename S, typename C>
+void ang_fast_setup(const AngPlan& P) {
+#define X(M, R)                            \
+  if (P.mmax == M && P.mrso == R) {        \
+    fast_attr<S, C, M, R>();               \
+    return;                                \
+  }
+  MDFT_ANG_FAST_CASES(X)
+#undef X
+  throw Error(4, "no specialised angular kernel for this grid");
+}
+
+template <typename S, typename C>
+void ang_fast_a2p(const AngPlan& P, const S* o, Cx<S>* p, bool from_xi, double rho0, cudaStream_t s) {
+#define X(M, R)                                          \
+  if (P.mmax == M && P.mrso == R) {                      \
+    fast_a2p<S, C, M, R>(P, o, p, from_xi, rho0, s);     \
+    return;                                              \
+  }
+  MDFT_ANG_FAST_CASES(X)
+#undef X
+  throw Error(4, "no specialised angular kernel for this grid");
+}
+
+template <typename S, typename C>
+void ang_fast_p2a(const AngPlan& P, const Cx<S>* p, S* o, cudaStream_t s) {
+#define X(M, R)                             \
+  if (P.mmax == M && P.mrso == R) {         \
+    fast_p2a<S, C, M, R>(P, p, o, s);       \
+    return;                                 \
+  }
+  MDFT_ANG_FAST_CASES(X)
+#undef X
+  throw Error(4, "no specialised angular kernel for this grid");
+}
+
+}  // namespace mdft

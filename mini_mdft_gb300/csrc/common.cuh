@@ -233,6 +233,7 @@ struct AngPlan {
   long long N;  // grid points
   int ntheta, nphi, npsi, K, mmax, mrso, np, no;
   int tile_a2p, tile_p2a;           // points per CTA
+  int fast;                         // 1: compile-time-shape kernels (angular_fast.cu)
   size_t smem_a2p, smem_p2a;        // dynamic shared memory bytes
   const void* coef_a2p;             // (ntheta, np) T : d * wtheta * fm / (nphi*npsi)
   const void* coef_p2a;             // (ntheta, np) T : d * fm
@@ -252,7 +253,15 @@ void launch_angl2proj(const AngPlan& P, const S* o, Cx<S>* p, bool from_xi,
 template <typename S, typename C>
 void launch_proj2angl(const AngPlan& P, const Cx<S>* p, S* o, cudaStream_t s);
 template <typename S, typename C>
-void ang_plan_finish(AngPlan& P);  // picks tiles / smem sizes, sets attributes
+void ang_plan_finish(AngPlan& P);
+// Compile-time-shape kernels for (mmax, mrso) in {1..5} x {2}.
+bool ang_fast_supported(int mmax, int mrso);
+template <typename S, typename C>
+void ang_fast_setup(const AngPlan& P);
+template <typename S, typename C>
+void ang_fast_a2p(const AngPlan& P, const S* o, Cx<S>* p, bool from_xi, double rho0, cudaStream_t s);
+template <typename S, typename C>
+void ang_fast_p2a(const AngPlan& P, const Cx<S>* p, S* o, cudaStream_t s);  // picks tiles / smem sizes, sets attributes
 
 // ---------------------------------------------------------------------------
 // Batched 1-D FFT along one axis of a (B, n, S) complex array.

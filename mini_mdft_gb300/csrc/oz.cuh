@@ -1,4 +1,4 @@
-// oz.cu -- the k-space step of Convolution::execute
+// oz.cuh -- the k-space step of Convolution::execute
 // (common/MDFT_Convolution.hpp:376-543), fused into one kernel.
 //
 // For each (q, -q) pair of the half-space pair list (:129-176) one warp:
@@ -19,6 +19,7 @@
 #include <cfloat>
 #include <type_traits>
 
+#pragma once
 #include "common.cuh"
 
 namespace mdft {
@@ -789,15 +790,5 @@ void launch_oz(const OzPlan& P, Cx<S>* p, cudaStream_t s) {
   oz_kernel<S><<<(unsigned)nb, 32 * P.warps_per_cta, P.smem, s>>>(P, p);
   launch_check("oz kernel launch");
 }
-
-template void oz_plan_finish<double, double>(OzPlan&);
-template void oz_plan_finish<float, float>(OzPlan&);
-template void oz_plan_finish<double, DF>(OzPlan&);
-template void oz_build_rtab<double>(const OzPlan&, DevBuf&);
-template void oz_build_rtab<float>(const OzPlan&, DevBuf&);
-template void oz_build_rtab<DF>(const OzPlan&, DevBuf&);
-template void launch_oz<double, double>(const OzPlan&, Cx<double>*, cudaStream_t);
-template void launch_oz<float, float>(const OzPlan&, Cx<float>*, cudaStream_t);
-template void launch_oz<double, DF>(const OzPlan&, Cx<double>*, cudaStream_t);
 
 }  // namespace mdft
