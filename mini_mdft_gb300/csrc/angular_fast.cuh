@@ -78,8 +78,9 @@ __device__ __forceinline__ Cx<C> ldtw(const void* t, int i) {
   return static_cast<const Cx<C>*>(t)[i];
 }
 
+// FP32: at most 128 registers so that two 256-thread CTAs share an SM
 template <typename S, typename C, int MMAX, int MRSO, bool FROM_XI>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, sizeof(C) == 4 ? 2 : 1)
 angl2proj_fast_kernel(const AngPlan P, const S* __restrict__ o, Cx<S>* __restrict__ p, C rho0) {
   using Sh = Shape<MMAX, MRSO>;
   constexpr int PTS = pts_per_cta<C, MMAX, MRSO>();
@@ -196,7 +197,7 @@ angl2proj_fast_kernel(const AngPlan P, const S* __restrict__ o, Cx<S>* __restric
 }
 
 template <typename S, typename C, int MMAX, int MRSO>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, sizeof(C) == 4 ? 2 : 1)
 proj2angl_fast_kernel(const AngPlan P, const Cx<S>* __restrict__ p, S* __restrict__ o) {
   using Sh = Shape<MMAX, MRSO>;
   constexpr int PTS = pts_per_cta<C, MMAX, MRSO>();

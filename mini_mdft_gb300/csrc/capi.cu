@@ -10,6 +10,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/mdft_gb300.h"
@@ -122,6 +123,9 @@ struct mdft_conv_s {
   std::vector<std::complex<double>> mnq;      // (np_new, nq) (getter)
   DevBuf pairs, kx, ky, kz, rot, pmap, ip_m, ip_mup, ip_mu2, ia_map, ctab, tw_x, tw_y, tw_z;
   DevBuf pinfo, palpha, ia_start, rtab;  // lane-per-pair OZ path
+  // double-float form: the projections stay packed DF pairs between the
+  // passes of execute() (needs the lane OZ path and one axis longer than 1)
+  bool df_packed = false;
   mdft::OzPlan oz{};
   mdft::FftAxis ax{}, ay{}, az{};
   explicit mdft_conv_s(const mdft::Grid& gg) : g(gg) {}
@@ -182,7 +186,15 @@ void fft_axis_build(mdft::FftAxis& a, DevBuf& twbuf, int n, long long S, long lo
   auto tw = twiddles<T>(n);
   twbuf.upload(tw.data(), sizeof(Cx<T>) * n);
   a.tw = twbuf.ptr;
-  mdft::fft_axis_finish<ST, T>(a);
+  if constexpr (std::is_same<T, mdft::DF>::value) {
+    // double-float: every load/store format the pass chains use
+    mdft::fft_axis_finish<double, double, T>(a);
+    mdft::fft_axis_finish<double, mdft::DF, T>(a);
+    mdft::fft_axis_finish<mdft::DF, mdft::DF, T>(a);
+    mdft::fft_axis_finish<mdft::DF, double, T>(a);
+  } else {
+    mdft::fft_axis_finish<ST, ST, T>(a);
+  }
 }
 
 template <typename S, typename T>
@@ -312,20 +324,50 @@ void conv_build(mdft_conv_s* h, const mdft::LucTable& t) {
   fft_axis_build<S, T>(h->az, h->tw_z, g.nz, 1, np * g.nx * g.ny);
   fft_axis_build<S, T>(h->ay, h->tw_y, g.ny, g.nz, np * g.nx * (long long)g.nz);
   fft_axis_build<S, T>(h->ax, h->tw_x, g.nx, (long long)g.ny * g.nz, np * (long long)g.ny * g.nz);
+  if constexpr (std::is_same<T, mdft::DF>::value) {
+    h->df_packed = O.lane_path && (g.nx > 1 || g.ny > 1 || g.nz > 1);
+    if (h->df_packed) mdft::oz_lane_attr<mdft::DF, mdft::DF>(O);
+  }
   (void)N;
 }
 
+// One 3-D transform as three axis passes (z, y, x forward; x, y, z
+// backward).  In the double-float form the passes of one chain keep the data
+// as packed DF pairs: the first pass converts from `in_packed` storage, the
+// last converts to `out_packed` storage.
 template <typename S, typename T>
-void conv_fft(mdft_conv_s* h, void* p, int sign, cudaStream_t s) {
-  auto* d = static_cast<Cx<S>*>(p);
+void conv_fft(mdft_conv_s* h, void* p, int sign, cudaStream_t s, bool in_packed = false,
+              bool out_packed = false) {
+  mdft::FftAxis* order[3];
   if (sign < 0) {
-    mdft::launch_fft_axis<S, T>(h->az, d, sign, s);
-    mdft::launch_fft_axis<S, T>(h->ay, d, sign, s);
-    mdft::launch_fft_axis<S, T>(h->ax, d, sign, s);
+    order[0] = &h->az;
+    order[1] = &h->ay;
+    order[2] = &h->ax;
   } else {
-    mdft::launch_fft_axis<S, T>(h->ax, d, sign, s);
-    mdft::launch_fft_axis<S, T>(h->ay, d, sign, s);
-    mdft::launch_fft_axis<S, T>(h->az, d, sign, s);
+    order[0] = &h->ax;
+    order[1] = &h->ay;
+    order[2] = &h->az;
+  }
+  if constexpr (std::is_same<T, mdft::DF>::value) {
+    mdft::FftAxis* live[3];
+    int nl = 0;
+    for (auto* a : order)
+      if (a->n > 1) live[nl++] = a;
+    throw_if(nl == 0 && in_packed != out_packed, "internal: no FFT pass to change the format", 4);
+    for (int i = 0; i < nl; ++i) {
+      const bool src = i == 0 ? in_packed : true;
+      const bool dst = i == nl - 1 ? out_packed : true;
+      if (!src && !dst)
+        mdft::launch_fft_axis<double, double, T>(*live[i], p, sign, s);
+      else if (!src && dst)
+        mdft::launch_fft_axis<double, mdft::DF, T>(*live[i], p, sign, s);
+      else if (src && dst)
+        mdft::launch_fft_axis<mdft::DF, mdft::DF, T>(*live[i], p, sign, s);
+      else
+        mdft::launch_fft_axis<mdft::DF, double, T>(*live[i], p, sign, s);
+    }
+  } else {
+    for (auto* a : order) mdft::launch_fft_axis<S, S, T>(*a, p, sign, s);
   }
 }
 
@@ -551,6 +593,14 @@ int mdft_conv_execute(mdft_conv_t h, void* p, void* stream) {
     with_types(h->prec, [&](auto st, auto ct) {
       using S = decltype(st);
       using C = decltype(ct);
+      if constexpr (std::is_same<C, mdft::DF>::value) {
+        if (h->df_packed) {
+          conv_fft<S, C>(h, p, -1, s, false, true);
+          mdft::launch_oz<mdft::DF, C>(h->oz, static_cast<Cx<mdft::DF>*>(p), s);
+          conv_fft<S, C>(h, p, +1, s, true, false);
+          return;
+        }
+      }
       conv_fft<S, C>(h, p, -1, s);
       mdft::launch_oz<S, C>(h->oz, static_cast<Cx<S>*>(p), s);
       conv_fft<S, C>(h, p, +1, s);

@@ -279,10 +279,13 @@ struct FftAxis {
   const void* tw;  // (n) Cx<T> : exp(-2 pi i t / n)
 };
 bool fft_factor(int n, FftAxis& a);  // false if n has a prime factor > 13
-template <typename S, typename C>
+// Si / So: storage type of the tile on load / store (the same size, in
+// place); the double-float form keeps the projections as packed DF pairs
+// between the passes of one convolution.
+template <typename Si, typename So, typename C>
 void fft_axis_finish(FftAxis& a);
-template <typename S, typename C>
-void launch_fft_axis(const FftAxis& a, Cx<S>* data, int sign, cudaStream_t s);
+template <typename Si, typename So, typename C>
+void launch_fft_axis(const FftAxis& a, void* data, int sign, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // Fused (q,-q) rotation + Ornstein-Zernike + rotation back.
@@ -320,6 +323,10 @@ template <typename C>
 void oz_build_rtab(const OzPlan& P, DevBuf& rtab);
 template <typename S, typename C>
 void launch_oz(const OzPlan& P, Cx<S>* p, cudaStream_t s);
+// Shared-memory attributes of the lane kernels for storage S (used for the
+// packed double-float storage inside one convolution).
+template <typename S, typename C>
+void oz_lane_attr(const OzPlan& P);
 
 // ---------------------------------------------------------------------------
 // Energy / gradient.

@@ -1,4 +1,4 @@
-// fft.cu -- batched in-place complex 1-D FFTs along one axis of the
+// fft.cuh -- batched in-place complex 1-D FFTs along one axis of the
 // projection array, the building block of the 3-D transforms of
 // Convolution::execute (common/MDFT_Convolution.hpp:198-208, :328, :546).
 //
@@ -14,11 +14,14 @@
 //
 // S is the storage type of the array (double or float), C the arithmetic
 // type (the same, or double-float DF for the FP64 form on the FP32 pipes).
+#pragma once
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace mdft {
 
-bool fft_factor(int n, FftAxis& a) {
+inline bool fft_factor_impl(int n, FftAxis& a) {
   a.n = n;
   a.nr = 0;
   int m = n;
@@ -99,10 +102,13 @@ __device__ __forceinline__ void small_dft(Cx<T>* v, int R, int sign, const Cx<T>
   }
 }
 
-// Runtime-radix kernel: any length whose prime factors are <= 13.
-template <typename S, typename C>
+// Runtime-radix kernel: any length whose prime factors are <= 13.  The tile
+// is loaded as Si and stored as So (same size; in place).
+template <typename Si, typename So, typename C>
 __global__ void __launch_bounds__(kFftThreads)
-fft_axis_kernel(const FftAxis A, Cx<S>* __restrict__ data, int sign) {
+fft_axis_kernel(const FftAxis A, void* __restrict__ vdata, int sign) {
+  const Cx<Si>* din = static_cast<const Cx<Si>*>(vdata);
+  Cx<So>* dout = static_cast<Cx<So>*>(vdata);
   extern __shared__ __align__(16) unsigned char sm[];
   const int n = A.n, CL = A.cols;
   Cx<C>* buf0 = reinterpret_cast<Cx<C>*>(sm);
@@ -115,7 +121,7 @@ fft_axis_kernel(const FftAxis A, Cx<S>* __restrict__ data, int sign) {
 
   for (int i = tid; i < n; i += bd) tw[i] = static_cast<const Cx<C>*>(A.tw)[i];
   if (S_ == 1) {
-    const Cx<S>* src = data + c0 * n;
+    const Cx<Si>* src = din + c0 * n;
     for (int i = tid; i < n * cc; i += bd) {
       const int c = i / n, j = i % n;
       buf0[j * CL + c] = ld_c<C>(src[i]);
@@ -125,7 +131,7 @@ fft_axis_kernel(const FftAxis A, Cx<S>* __restrict__ data, int sign) {
       const int j = i / cc, c = i % cc;
       const long long col = c0 + c;
       const long long b = col / S_, s = col % S_;
-      buf0[j * CL + c] = ld_c<C>(data[(b * n + j) * S_ + s]);
+      buf0[j * CL + c] = ld_c<C>(din[(b * n + j) * S_ + s]);
     }
   }
   Cx<C>* in = buf0;
@@ -156,17 +162,17 @@ fft_axis_kernel(const FftAxis A, Cx<S>* __restrict__ data, int sign) {
   }
   __syncthreads();
   if (S_ == 1) {
-    Cx<S>* dst = data + c0 * n;
+    Cx<So>* dst = dout + c0 * n;
     for (int i = tid; i < n * cc; i += bd) {
       const int c = i / n, j = i % n;
-      dst[i] = st_c<S>(in[j * CL + c]);
+      dst[i] = st_c<So>(in[j * CL + c]);
     }
   } else {
     for (int i = tid; i < n * cc; i += bd) {
       const int j = i / cc, c = i % cc;
       const long long col = c0 + c;
       const long long b = col / S_, s = col % S_;
-      data[(b * n + j) * S_ + s] = st_c<S>(in[j * CL + c]);
+      dout[(b * n + j) * S_ + s] = st_c<So>(in[j * CL + c]);
     }
   }
 }
@@ -276,9 +282,11 @@ __device__ __forceinline__ Cx<T>* stages(Cx<T>* in, Cx<T>* out, const Cx<T>* tw,
   return stages<T, N, LD, FWD, Ns * R>(out, in, tw, cols, cc, RList<Rest...>{});
 }
 
-template <typename S, typename C, int N, int COLS, bool FWD>
+template <typename Si, typename So, typename C, int N, int COLS, bool FWD>
 __global__ void __launch_bounds__(256)
-fft_fixed_kernel(const FftAxis A, Cx<S>* __restrict__ data) {
+fft_fixed_kernel(const FftAxis A, void* __restrict__ vdata) {
+  const Cx<Si>* din = static_cast<const Cx<Si>*>(vdata);
+  Cx<So>* dout = static_cast<Cx<So>*>(vdata);
   extern __shared__ __align__(16) unsigned char sm[];
   constexpr int LD = COLS + 1;  // padded column stride of the tile
   Cx<C>* buf0 = reinterpret_cast<Cx<C>*>(sm);
@@ -290,7 +298,7 @@ fft_fixed_kernel(const FftAxis A, Cx<S>* __restrict__ data) {
   const long long S_ = A.S;
   for (int i = tid; i < N; i += bd) tw[i] = static_cast<const Cx<C>*>(A.tw)[i];
   if (S_ == 1) {
-    const Cx<S>* src = data + c0 * N;
+    const Cx<Si>* src = din + c0 * N;
     for (int i = tid; i < N * cc; i += bd) {
       const int c = i / N, j = i % N;
       buf0[j * LD + c] = ld_c<C>(src[i]);
@@ -298,7 +306,7 @@ fft_fixed_kernel(const FftAxis A, Cx<S>* __restrict__ data) {
   } else {
     const long long b = c0 / S_, s0 = c0 % S_;
     if (s0 + cc <= S_) {  // the tile's columns are one contiguous run per row
-      const Cx<S>* base = data + b * N * S_ + s0;
+      const Cx<Si>* base = din + b * N * S_ + s0;
       for (int i = tid; i < N * COLS; i += bd) {
         const int j = i / COLS, c = i % COLS;
         if (c < cc) buf0[j * LD + c] = ld_c<C>(base[(long long)j * S_ + c]);
@@ -308,7 +316,7 @@ fft_fixed_kernel(const FftAxis A, Cx<S>* __restrict__ data) {
         const int j = i / COLS, c = i % COLS;
         if (c < cc) {
           const long long col = c0 + c, bb = col / S_, ss = col % S_;
-          buf0[j * LD + c] = ld_c<C>(data[(bb * N + j) * S_ + ss]);
+          buf0[j * LD + c] = ld_c<C>(din[(bb * N + j) * S_ + ss]);
         }
       }
     }
@@ -316,25 +324,25 @@ fft_fixed_kernel(const FftAxis A, Cx<S>* __restrict__ data) {
   Cx<C>* res = stages<C, N, LD, FWD, 1>(buf0, buf1, tw, COLS, cc, typename FftRadices<N>::type{});
   __syncthreads();
   if (S_ == 1) {
-    Cx<S>* dst = data + c0 * N;
+    Cx<So>* dst = dout + c0 * N;
     for (int i = tid; i < N * cc; i += bd) {
       const int c = i / N, j = i % N;
-      dst[i] = st_c<S>(res[j * LD + c]);
+      dst[i] = st_c<So>(res[j * LD + c]);
     }
   } else {
     const long long b = c0 / S_, s0 = c0 % S_;
     if (s0 + cc <= S_) {
-      Cx<S>* base = data + b * N * S_ + s0;
+      Cx<So>* base = dout + b * N * S_ + s0;
       for (int i = tid; i < N * COLS; i += bd) {
         const int j = i / COLS, c = i % COLS;
-        if (c < cc) base[(long long)j * S_ + c] = st_c<S>(res[j * LD + c]);
+        if (c < cc) base[(long long)j * S_ + c] = st_c<So>(res[j * LD + c]);
       }
     } else {
       for (int i = tid; i < N * COLS; i += bd) {
         const int j = i / COLS, c = i % COLS;
         if (c < cc) {
           const long long col = c0 + c, bb = col / S_, ss = col % S_;
-          data[(bb * N + j) * S_ + ss] = st_c<S>(res[j * LD + c]);
+          dout[(bb * N + j) * S_ + ss] = st_c<So>(res[j * LD + c]);
         }
       }
     }
@@ -352,23 +360,23 @@ size_t fixed_smem() {
   return sizeof(Cx<C>) * ((size_t)2 * N * LD + N);
 }
 
-template <typename S, typename C, int N>
+template <typename Si, typename So, typename C, int N>
 void fixed_attr() {
-  allow_max_smem(fft_fixed_kernel<S, C, N, fixed_cols<C>(), true>, fixed_smem<C, N>(),
+  allow_max_smem(fft_fixed_kernel<Si, So, C, N, fixed_cols<C>(), true>, fixed_smem<C, N>(),
                  "fft smem attribute");
-  allow_max_smem(fft_fixed_kernel<S, C, N, fixed_cols<C>(), false>, fixed_smem<C, N>(),
+  allow_max_smem(fft_fixed_kernel<Si, So, C, N, fixed_cols<C>(), false>, fixed_smem<C, N>(),
                  "fft smem attribute");
 }
 
-template <typename S, typename C, int N>
-void fixed_launch(const FftAxis& a, Cx<S>* data, int sign, cudaStream_t s) {
+template <typename Si, typename So, typename C, int N>
+void fixed_launch(const FftAxis& a, void* data, int sign, cudaStream_t s) {
   constexpr int COLS = fixed_cols<C>();
   const long long nb = (a.ncols + COLS - 1) / COLS;
   throw_if(nb > 0x7fffffffLL, "FFT batch too large", 4);
   if (sign < 0)
-    fft_fixed_kernel<S, C, N, COLS, true><<<(unsigned)nb, 256, fixed_smem<C, N>(), s>>>(a, data);
+    fft_fixed_kernel<Si, So, C, N, COLS, true><<<(unsigned)nb, 256, fixed_smem<C, N>(), s>>>(a, data);
   else
-    fft_fixed_kernel<S, C, N, COLS, false><<<(unsigned)nb, 256, fixed_smem<C, N>(), s>>>(a, data);
+    fft_fixed_kernel<Si, So, C, N, COLS, false><<<(unsigned)nb, 256, fixed_smem<C, N>(), s>>>(a, data);
 }
 
 #define MDFT_FIXED_SIZES(X) X(16) X(32) X(64) X(128) X(256) X(48) X(96) X(192) X(80) X(160)
@@ -383,12 +391,12 @@ bool fixed_supported(int n) {
   return false;
 }
 
-template <typename S, typename C>
+template <typename Si, typename So, typename C>
 void fixed_setup(int n, size_t& smem) {
   switch (n) {
 #define X(N)                      \
   case N:                         \
-    fixed_attr<S, C, N>();        \
+    fixed_attr<Si, So, C, N>();   \
     smem = fixed_smem<C, N>();    \
     return;
     MDFT_FIXED_SIZES(X)
@@ -396,12 +404,12 @@ void fixed_setup(int n, size_t& smem) {
   }
 }
 
-template <typename S, typename C>
-void fixed_dispatch(const FftAxis& a, Cx<S>* data, int sign, cudaStream_t s) {
+template <typename Si, typename So, typename C>
+void fixed_dispatch(const FftAxis& a, void* data, int sign, cudaStream_t s) {
   switch (a.n) {
-#define X(N)                                   \
-  case N:                                      \
-    fixed_launch<S, C, N>(a, data, sign, s);   \
+#define X(N)                                       \
+  case N:                                          \
+    fixed_launch<Si, So, C, N>(a, data, sign, s);  \
     return;
     MDFT_FIXED_SIZES(X)
 #undef X
@@ -411,12 +419,12 @@ void fixed_dispatch(const FftAxis& a, Cx<S>* data, int sign, cudaStream_t s) {
 
 }  // namespace
 
-template <typename S, typename C>
+template <typename Si, typename So, typename C>
 void fft_axis_finish(FftAxis& a) {
   if (fixed_supported(a.n)) {
     a.fixed = 1;
     a.cols = fixed_cols<C>();
-    fixed_setup<S, C>(a.n, a.smem);
+    fixed_setup<Si, So, C>(a.n, a.smem);
     return;
   }
   a.fixed = 0;
@@ -432,29 +440,26 @@ void fft_axis_finish(FftAxis& a) {
   a.cols = cols;
   a.smem = sizeof(Cx<C>) * ((size_t)2 * a.n * cols + a.n);
   throw_if(a.smem > 200 * 1024, "FFT length too large for the shared-memory tile", 4);
-  allow_max_smem(fft_axis_kernel<S, C>, a.smem, "fft smem attribute");
+  allow_max_smem(fft_axis_kernel<Si, So, C>, a.smem, "fft smem attribute");
 }
 
-template <typename S, typename C>
-void launch_fft_axis(const FftAxis& a, Cx<S>* data, int sign, cudaStream_t s) {
-  if (a.n <= 1 || a.ncols == 0) return;
+template <typename Si, typename So, typename C>
+void launch_fft_axis(const FftAxis& a, void* data, int sign, cudaStream_t s) {
+  if (a.n <= 1 || a.ncols == 0) {
+    // a length-1 axis is the identity, but the storage format may change
+    throw_if(!std::is_same<Si, So>::value, "internal: format change on a length-1 axis", 4);
+    return;
+  }
   clear_stale_error();
   if (a.fixed) {
-    fixed_dispatch<S, C>(a, data, sign, s);
+    fixed_dispatch<Si, So, C>(a, data, sign, s);
     launch_check("fft kernel launch");
     return;
   }
   const long long nb = (a.ncols + a.cols - 1) / a.cols;
   throw_if(nb > 0x7fffffffLL, "FFT batch too large", 4);
-  fft_axis_kernel<S, C><<<(unsigned)nb, kFftThreads, a.smem, s>>>(a, data, sign);
+  fft_axis_kernel<Si, So, C><<<(unsigned)nb, kFftThreads, a.smem, s>>>(a, data, sign);
   launch_check("fft kernel launch");
 }
-
-template void fft_axis_finish<double, double>(FftAxis&);
-template void fft_axis_finish<float, float>(FftAxis&);
-template void fft_axis_finish<double, DF>(FftAxis&);
-template void launch_fft_axis<double, double>(const FftAxis&, Cx<double>*, int, cudaStream_t);
-template void launch_fft_axis<float, float>(const FftAxis&, Cx<float>*, int, cudaStream_t);
-template void launch_fft_axis<double, DF>(const FftAxis&, Cx<double>*, int, cudaStream_t);
 
 }  // namespace mdft

@@ -739,6 +739,25 @@ void oz_plan_finish(OzPlan& P) {
   allow_max_smem(oz_kernel<S>, P.smem, "oz smem attribute");
 }
 
+template <typename S, typename C>
+void oz_lane_attr(const OzPlan& P) {
+  throw_if(!P.lane_path, "internal: lane attributes without the lane path", 4);
+#define MDFT_OZ_ATTR2(K)                                                           \
+  if constexpr (split_pairs<C>())                                                \
+    allow_max_smem(oz_lane_kernel<S, C, K>, P.smem, "oz smem attribute");        \
+  else                                                                           \
+    allow_max_smem(oz_lane1_kernel<S, C, K>, P.smem, "oz smem attribute");
+  switch (P.mmax) {
+    case 1: MDFT_OZ_ATTR2(1) break;
+    case 2: MDFT_OZ_ATTR2(2) break;
+    case 3: MDFT_OZ_ATTR2(3) break;
+    case 4: MDFT_OZ_ATTR2(4) break;
+    case 5: MDFT_OZ_ATTR2(5) break;
+    case 6: MDFT_OZ_ATTR2(6) break;
+  }
+#undef MDFT_OZ_ATTR2
+}
+
 template <typename C>
 void oz_build_rtab(const OzPlan& P, DevBuf& rtab) {
   const long long n = P.npairs_pad * (long long)P.nR;
@@ -786,9 +805,13 @@ void launch_oz(const OzPlan& P, Cx<S>* p, cudaStream_t s) {
     launch_check("oz lane kernel launch");
     return;
   }
-  const long long nb = (P.npairs + P.warps_per_cta - 1) / P.warps_per_cta;
-  oz_kernel<S><<<(unsigned)nb, 32 * P.warps_per_cta, P.smem, s>>>(P, p);
-  launch_check("oz kernel launch");
+  if constexpr (std::is_same<S, DF>::value) {
+    throw Error(4, "internal: packed storage needs the lane path");
+  } else {
+    const long long nb = (P.npairs + P.warps_per_cta - 1) / P.warps_per_cta;
+    oz_kernel<S><<<(unsigned)nb, 32 * P.warps_per_cta, P.smem, s>>>(P, p);
+    launch_check("oz kernel launch");
+  }
 }
 
 }  // namespace mdft
