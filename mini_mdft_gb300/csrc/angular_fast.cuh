@@ -64,13 +64,21 @@ constexpr int pts_per_cta() {
   return pts;
 }
 
+// bytes of the contraction tables at the end of angl2proj's shared memory:
+// coef (NT x NP) and the packed (mup + mmax, mu2) of each projection
+template <typename C, int MMAX, int MRSO>
+constexpr size_t tab_bytes() {
+  using Sh = Shape<MMAX, MRSO>;
+  return (size_t)Sh::NT * Sh::NP * sizeof(C) + (size_t)Sh::NP * sizeof(int);
+}
+
 template <typename C, int MMAX, int MRSO>
 constexpr size_t fast_smem() {
   using Sh = Shape<MMAX, MRSO>;
   constexpr int PTS = pts_per_cta<C, MMAX, MRSO>();
   const size_t a = ((size_t)PTS * Sh::LDO * sizeof(C) + 15) & ~size_t(15);
   const size_t z = (size_t)Sh::NT * (Sh::K + 1) * Sh::NPHI * PTS * sizeof(Cx<C>);
-  return a + z;
+  return a + z + tab_bytes<C, MMAX, MRSO>();
 }
 
 template <typename C>
@@ -90,9 +98,13 @@ angl2proj_fast_kernel(const AngPlan P, const S* __restrict__ o, Cx<S>* __restric
   extern __shared__ __align__(16) unsigned char sm[];
   C* ot = reinterpret_cast<C*>(sm);
   Cx<C>* Zs = reinterpret_cast<Cx<C>*>(sm + (((size_t)PTS * LDO * sizeof(C) + 15) & ~size_t(15)));
+  C* coef_s = reinterpret_cast<C*>(Zs + (size_t)NT * (K + 1) * NPHI * PTS);
+  int* idx_s = reinterpret_cast<int*>(coef_s + NT * NP);
   const int tid = threadIdx.x;
   const long long pt0 = (long long)blockIdx.x * PTS;
   const int cnt = (int)min((long long)PTS, P.N - pt0);
+  for (int i = tid; i < NT * NP; i += blockDim.x) coef_s[i] = static_cast<const C*>(P.coef_a2p)[i];
+  for (int i = tid; i < NP; i += blockDim.x) idx_s[i] = (P.ip_mup[i] + MMAX) | (P.ip_mu2[i] << 16);
 
   // stage the contiguous o tile (and fold in get_delta_rho if asked)
   const S* src = o + pt0 * NO;
@@ -179,17 +191,16 @@ angl2proj_fast_kernel(const AngPlan P, const S* __restrict__ o, Cx<S>* __restric
   __syncthreads();
 
   // theta contraction, one thread per (point, projection)
-  const C* coef = static_cast<const C*>(P.coef_a2p);
   for (int w = tid; w < NP * PTS; w += blockDim.x) {
     const int ip = w / PTS, q = w - ip * PTS;
     if (q >= cnt) continue;
-    const int mupi = P.ip_mup[ip] + MMAX, mu2 = P.ip_mu2[ip];
+    const int mm = idx_s[ip], mupi = mm & 0xffff, mu2 = mm >> 16;
     const Cx<C>* z = Zs + ((size_t)mu2 * NPHI + mupi) * PTS + q;
     Cx<C> sum = mkc<C>(C(0), C(0));
 #pragma unroll
     for (int th = 0; th < NT; ++th) {
       const Cx<C> v = z[(size_t)th * (K + 1) * NPHI * PTS];
-      const C c = coef[th * NP + ip];
+      const C c = coef_s[th * NP + ip];
       sum = mkc<C>(sum.re + v.re * c, sum.im + v.im * c);
     }
     p[(long long)ip * P.N + pt0 + q] = mkc<S>(to_storage<S>(sum.re), to_storage<S>(sum.im));

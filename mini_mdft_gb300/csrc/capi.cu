@@ -8,6 +8,7 @@
 #include <cmath>
 #include <complex>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <string>
 #include <type_traits>
@@ -122,7 +123,7 @@ struct mdft_conv_s {
   std::vector<int> pair_list;                 // reference order (getter)
   std::vector<std::complex<double>> mnq;      // (np_new, nq) (getter)
   DevBuf pairs, kx, ky, kz, rot, pmap, ip_m, ip_mup, ip_mu2, ia_map, ctab, tw_x, tw_y, tw_z;
-  DevBuf pinfo, palpha, ia_start, rtab;  // lane-per-pair OZ path
+  DevBuf pinfo, palpha, ia_start, rtab, ceff;  // lane-per-pair OZ path
   // double-float form: the projections stay packed DF pairs between the
   // passes of execute() (needs the lane OZ path and one axis longer than 1)
   bool df_packed = false;
@@ -287,6 +288,7 @@ void conv_build(mdft_conv_s* h, const mdft::LucTable& t) {
     O.nR = (g.mmax + 1) * (2 * g.mmax + 1) * (2 * g.mmax + 3) / 3;
     std::vector<int4> info((size_t)O.npairs_pad, make_int4(0, 0, 0, 0));
     std::vector<T> alpha((size_t)O.npairs_pad, T(0));
+    std::vector<double> alpha_d((size_t)O.npairs_pad, 0.0);
     for (int i = 0; i < h->npairs; ++i) {
       const int ix = pr[i].x, iy = pr[i].y, iz = pr[i].z;
       const int ixm = ix == 0 ? 0 : g.nx - ix, iym = iy == 0 ? 0 : g.ny - iy, izm = iz == 0 ? 0 : g.nz - iz;
@@ -299,7 +301,41 @@ void conv_build(mdft_conv_s* h, const mdft::LucTable& t) {
       const bool sing = qeq && (ix == g.nx / 2 || iy == g.ny / 2 || iz == g.nz / 2);
       info[i] = make_int4((int)(((long long)ix * g.ny + iy) * g.nz + iz),
                           (int)(((long long)ixm * g.ny + iym) * g.nz + izm), iq, sing ? 1 : 0);
-      alpha[i] = from_ld<T>((long double)(eiq - (double)iq));
+      alpha_d[i] = eiq - (double)iq;
+      alpha[i] = from_ld<T>((long double)alpha_d[i]);
+    }
+    // c(|q|) interpolated once per distinct (iq, alpha) of the pair list
+    // (MDFT_Convolution.hpp:449-463): on a cubic box the pairs share a few
+    // thousand |q| values, so the per-pair interpolation becomes a row read.
+    {
+      std::map<std::pair<int, double>, int> rows;
+      std::vector<std::pair<int, double>> keys;
+      std::vector<int> row_of(h->npairs);
+      for (int i = 0; i < h->npairs; ++i) {
+        const std::pair<int, double> key(info[i].z, alpha_d[i]);
+        auto it = rows.find(key);
+        if (it == rows.end()) {
+          it = rows.emplace(key, (int)keys.size()).first;
+          keys.push_back(key);
+        }
+        row_of[i] = it->second;
+      }
+      const size_t bytes = keys.size() * (size_t)g.np_new * sizeof(Cx<T>);
+      if (bytes <= (size_t)256 << 20) {
+        std::vector<Cx<T>> ce(keys.size() * (size_t)g.np_new);
+        for (size_t r = 0; r < keys.size(); ++r) {
+          const int iq = keys[r].first;
+          const long double a = keys[r].second, b = 1.0L - a;
+          for (int ia = 0; ia < g.np_new; ++ia) {
+            const auto lo = h->mnq[(size_t)ia * need + iq], hi = h->mnq[(size_t)ia * need + iq + 1];
+            ce[r * g.np_new + ia] = mdft::mkc<T>(from_ld<T>(a * hi.real() + b * lo.real()),
+                                                 from_ld<T>(a * hi.imag() + b * lo.imag()));
+          }
+        }
+        h->ceff.upload(ce.data(), sizeof(Cx<T>) * ce.size());
+        for (int i = 0; i < h->npairs; ++i) info[i].z = row_of[i];
+        O.ceff = h->ceff.ptr;
+      }
     }
     h->pinfo.upload(info.data(), sizeof(int4) * info.size());
     h->palpha.upload(alpha.data(), sizeof(T) * alpha.size());

@@ -305,6 +305,9 @@ struct OzPlan {
   const int* ip_mu2;
   const int* ia_map;       // (np, mmax+1, 2mmax/mrso+1)
   const void* ctab;        // (nq, np_new) Cx<T>, transposed mnmunukhi_q
+  // (nu, np_new) Cx<C>: c(|q|) already interpolated for each distinct |q| of
+  // the pair list (lane path; pinfo.z then indexes its rows), or null
+  const void* ceff;
   int warps_per_cta;
   size_t smem;
   // Lane-per-pair path: per-pair geometry computed once at plan creation.

@@ -538,7 +538,8 @@ oz_lane_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
   const bool singular = info.w != 0;
   const C alpha = static_cast<const C*>(P.palpha)[pair];
   const C beta = C(1) - alpha;
-  const Cx<C>* clo = static_cast<const Cx<C>*>(P.ctab) + (size_t)iq * P.np_new;
+  const bool pre = P.ceff != nullptr;
+  const Cx<C>* clo = static_cast<const Cx<C>*>(pre ? P.ceff : P.ctab) + (size_t)iq * P.np_new;
   const Cx<C>* chi = clo + P.np_new;
   const int other = lane ^ 16;
 #pragma unroll
@@ -553,8 +554,13 @@ oz_lane_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
         for (int n = (k < 0 ? -k : k); n <= MMAX; ++n) {
           const int nn = n / mrso;
           for (int nu2 = -nn; nu2 <= nn; ++nu2, ++ia) {
-            const Cx<C> h = chi[ia], lo = clo[ia];
-            const Cx<C> c = mkc<C>(alpha * h.re + beta * lo.re, alpha * h.im + beta * lo.im);
+            Cx<C> c;
+            if (pre) {
+              c = clo[ia];
+            } else {
+              const Cx<C> h = chi[ia], lo = clo[ia];
+              c = mkc<C>(alpha * h.re + beta * lo.re, alpha * h.im + beta * lo.im);
+            }
             if (nu2 < 0)
               sacc = cmac(sacc, c, D[ipx(n, k, -nu2) * 32 + lane]);
             else
@@ -639,7 +645,8 @@ oz_lane1_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
   const bool singular = info.w != 0;
   const C alpha = static_cast<const C*>(P.palpha)[pair];
   const C beta = C(1) - alpha;
-  const Cx<C>* clo = static_cast<const Cx<C>*>(P.ctab) + (size_t)iq * P.np_new;
+  const bool pre = P.ceff != nullptr;
+  const Cx<C>* clo = static_cast<const Cx<C>*>(pre ? P.ceff : P.ctab) + (size_t)iq * P.np_new;
   const Cx<C>* chi = clo + P.np_new;
 #pragma unroll
   for (int m = 0; m <= MMAX; ++m) {
@@ -653,8 +660,13 @@ oz_lane1_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
         for (int n = (k < 0 ? -k : k); n <= MMAX; ++n) {
           const int nn = n / mrso;
           for (int nu2 = -nn; nu2 <= nn; ++nu2, ++ia) {
-            const Cx<C> h = chi[ia], lo = clo[ia];
-            const Cx<C> c = mkc<C>(alpha * h.re + beta * lo.re, alpha * h.im + beta * lo.im);
+            Cx<C> c;
+            if (pre) {
+              c = clo[ia];
+            } else {
+              const Cx<C> h = chi[ia], lo = clo[ia];
+              c = mkc<C>(alpha * h.re + beta * lo.re, alpha * h.im + beta * lo.im);
+            }
             if (nu2 < 0) {
               const int j = ipx(n, k, -nu2) * 32 + lane;
               sq = cmac(sq, c, Dq[j]);
