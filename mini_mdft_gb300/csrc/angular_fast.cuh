@@ -45,10 +45,8 @@ struct Shape {
   }
 };
 
-template <typename C>
-constexpr int a2p_threads() {
-  return 256;
-}
+// threads per CTA of both kernels (the launches and the staging loops)
+constexpr int A2P_THREADS = 256;
 
 // points per CTA: keep the CTA's shared memory near 100 KB
 template <typename C, int MMAX, int MRSO>
@@ -88,7 +86,7 @@ __device__ __forceinline__ Cx<C> ldtw(const void* t, int i) {
 
 // FP32: at most 128 registers so that two 256-thread CTAs share an SM
 template <typename S, typename C, int MMAX, int MRSO, bool FROM_XI>
-__global__ void __launch_bounds__(256, sizeof(C) == 4 ? 2 : 1)
+__global__ void __launch_bounds__(A2P_THREADS, sizeof(C) == 4 ? 2 : 1)
 angl2proj_fast_kernel(const AngPlan P, const S* __restrict__ o, Cx<S>* __restrict__ p, C rho0) {
   using Sh = Shape<MMAX, MRSO>;
   constexpr int PTS = pts_per_cta<C, MMAX, MRSO>();
@@ -106,13 +104,29 @@ angl2proj_fast_kernel(const AngPlan P, const S* __restrict__ o, Cx<S>* __restric
   for (int i = tid; i < NT * NP; i += blockDim.x) coef_s[i] = static_cast<const C*>(P.coef_a2p)[i];
   for (int i = tid; i < NP; i += blockDim.x) idx_s[i] = (P.ip_mup[i] + MMAX) | (P.ip_mu2[i] << 16);
 
-  // stage the contiguous o tile (and fold in get_delta_rho if asked)
-  const S* src = o + pt0 * NO;
-  for (int i = tid; i < cnt * NO; i += blockDim.x) {
-    const int q = i / NO, j = i - q * NO;
-    C v = to_compute<C>(src[i]);
-    if (FROM_XI) v = rho0 * (v * v - C(1));
-    ot[q * LDO + j] = v;
+  // stage the contiguous o tile (and fold in get_delta_rho if asked); all of
+  // a thread's loads are issued before the first shared store, so the tile
+  // costs one memory round trip instead of one per element
+  {
+    constexpr int IT = (PTS * NO + A2P_THREADS - 1) / A2P_THREADS;
+    const S* src = o + pt0 * NO;
+    const int n = cnt * NO;
+    S v[IT];
+#pragma unroll
+    for (int r = 0; r < IT; ++r) {
+      const int i = tid + r * A2P_THREADS;
+      if (i < n) v[r] = src[i];
+    }
+#pragma unroll
+    for (int r = 0; r < IT; ++r) {
+      const int i = tid + r * A2P_THREADS;
+      if (i < n) {
+        const int q = i / NO, j = i - q * NO;
+        C x = to_compute<C>(v[r]);
+        if (FROM_XI) x = rho0 * (x * x - C(1));
+        ot[q * LDO + j] = x;
+      }
+    }
   }
   __syncthreads();
 
@@ -208,7 +222,7 @@ angl2proj_fast_kernel(const AngPlan P, const S* __restrict__ o, Cx<S>* __restric
 }
 
 template <typename S, typename C, int MMAX, int MRSO>
-__global__ void __launch_bounds__(256, sizeof(C) == 4 ? 2 : 1)
+__global__ void __launch_bounds__(A2P_THREADS, sizeof(C) == 4 ? 2 : 1)
 proj2angl_fast_kernel(const AngPlan P, const Cx<S>* __restrict__ p, S* __restrict__ o) {
   using Sh = Shape<MMAX, MRSO>;
   constexpr int PTS = pts_per_cta<C, MMAX, MRSO>();
@@ -222,12 +236,22 @@ proj2angl_fast_kernel(const AngPlan P, const Cx<S>* __restrict__ p, S* __restric
   const long long pt0 = (long long)blockIdx.x * PTS;
   const int cnt = (int)min((long long)PTS, P.N - pt0);
 
-  // stage p(ip, pt0 .. pt0 + cnt) as Ps[ip][point]
-  for (int w = tid; w < NP * PTS; w += blockDim.x) {
-    const int ip = w / PTS, q = w - ip * PTS;
-    if (q >= cnt) continue;
-    const Cx<S> v = p[(long long)ip * P.N + pt0 + q];
-    Ps[w] = mkc<C>(to_compute<C>(v.re), to_compute<C>(v.im));
+  // stage p(ip, pt0 .. pt0 + cnt) as Ps[ip][point], loads batched as above
+  {
+    constexpr int IT = (NP * PTS + A2P_THREADS - 1) / A2P_THREADS;
+    Cx<S> v[IT];
+#pragma unroll
+    for (int r = 0; r < IT; ++r) {
+      const int w = tid + r * A2P_THREADS;
+      const int ip = w / PTS, q = w - ip * PTS;
+      if (w < NP * PTS && q < cnt) v[r] = p[(long long)ip * P.N + pt0 + q];
+    }
+#pragma unroll
+    for (int r = 0; r < IT; ++r) {
+      const int w = tid + r * A2P_THREADS;
+      const int q = w - (w / PTS) * PTS;
+      if (w < NP * PTS && q < cnt) Ps[w] = mkc<C>(to_compute<C>(v[r].re), to_compute<C>(v[r].im));
+    }
   }
   __syncthreads();
 
@@ -343,9 +367,9 @@ void fast_a2p(const AngPlan& P, const S* o, Cx<S>* p, bool from_xi, double rho0,
   const long long nb = (P.N + PTS - 1) / PTS;
   throw_if(nb > 0x7fffffffLL, "grid too large", 4);
   if (from_xi)
-    angl2proj_fast_kernel<S, C, MMAX, MRSO, true><<<(unsigned)nb, 256, sm, s>>>(P, o, p, C(rho0));
+    angl2proj_fast_kernel<S, C, MMAX, MRSO, true><<<(unsigned)nb, A2P_THREADS, sm, s>>>(P, o, p, C(rho0));
   else
-    angl2proj_fast_kernel<S, C, MMAX, MRSO, false><<<(unsigned)nb, 256, sm, s>>>(P, o, p, C(rho0));
+    angl2proj_fast_kernel<S, C, MMAX, MRSO, false><<<(unsigned)nb, A2P_THREADS, sm, s>>>(P, o, p, C(rho0));
 }
 
 template <typename S, typename C, int MMAX, int MRSO>
@@ -356,7 +380,7 @@ void fast_p2a(const AngPlan& P, const Cx<S>* p, S* o, cudaStream_t s) {
                          (size_t)Sh::NP * PTS * sizeof(Cx<C>);
   const long long nb = (P.N + PTS - 1) / PTS;
   throw_if(nb > 0x7fffffffLL, "grid too large", 4);
-  proj2angl_fast_kernel<S, C, MMAX, MRSO><<<(unsigned)nb, 256, sm2, s>>>(P, p, o);
+  proj2angl_fast_kernel<S, C, MMAX, MRSO><<<(unsigned)nb, A2P_THREADS, sm2, s>>>(P, p, o);
 }
 
 }  // namespace

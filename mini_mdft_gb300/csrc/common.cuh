@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
 #include <string>
 
 #include "host_setup.hpp"
@@ -101,45 +102,160 @@ __host__ __device__ __forceinline__ bool df_abs_lt(DF x, float e) {
   return h < e || (h == e && (x.hi > 0.f ? x.lo < 0.f : x.lo > 0.f));
 }
 
-// double <-> double-float conversions built from the IEEE bit fields, so
-// that they run on the integer and FP32 pipes: the hardware double<->float
-// conversions and the FP64 add they need share this GPU's narrow FP64 pipe.
+// double <-> double-float conversions built from the IEEE bit fields with
+// integer and FP32 instructions only: the hardware double<->float conversions
+// and the FP64 add they would need share this GPU's narrow FP64 pipe, and
+// even an untaken fallback branch costs FP64 issue slots once the compiler
+// predicates it.  Host and device run the same code.
+__host__ __device__ __forceinline__ unsigned long long bits_of(double x) {
 #ifdef __CUDA_ARCH__
-__device__ __forceinline__ DF df_from_double_dev(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (unsigned long long)__double_as_longlong(x);
+#else
+  unsigned long long b;
+  memcpy(&b, &x, sizeof b);
+  return b;
+#endif
+}
+__host__ __device__ __forceinline__ double double_of(unsigned long long b) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)b);
+#else
+  double x;
+  memcpy(&x, &b, sizeof x);
+  return x;
+#endif
+}
+__host__ __device__ __forceinline__ unsigned bits_of(float x) {
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(x);
+#else
+  unsigned b;
+  memcpy(&b, &x, sizeof b);
+  return b;
+#endif
+}
+__host__ __device__ __forceinline__ float float_of(unsigned b) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(b);
+#else
+  float x;
+  memcpy(&x, &b, sizeof x);
+  return x;
+#endif
+}
+// leading zeros of a non-zero word
+__host__ __device__ __forceinline__ int clz32(unsigned x) {
+#ifdef __CUDA_ARCH__
+  return __clz(x);
+#else
+  return __builtin_clz(x);
+#endif
+}
+__host__ __device__ __forceinline__ int clz64(unsigned long long x) {
+#ifdef __CUDA_ARCH__
+  return __clzll((long long)x);
+#else
+  return __builtin_clzll(x);
+#endif
+}
+
+// x -> (hi, lo): hi is x truncated to 24 significant bits, lo the next 24
+// bits (truncated); |x - (hi + lo)| < 2^-47 |x| for 2^-73 <= |x| < 2^128.
+// Smaller |x| keep hi only (x truncated to float, subnormal or zero), larger
+// ones become +-inf; NaN stays NaN.
+__host__ __device__ __forceinline__ DF df_from_double_bits(double x) {
+  const unsigned long long b = bits_of(x);
   const unsigned hi32 = (unsigned)(b >> 32), lo32 = (unsigned)b;
   const unsigned e = (hi32 >> 20) & 0x7ffu;  // biased exponent
   const unsigned sign = hi32 & 0x80000000u;
-  if ((b << 1) == 0) return DF(__uint_as_float(sign), 0.f);  // +-0
-  // 2^-73 <= |x| < 2^128: hi (x truncated to 24 bits) and lo (the rest,
-  // truncated to 24 bits) are normal floats
+  const unsigned m23 = ((hi32 & 0x000fffffu) << 3) | (lo32 >> 29);  // top 23 fraction bits
   if (e >= 950u && e <= 1150u) {
-    const unsigned m23 = ((hi32 & 0x000fffffu) << 3) | (lo32 >> 29);
-    const float h = __uint_as_float(sign | ((e - 896u) << 23) | m23);
-    const unsigned r = lo32 & 0x1fffffffu;  // remaining 29 mantissa bits
+    const float h = float_of(sign | ((e - 896u) << 23) | m23);
+    const unsigned r = lo32 & 0x1fffffffu;  // remaining 29 fraction bits
     float l = 0.f;
     if (r) {
-      const int top = 31 - __clz(r);  // leading bit, 0..28
+      const int top = 31 - clz32(r);  // leading bit, 0..28
       const unsigned mr = top >= 23 ? (r >> (top - 23)) : (r << (23 - top));
       const unsigned lexp = e - 948u + (unsigned)top;  // biased exponent of lo, 2..230
-      l = __uint_as_float(sign | (lexp << 23) | (mr & 0x7fffffu));
+      l = float_of(sign | (lexp << 23) | (mr & 0x7fffffu));
     }
     return df_fast_two_sum(h, l);
   }
-  return DF(x);  // tiny, huge, inf, nan: hardware conversions
+  if (e > 1150u) {  // |x| >= 2^128, inf, NaN
+    const bool nan = e == 0x7ffu && (b & 0x000fffffffffffffull) != 0;
+    return DF(float_of(sign | (nan ? 0x7fc00000u : 0x7f800000u)), 0.f);
+  }
+  if (e >= 897u) return DF(float_of(sign | ((e - 896u) << 23) | m23), 0.f);  // normal float
+  if (e < 874u) return DF(float_of(sign), 0.f);  // below the smallest subnormal float
+  // subnormal float: m 2^-149 with m = significand >> (926 - e), 1 <= m < 2^23
+  const unsigned long long full = (b & 0x000fffffffffffffull) | (1ull << 52);
+  return DF(float_of(sign | (unsigned)(full >> (926u - e))), 0.f);
 }
-__device__ __forceinline__ double f2d_bits(float f) {
-  const unsigned u = __float_as_uint(f);
+
+// float -> double, exact for every float (zero, subnormal, inf, NaN too)
+__host__ __device__ __forceinline__ double f2d_bits(float f) {
+  const unsigned u = bits_of(f);
   const unsigned ex = (u >> 23) & 0xffu;
-  if ((u << 1) == 0) return __longlong_as_double((long long)((unsigned long long)u << 32));  // +-0
-  if (ex == 0u || ex == 0xffu) return (double)f;  // denormal, inf, nan
-  const unsigned long long bits = ((unsigned long long)(u & 0x80000000u) << 32) |
-                                  ((unsigned long long)(ex + 896u) << 52) |
-                                  ((unsigned long long)(u & 0x7fffffu) << 29);
-  return __longlong_as_double((long long)bits);
+  const unsigned long long s = (unsigned long long)(u & 0x80000000u) << 32;
+  const unsigned long long fr = u & 0x7fffffu;
+  if (ex == 0xffu) return double_of(s | 0x7ff0000000000000ull | (fr << 29));
+  if (ex == 0u) {
+    if (fr == 0) return double_of(s);
+    const int top = 31 - clz32((unsigned)fr);  // value = 1.x 2^(top - 149)
+    return double_of(s | ((unsigned long long)(top + 874) << 52) |
+                     ((fr << (52 - top)) & 0x000fffffffffffffull));
+  }
+  return double_of(s | ((unsigned long long)(ex + 896u) << 52) | (fr << 29));
 }
-__device__ __forceinline__ double df_to_double_dev(DF a) { return f2d_bits(a.hi) + f2d_bits(a.lo); }
-#endif
+
+// (hi, lo) -> double: the two significands aligned in a 64-bit integer,
+// added, and rounded to 53 bits (to nearest, ties away from zero); equal to
+// the rounded sum hi + lo except on exact ties.
+__host__ __device__ __forceinline__ double df_to_double_bits(DF a) {
+  const unsigned uh = bits_of(a.hi), ul = bits_of(a.lo);
+  const unsigned eh = (uh >> 23) & 0xffu, el = (ul >> 23) & 0xffu;
+  if (eh == 0xffu || (ul << 1) == 0) return f2d_bits(a.hi);  // inf/NaN, or lo = 0
+  if (el == 0xffu || (uh << 1) == 0) return f2d_bits(a.lo);
+  // signed significands (subnormals: exponent 1, no implicit bit)
+  const long long mh = (long long)((uh & 0x7fffffu) | (eh ? 0x800000u : 0u));
+  const long long ml = (long long)((ul & 0x7fffffu) | (el ? 0x800000u : 0u));
+  const int xh = eh ? (int)eh : 1, xl = el ? (int)el : 1;
+  long long big = (uh >> 31) ? -mh : mh, small = (ul >> 31) ? -ml : ml;
+  int xb = xh, d = xh - xl;
+  if (d < 0) {
+    const long long t = big;
+    big = small;
+    small = t;
+    xb = xl;
+    d = -d;
+  }
+  // |each term| < 2^61; the shifted-out bits of the smaller term leave a
+  // sticky half unit, so S = 2 (big + small >> d) + sticky fits in 63 bits
+  // and rounds as the exact sum does
+  long long S = big * (1ll << 37);
+  bool sticky = false;
+  if (d < 62) {
+    const long long t = small * (1ll << 37);
+    S += t >> d;
+    sticky = (t & ((1ll << d) - 1)) != 0;
+  } else {
+    sticky = small != 0;
+  }
+  S = 2 * S + (sticky ? 1 : 0);
+  if (S == 0) return 0.0;
+  const unsigned long long sign = S < 0 ? 0x8000000000000000ull : 0ull;
+  unsigned long long U = S < 0 ? (unsigned long long)(-S) : (unsigned long long)S;
+  int top = 63 - clz64(U);  // value = U 2^(xb - 188)
+  if (top > 52) {
+    U += 1ull << (top - 53);  // round half away from zero
+    if (U >> (top + 1)) ++top;
+    U >>= top - 52;
+  } else {
+    U <<= 52 - top;
+  }
+  const unsigned long long be = (unsigned long long)(top + xb + 835);  // 836..1151
+  return double_of(sign | (be << 52) | (U & 0x000fffffffffffffull));
+}
 
 // Storage <-> compute conversions (identity unless the compute type is DF).
 template <typename C, typename S>
@@ -149,7 +265,7 @@ __host__ __device__ __forceinline__ C to_compute(S x) {
 template <>
 __host__ __device__ __forceinline__ DF to_compute<DF, double>(double x) {
 #ifdef __CUDA_ARCH__
-  return df_from_double_dev(x);
+  return df_from_double_bits(x);
 #else
   return DF(x);
 #endif
@@ -161,7 +277,7 @@ __host__ __device__ __forceinline__ S to_storage(C x) {
 template <>
 __host__ __device__ __forceinline__ double to_storage<double, DF>(DF x) {
 #ifdef __CUDA_ARCH__
-  return df_to_double_dev(x);
+  return df_to_double_bits(x);
 #else
   return (double)x;
 #endif
