@@ -24,12 +24,21 @@
 
 namespace mdft {
 
+// The split lane kernel specialised for mrso = 2 on packed storage (S = C):
+// defined in oz_r2.cuh and instantiated in its own translation units.
+template <typename C, int MMAX>
+void oz_lane_r2_attr(size_t smem);
+template <typename C, int MMAX>
+void oz_lane_r2_launch(const OzPlan& P, Cx<C>* p, dim3 grid, dim3 block, cudaStream_t s);
+
 namespace {
 
 constexpr int kRotL5 = 5, kRotM13 = 13;  // RotationCoeffs extents (l-2, m+6)
 
 __host__ __device__ constexpr int roff(int l) { return l * (2 * l - 1) * (2 * l + 1) / 3; }
 __host__ __device__ constexpr int nrot(int mmax) { return roff(mmax + 1); }
+// offset of block l in the half table (entries with m1 >= 0): sum (2l'+1)(l'+1)
+__host__ __device__ constexpr int hoff(int l) { return l == 0 ? 0 : hoff(l - 1) + (2 * l - 1) * l; }
 
 template <typename T>
 struct OzSmem {
@@ -459,11 +468,23 @@ __global__ void rot_table_kernel(const OzPlan P, Cx<double>* __restrict__ rt64) 
   rot_recursion(q0, q1, q2, P.mmax, A, B, Cc, D, R);
 }
 
+// Half table of the split lane kernel from the FP64 table: per block of 32
+// pairs the entries Rh(l, m, j) = R(l, m, j), j = 0..l, at hoff(l) +
+// (m + l)(l + 1) + j, converted to C.
 template <typename C>
-__global__ void rot_table_convert(const Cx<double>* __restrict__ a, Cx<C>* __restrict__ b, long long n) {
+__global__ void rot_table_half(const Cx<double>* __restrict__ full, Cx<C>* __restrict__ half,
+                               long long nblk, int mmax, int nfull, int nhalf) {
+  const long long n = nblk * nhalf * 32;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x)
-    b[i] = mkc<C>(to_compute<C>(a[i].re), to_compute<C>(a[i].im));
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long t = i >> 5, blk = t / nhalf;
+    const int lane = (int)(i & 31), e = (int)(t - blk * nhalf);
+    int l = 0;
+    while (l < mmax && hoff(l + 1) <= e) ++l;
+    const int r = e - hoff(l), m = r / (l + 1) - l, j = r % (l + 1);
+    const long long src = (blk * nfull + roff(l) + (m + l) * (2 * l + 1) + (j + l)) * 32 + lane;
+    half[i] = mkc<C>(to_compute<C>(full[src].re), to_compute<C>(full[src].im));
+  }
 }
 
 // Projection index of (m, mup, mu2) in OrientationProjectionMap order
@@ -476,8 +497,44 @@ struct PIndex {
   }
 };
 
-template <typename S, typename C, int MMAX>
-__global__ void __launch_bounds__(256, 2)
+// coefficient slots of the OZ sum of one projection, terms n' < n, when
+// mrso is a compile-time constant: sum_{n' < n} (2 (n' / mrso) + 1)
+__host__ __device__ constexpr int oz_coff(int n, int mrso) {
+  return n <= 0 ? 0 : oz_coff(n - 1, mrso) + 2 * ((n - 1) / mrso) + 1;
+}
+// projections of an angular grid: sum_m (2m+1)(m/mrso+1)
+__host__ __device__ constexpr int oz_np(int mmax, int mrso) {
+  return mmax < 0 ? 0 : oz_np(mmax - 1, mrso) + (2 * mmax + 1) * (mmax / mrso + 1);
+}
+// warps per CTA of the lane kernels: one warp's shared columns take
+// per_warp bytes; the split kernel keeps a CTA near 100 KB so that two share
+// an SM, the unsplit one near 200 KB
+__host__ __device__ constexpr int lane_warps(size_t per_warp, bool split) {
+  return (int)((split ? 100 : 200) * 1024 / per_warp) < 1   ? 1
+         : (int)((split ? 100 : 200) * 1024 / per_warp) > 8 ? 8
+                                                              : (int)((split ? 100 : 200) * 1024 / per_warp);
+}
+// threads per CTA the split kernel is compiled for: exact when mrso is a
+// compile-time constant, 256 (the most) otherwise
+template <typename C, int MMAX, int MRSO>
+constexpr int oz_split_threads() {
+  return MRSO > 0 ? 32 * lane_warps((size_t)oz_np(MMAX, MRSO) * 32 * sizeof(Cx<C>), true) : 256;
+}
+// registers per thread that keep two such CTAs on one SM (at most 255):
+// the warps spread over the SM's four schedulers, each with a quarter of the
+// register file (16384), so the busiest scheduler holds ceil(2 W / 4) warps
+template <typename C, int MMAX, int MRSO>
+constexpr int oz_split_regs() {
+  return 16384 / (32 * ((2 * (oz_split_threads<C, MMAX, MRSO>() / 32) + 3) / 4)) / 8 * 8 > 255
+             ? 255
+             : 16384 / (32 * ((2 * (oz_split_threads<C, MMAX, MRSO>() / 32) + 3) / 4)) / 8 * 8;
+}
+
+// MRSO > 0: the molecule's rotational symmetry order fixed at compile time
+// (every loop over nu unrolled, so the c(|q|) loads of a projection can be
+// issued together); MRSO = 0: read from the plan.
+template <typename S, typename C, int MMAX, int MRSO>
+__global__ void __maxnreg__((oz_split_regs<C, MMAX, MRSO>()))
 oz_lane_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
   extern __shared__ __align__(16) unsigned char sm[];
   // Two lanes per pair: lane i (< 16) carries the q side of pair i of the
@@ -490,7 +547,8 @@ oz_lane_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
   if (grp * 16 >= P.npairs) return;  // whole warp exits together
   const long long pair = grp * 16 + (lane & 15);
   const bool valid = pair < P.npairs;
-  const int np = P.np, mrso = P.mrso;
+  const int np = P.np;
+  const int mrso = MRSO > 0 ? MRSO : P.mrso;
   Cx<C>* D = reinterpret_cast<Cx<C>*>(sm + (size_t)wib * np * 32 * sizeof(Cx<C>));
   PIndex ipx;
   ipx.mrso = mrso;
@@ -507,13 +565,20 @@ oz_lane_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
   const long long lown = side ? info.y : info.x;
   // the q side does not store at self-paired k-points: the -q store wins
   const bool store = valid && (side == 1 || info.x != info.y);
-  const int ks = side ? -1 : 1;  // R(m, mup, +-khi)
+  // Half table Rh(l, m, j) = R(l, m, j) for j >= 0; for m1 < 0,
+  // R(l, m, m1) = (-1)^(m+m1) conj Rh(l, -m, -m1).  Both lanes of a pair
+  // read the same entries, so every load serves the two half-warps.
   const Cx<C>* Rt = static_cast<const Cx<C>*>(P.rtab) + (pair >> 5) * (long long)P.nR * 32 + (pair & 31);
-#define RT(l, m, m1) Rt[(roff(l) + ((m) + (l)) * (2 * (l) + 1) + ((m1) + (l))) * 32]
+#define RH(l, m, j) Rt[(hoff(l) + ((m) + (l)) * ((l) + 1) + (j)) * 32]
 
-  // rotation to the q frame (MDFT_Convolution.hpp:427-443), block by block
+  // rotation to the q frame (MDFT_Convolution.hpp:427-443), block by block:
+  // D(m, k) = sum_a g_a R(m, a - m, ks k) with ks = +1 on the q side and -1
+  // on the -q side.  For j = |k| > 0 one side needs column +j (direct) and
+  // the other column -j (mirrored), both from the row Rh(m, ., j).
 #pragma unroll
   for (int m = 0; m <= MMAX; ++m) {
+    const bool flip = side && (m & 1);  // (-1)^m of R(-q) = (-1)^l R(q)
+#pragma unroll 1
     for (int mu2 = 0; mu2 <= m / mrso; ++mu2) {
       Cx<C> g[2 * MMAX + 1];
 #pragma unroll
@@ -521,13 +586,38 @@ oz_lane_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
         const Cx<S> u = p[(long long)ipx(m, a - m, mu2) * N + lown];
         g[a] = mkc<C>(to_compute<C>(u.re), to_compute<C>(u.im));
       }
-#pragma unroll 1
-      for (int k = -m; k <= m; ++k) {
-        Cx<C> x = mkc<C>(C(0), C(0));
+      {  // k = 0: column 0 on both sides
+        CAcc<C> x;
+        cacc_zero(x);
 #pragma unroll
-        for (int a = 0; a <= 2 * m; ++a) x = cmac(x, g[a], RT(m, a - m, ks * k));
-        if (side && (m & 1)) x = mkc<C>(-x.re, -x.im);
-        D[ipx(m, k, mu2) * 32 + lane] = x;
+        for (int b = 0; b <= 2 * m; ++b) cacc_mac(x, g[b], RH(m, b - m, 0));
+        Cx<C> v = cacc_get(x);
+        if (flip) v = mkc<C>(-v.re, -v.im);
+        D[ipx(m, 0, mu2) * 32 + lane] = v;
+      }
+#pragma unroll 1
+      for (int j = 1; j <= m; ++j) {
+        // direct: sum_b g_b h_b; mirrored: sum_b (-1)^(m+b+j) g_{2m-b} conj(h_b)
+        CAcc<C> xd, xm;
+        cacc_zero(xd);
+        cacc_zero(xm);
+#pragma unroll
+        for (int b = 0; b <= 2 * m; ++b) {
+          const Cx<C> h = RH(m, b - m, j);
+          cacc_mac(xd, g[b], h);
+          const Cx<C> gm = g[2 * m - b];
+          cacc_macc(xm, ((m + b) & 1) ? mkc<C>(-gm.re, -gm.im) : gm, h);
+        }
+        Cx<C> vd = cacc_get(xd), vm = cacc_get(xm);
+        if (j & 1) vm = mkc<C>(-vm.re, -vm.im);
+        // q side: k = +j direct, k = -j mirrored; -q side the other way round
+        Cx<C> kp = side ? vm : vd, kn = side ? vd : vm;
+        if (flip) {
+          kp = mkc<C>(-kp.re, -kp.im);
+          kn = mkc<C>(-kn.re, -kn.im);
+        }
+        D[ipx(m, j, mu2) * 32 + lane] = kp;
+        D[ipx(m, -j, mu2) * 32 + lane] = kn;
       }
     }
   }
@@ -542,45 +632,89 @@ oz_lane_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
   const Cx<C>* clo = static_cast<const Cx<C>*>(pre ? P.ceff : P.ctab) + (size_t)iq * P.np_new;
   const Cx<C>* chi = clo + P.np_new;
   const int other = lane ^ 16;
+  // c(|q|) of coefficient ia, and term (n, nu2) of the OZ sum of projection
+  // (m, k, mu2): c times the own column at -nu2 (nu2 < 0) or the partner's,
+  // conjugated, at nu2
+#define OZ_COEF(ia)                                                                        \
+  (pre ? clo[ia]                                                                           \
+       : mkc<C>(alpha * chi[ia].re + beta * clo[ia].re, alpha * chi[ia].im + beta * clo[ia].im))
+#define OZ_TERM(s, c, n, k, nu2)                         \
+  do {                                                   \
+    if ((nu2) < 0)                                       \
+      cacc_mac(s, c, D[ipx(n, k, -(nu2)) * 32 + lane]);  \
+    else                                                 \
+      cacc_macc(s, c, D[ipx(n, k, (nu2)) * 32 + other]); \
+  } while (0)
 #pragma unroll
   for (int m = 0; m <= MMAX; ++m) {
+    const bool flip = side && (m & 1);
+#pragma unroll 1
     for (int mu2 = 0; mu2 <= m / mrso; ++mu2) {
-      Cx<C> g[2 * MMAX + 1];
+      // rotation back as the OZ outputs appear: out_a += g_k conj R(m, a, ks k)
+      CAcc<C> acc[2 * MMAX + 1];
 #pragma unroll
+      for (int a = 0; a <= 2 * m; ++a) cacc_zero(acc[a]);
+#pragma unroll 1
       for (int k = -m; k <= m; ++k) {
-        int ia = P.ia_start[ipx(m, k, mu2)];
-        Cx<C> sacc = mkc<C>(C(0), C(0));
+        const int ak = k < 0 ? -k : k;
+        CAcc<C> sacc;
+        cacc_zero(sacc);
+        const int ia_k = P.ia_start[ipx(m, k, mu2)];
+        if constexpr (MRSO > 0) {
+          // slot t of term (n, u) at ia0 + t; every loop below unrolls
+          const int ia0 = ia_k - oz_coff(ak, MRSO);
 #pragma unroll
-        for (int n = (k < 0 ? -k : k); n <= MMAX; ++n) {
-          const int nn = n / mrso;
-          for (int nu2 = -nn; nu2 <= nn; ++nu2, ++ia) {
-            Cx<C> c;
-            if (pre) {
-              c = clo[ia];
-            } else {
-              const Cx<C> h = chi[ia], lo = clo[ia];
-              c = mkc<C>(alpha * h.re + beta * lo.re, alpha * h.im + beta * lo.im);
+          for (int n = 0; n <= MMAX; ++n) {
+            if (n < ak) continue;
+            const int nn = n / MRSO;
+#pragma unroll
+            for (int u = 0; u <= 2 * nn; ++u) {
+              const Cx<C> c = OZ_COEF(ia0 + oz_coff(n, MRSO) + u);
+              OZ_TERM(sacc, c, n, k, u - nn);
             }
-            if (nu2 < 0)
-              sacc = cmac(sacc, c, D[ipx(n, k, -nu2) * 32 + lane]);
-            else
-              sacc = cmac(sacc, c, conj(D[ipx(n, k, nu2) * 32 + other]));
+          }
+        } else {
+          int ia = ia_k;
+#pragma unroll
+          for (int n = 0; n <= MMAX; ++n) {
+            if (n < ak) continue;
+            const int nn = n / mrso;
+            for (int nu2 = -nn; nu2 <= nn; ++nu2, ++ia) {
+              const Cx<C> c = OZ_COEF(ia);
+              OZ_TERM(sacc, c, n, k, nu2);
+            }
           }
         }
-        g[k + m] = chop(sacc);
-      }
-#pragma unroll 1
-      for (int a = -m; a <= m; ++a) {
-        Cx<C> x = mkc<C>(C(0), C(0));
+        const Cx<C> gk = chop(cacc_get(sacc));
+        // conj R(m, a, kk), kk = ks k: conj Rh(m, a, |k|) when kk >= 0, else
+        // (-1)^(a+k) Rh(m, -a, |k|); the row Rh(m, ., |k|) serves both sides
+        const bool direct = side ? (k <= 0) : (k >= 0);
+        const bool kodd = (k & 1) != 0;
+        Cx<C> h[2 * MMAX + 1];
 #pragma unroll
-        for (int k = -m; k <= m; ++k) x = cmac(x, g[k + m], conj(RT(m, a, ks * k)));
-        if (side && (m & 1)) x = mkc<C>(-x.re, -x.im);
-        if (side && singular) x = conj(x);
-        if (store) p[(long long)ipx(m, a, mu2) * N + lown] = mkc<S>(to_storage<S>(x.re), to_storage<S>(x.im));
+        for (int b = 0; b <= 2 * m; ++b) h[b] = RH(m, b - m, ak);
+#pragma unroll
+        for (int a = 0; a <= 2 * m; ++a) {
+          const Cx<C> hd = h[a], hm = h[2 * m - a];
+          const bool neg = (((a - m) & 1) != 0) != kodd;
+          Cx<C> r;
+          r.re = direct ? hd.re : (neg ? -hm.re : hm.re);
+          r.im = direct ? -hd.im : (neg ? -hm.im : hm.im);
+          cacc_mac(acc[a], gk, r);
+        }
+      }
+#pragma unroll
+      for (int a = 0; a <= 2 * m; ++a) {
+        Cx<C> v = cacc_get(acc[a]);
+        if (flip) v = mkc<C>(-v.re, -v.im);
+        if (side && singular) v = conj(v);
+        if (store) p[(long long)ipx(m, a - m, mu2) * N + lown] = mkc<S>(to_storage<S>(v.re), to_storage<S>(v.im));
       }
     }
   }
-#undef RT
+#undef OZ_COEF
+#undef OZ_TERM
+#undef RH
 }
 
 // One lane per pair (both sides in one thread): used for FP64 arithmetic,
@@ -715,6 +849,51 @@ size_t lane_smem_per_warp(int np) {
   return (size_t)np * 32 * sizeof(Cx<C>) * (split_pairs<C>() ? 1 : 2);
 }
 
+// Shared-memory attribute and launch of the lane kernel for one mmax: the
+// split kernel specialised for mrso = 2 (packed storage) comes from its own
+// translation unit, every other case from the generic instantiations here.
+template <typename S, typename C, int K>
+void lane_attr_one(const OzPlan& P) {
+  if constexpr (split_pairs<C>()) {
+    if constexpr (std::is_same<S, C>::value) {
+      if (P.mrso == 2) {
+        oz_lane_r2_attr<C, K>(P.smem);
+        return;
+      }
+    }
+    allow_max_smem(oz_lane_kernel<S, C, K, 0>, P.smem, "oz smem attribute");
+  } else {
+    allow_max_smem(oz_lane1_kernel<S, C, K>, P.smem, "oz smem attribute");
+  }
+}
+
+template <typename S, typename C>
+void lane_attr_all(const OzPlan& P) {
+  switch (P.mmax) {
+    case 1: lane_attr_one<S, C, 1>(P); break;
+    case 2: lane_attr_one<S, C, 2>(P); break;
+    case 3: lane_attr_one<S, C, 3>(P); break;
+    case 4: lane_attr_one<S, C, 4>(P); break;
+    case 5: lane_attr_one<S, C, 5>(P); break;
+    case 6: lane_attr_one<S, C, 6>(P); break;
+  }
+}
+
+template <typename S, typename C, int K>
+void lane_launch_one(const OzPlan& P, Cx<S>* p, dim3 grid, dim3 block, cudaStream_t s) {
+  if constexpr (split_pairs<C>()) {
+    if constexpr (std::is_same<S, C>::value) {
+      if (P.mrso == 2) {
+        oz_lane_r2_launch<C, K>(P, p, grid, block, s);
+        return;
+      }
+    }
+    oz_lane_kernel<S, C, K, 0><<<grid, block, P.smem, s>>>(P, p);
+  } else {
+    oz_lane1_kernel<S, C, K><<<grid, block, P.smem, s>>>(P, p);
+  }
+}
+
 }  // namespace
 
 template <typename S, typename C>
@@ -724,24 +903,9 @@ void oz_plan_finish(OzPlan& P) {
   const size_t per_warp = lane_smem_per_warp<C>(P.np);
   P.lane_path = (P.mmax <= kLaneMaxMmax && per_warp <= 64 * 1024 && P.N < (1LL << 31)) ? 1 : 0;
   if (P.lane_path) {
-    // split: at most ~100 KB per CTA so that two CTAs share an SM
-    int w = (int)(((split_pairs<C>() ? 100 : 200) * 1024) / per_warp);
-    P.warps_per_cta = w < 1 ? 1 : (w > 8 ? 8 : w);
+    P.warps_per_cta = lane_warps(per_warp, split_pairs<C>());
     P.smem = per_warp * P.warps_per_cta;
-#define MDFT_OZ_ATTR(K)                                                              \
-  if constexpr (split_pairs<C>())                                                  \
-    allow_max_smem(oz_lane_kernel<S, C, K>, P.smem, "oz smem attribute");          \
-  else                                                                             \
-    allow_max_smem(oz_lane1_kernel<S, C, K>, P.smem, "oz smem attribute");
-    switch (P.mmax) {
-      case 1: MDFT_OZ_ATTR(1) break;
-      case 2: MDFT_OZ_ATTR(2) break;
-      case 3: MDFT_OZ_ATTR(3) break;
-      case 4: MDFT_OZ_ATTR(4) break;
-      case 5: MDFT_OZ_ATTR(5) break;
-      case 6: MDFT_OZ_ATTR(6) break;
-    }
-#undef MDFT_OZ_ATTR
+    lane_attr_all<S, C>(P);
     return;
   }
   const OzSmem<S> L(P.mmax, P.np);
@@ -754,36 +918,29 @@ void oz_plan_finish(OzPlan& P) {
 template <typename S, typename C>
 void oz_lane_attr(const OzPlan& P) {
   throw_if(!P.lane_path, "internal: lane attributes without the lane path", 4);
-#define MDFT_OZ_ATTR2(K)                                                           \
-  if constexpr (split_pairs<C>())                                                \
-    allow_max_smem(oz_lane_kernel<S, C, K>, P.smem, "oz smem attribute");        \
-  else                                                                           \
-    allow_max_smem(oz_lane1_kernel<S, C, K>, P.smem, "oz smem attribute");
-  switch (P.mmax) {
-    case 1: MDFT_OZ_ATTR2(1) break;
-    case 2: MDFT_OZ_ATTR2(2) break;
-    case 3: MDFT_OZ_ATTR2(3) break;
-    case 4: MDFT_OZ_ATTR2(4) break;
-    case 5: MDFT_OZ_ATTR2(5) break;
-    case 6: MDFT_OZ_ATTR2(6) break;
-  }
-#undef MDFT_OZ_ATTR2
+  lane_attr_all<S, C>(P);
 }
 
 template <typename C>
 void oz_build_rtab(const OzPlan& P, DevBuf& rtab) {
-  const long long n = P.npairs_pad * (long long)P.nR;
-  constexpr bool keep64 = std::is_same<C, double>::value;
+  // the unsplit kernel (FP64) reads the full table, the split kernels the
+  // half table (entries with m1 >= 0)
+  constexpr bool split = split_pairs<C>();
+  const int nfull = nrot(P.mmax), nhalf = hoff(P.mmax + 1);
+  throw_if(P.nR != (split ? nhalf : nfull), "internal: R table size", 4);
+  OzPlan F = P;
+  F.nR = nfull;
   DevBuf rt64;
-  DevBuf& target64 = keep64 ? rtab : rt64;
-  target64.alloc(sizeof(Cx<double>) * (size_t)n);
+  DevBuf& target64 = split ? rt64 : rtab;
+  target64.alloc(sizeof(Cx<double>) * (size_t)(P.npairs_pad * (long long)nfull));
   const long long nb = (P.npairs_pad + 127) / 128;
   clear_stale_error();
-  rot_table_kernel<<<(unsigned)nb, 128>>>(P, target64.as<Cx<double>>());
+  rot_table_kernel<<<(unsigned)nb, 128>>>(F, target64.as<Cx<double>>());
   launch_check("R(q) table kernel launch");
-  if (!keep64) {
-    rtab.alloc(sizeof(Cx<C>) * (size_t)n);
-    rot_table_convert<C><<<152 * 8, 256>>>(rt64.as<Cx<double>>(), rtab.as<Cx<C>>(), n);
+  if (split) {
+    rtab.alloc(sizeof(Cx<C>) * (size_t)(P.npairs_pad * (long long)nhalf));
+    rot_table_half<C><<<152 * 8, 256>>>(rt64.as<Cx<double>>(), rtab.as<Cx<C>>(), P.npairs_pad / 32,
+                                        P.mmax, nfull, nhalf);
     launch_check("R(q) table conversion launch");
   }
   cuda_check(cudaDeviceSynchronize(), "R(q) table build");
@@ -799,21 +956,15 @@ void launch_oz(const OzPlan& P, Cx<S>* p, cudaStream_t s) {
     const long long nb = (ngrp + P.warps_per_cta - 1) / P.warps_per_cta;
     throw_if(nb > 0x7fffffffLL, "too many k-space pairs", 4);
     const dim3 grid((unsigned)nb), block(32 * P.warps_per_cta);
-#define MDFT_OZ_LAUNCH(K)                                             \
-  if constexpr (split_pairs<C>())                                   \
-    oz_lane_kernel<S, C, K><<<grid, block, P.smem, s>>>(P, p);      \
-  else                                                              \
-    oz_lane1_kernel<S, C, K><<<grid, block, P.smem, s>>>(P, p);
     switch (P.mmax) {
-      case 1: MDFT_OZ_LAUNCH(1) break;
-      case 2: MDFT_OZ_LAUNCH(2) break;
-      case 3: MDFT_OZ_LAUNCH(3) break;
-      case 4: MDFT_OZ_LAUNCH(4) break;
-      case 5: MDFT_OZ_LAUNCH(5) break;
-      case 6: MDFT_OZ_LAUNCH(6) break;
+      case 1: lane_launch_one<S, C, 1>(P, p, grid, block, s); break;
+      case 2: lane_launch_one<S, C, 2>(P, p, grid, block, s); break;
+      case 3: lane_launch_one<S, C, 3>(P, p, grid, block, s); break;
+      case 4: lane_launch_one<S, C, 4>(P, p, grid, block, s); break;
+      case 5: lane_launch_one<S, C, 5>(P, p, grid, block, s); break;
+      case 6: lane_launch_one<S, C, 6>(P, p, grid, block, s); break;
       default: throw Error(4, "mmax outside the lane kernel's range");
     }
-#undef MDFT_OZ_LAUNCH
     launch_check("oz lane kernel launch");
     return;
   }
