@@ -37,8 +37,11 @@ constexpr int kRotL5 = 5, kRotM13 = 13;  // RotationCoeffs extents (l-2, m+6)
 
 __host__ __device__ constexpr int roff(int l) { return l * (2 * l - 1) * (2 * l + 1) / 3; }
 __host__ __device__ constexpr int nrot(int mmax) { return roff(mmax + 1); }
-// offset of block l in the half table (entries with m1 >= 0): sum (2l'+1)(l'+1)
-__host__ __device__ constexpr int hoff(int l) { return l == 0 ? 0 : hoff(l - 1) + (2 * l - 1) * l; }
+// offset of block l in the half table (entries with m1 >= 0):
+// sum_{l' < l} (2l'+1)(l'+1) = l(l+1)(4l-1)/6 (closed forms throughout: a
+// recursive constexpr function becomes a real call when an argument is not
+// a constant)
+__host__ __device__ constexpr int hoff(int l) { return l * (l + 1) * (4 * l - 1) / 6; }
 
 template <typename T>
 struct OzSmem {
@@ -497,10 +500,11 @@ struct PIndex {
   }
 };
 
-// coefficient slots of the OZ sum of one projection, terms n' < n, when
-// mrso is a compile-time constant: sum_{n' < n} (2 (n' / mrso) + 1)
+// coefficient slots of the OZ sum of one projection, terms n' < n:
+// sum_{n' < n} (2 (n' / mrso) + 1) = n + mrso q (q - 1) + 2 q (n mod mrso),
+// q = n / mrso
 __host__ __device__ constexpr int oz_coff(int n, int mrso) {
-  return n <= 0 ? 0 : oz_coff(n - 1, mrso) + 2 * ((n - 1) / mrso) + 1;
+  return n + mrso * (n / mrso) * (n / mrso - 1) + 2 * (n / mrso) * (n % mrso);
 }
 // projections of an angular grid: sum_m (2m+1)(m/mrso+1)
 __host__ __device__ constexpr int oz_np(int mmax, int mrso) {
