@@ -190,30 +190,25 @@ def timed_steps(P, K, flush):
 
 
 def stage_times(P, reps, flush):
-    """Average device time of each stage, for the roofline of the dominant
-    kernel (events on the launching stream)."""
+    """Average device time of each stage of the round trip as step() runs it
+    (CUDA events on the launching stream; the convolution's inner stages
+    through Convolution.execute_timed, so the double-float form is timed on
+    its packed kernels).  L2 is flushed before each round trip."""
     import torch
-    res = {}
-    stages = {
-        "angl2proj": lambda: P["opt"].angl2proj(P["dr"], P["p"]),
-        "fft_forward": lambda: P["conv"].fft(P["p"], -1),
-        "oz": lambda: P["conv"].kspace(P["p"]),
-        "fft_backward": lambda: P["conv"].fft(P["p"], +1),
-        "proj2angl": lambda: P["opt"].proj2angl(P["p"], P["vexc"]),
-    }
-    for name, fn in stages.items():
-        tot = 0.0
-        for _ in range(reps):
-            flush.zero_()
-            a = torch.cuda.Event(enable_timing=True)
-            b = torch.cuda.Event(enable_timing=True)
-            a.record()
-            fn()
-            b.record()
-            torch.cuda.synchronize()
-            tot += a.elapsed_time(b) / 1e3
-        res[name] = tot / reps
-    return res
+    names = ["angl2proj", "fft_forward", "oz", "fft_backward", "proj2angl"]
+    tot = dict.fromkeys(names, 0.0)
+    for _ in range(reps):
+        flush.zero_()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+        ev[0].record()
+        P["opt"].angl2proj(P["dr"], P["p"])
+        P["conv"].execute_timed(P["p"], ev[1:5])
+        P["opt"].proj2angl(P["p"], P["vexc"])
+        ev[5].record()
+        torch.cuda.synchronize()
+        for i, n in enumerate(names):
+            tot[n] += ev[i].elapsed_time(ev[i + 1]) / 1e3
+    return {n: t / reps for n, t in tot.items()}
 
 
 def e2e_steps(P, K, warm):

@@ -127,6 +127,15 @@ int mdft_conv_destroy(mdft_conv_t h);
  * p (np, nx, ny, nz): forward 3-D FFT, per-(q,-q) rotation + OZ + rotation
  * back, inverse 3-D FFT, all unnormalised as in the reference. */
 int mdft_conv_execute(mdft_conv_t h, void* p, void* stream);
+/* execute(deltarho_p) with its stages timed: events[0..3] are four
+ * cudaEvent_t (created by the caller, timing enabled), recorded on `stream`
+ * before the forward FFT and after the forward FFT, the k-space step and the
+ * inverse FFT.  Same kernels and results as mdft_conv_execute.  No
+ * counterpart in the reference (its execute has no stage timers); it exists
+ * so that a benchmark can time the stages as execute runs them (the
+ * double-float form keeps the projections packed between its stages, which
+ * the separate mdft_conv_fft / mdft_conv_kspace calls below do not). */
+int mdft_conv_execute_timed(mdft_conv_t h, void* p, void* stream, void* const* events);
 /* The two 3-D FFT passes of execute on their own (sign -1 forward,
  * +1 backward; unnormalised), and the k-space step alone. */
 int mdft_conv_fft(mdft_conv_t h, void* p, int sign, void* stream);

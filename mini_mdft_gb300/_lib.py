@@ -43,6 +43,7 @@ SIGNATURES = {
     "mdft_conv_create_from_file": (i32, [C.POINTER(vp), vp, C.c_char_p, i32, i32]),
     "mdft_conv_destroy": (i32, [vp]),
     "mdft_conv_execute": (i32, [vp, vp, vp]),
+    "mdft_conv_execute_timed": (i32, [vp, vp, vp, C.POINTER(vp)]),
     "mdft_conv_fft": (i32, [vp, vp, i32, vp]),
     "mdft_conv_kspace": (i32, [vp, vp, vp]),
     "mdft_conv_info": (i32, [vp, ip, dp]),

@@ -272,6 +272,21 @@ class Convolution:
         _check_field(deltarho_p, self.N * self.np, self._cdt(), "deltarho_p")
         check(lib().mdft_conv_execute(self.h, _dptr(deltarho_p), _stream()))
 
+    def execute_timed(self, deltarho_p, events):
+        """execute() with its stages timed: ``events`` are four
+        torch.cuda.Event(enable_timing=True), recorded on the current stream
+        before the forward FFT and after the forward FFT, the k-space step and
+        the inverse FFT (mdft_conv_execute_timed).  No counterpart in the
+        reference; it times the kernels execute() itself runs."""
+        _check_field(deltarho_p, self.N * self.np, self._cdt(), "deltarho_p")
+        if len(events) != 4:
+            raise ValueError("execute_timed needs four events")
+        for e in events:
+            if not e.cuda_event:  # torch creates the CUDA event on first record
+                e.record()
+        arr = (C.c_void_p * 4)(*[C.c_void_p(e.cuda_event) for e in events])
+        check(lib().mdft_conv_execute_timed(self.h, _dptr(deltarho_p), _stream(), arr))
+
     def fft(self, p, sign):
         _check_field(p, self.N * self.np, self._cdt(), "p")
         check(lib().mdft_conv_fft(self.h, _dptr(p), int(sign), _stream()))

@@ -624,26 +624,53 @@ int mdft_conv_kspace(mdft_conv_t h, void* p, void* stream) {
   });
 }
 
+namespace {
+// execute(): forward FFT, k-space step, inverse FFT.  ev (optional) receives
+// an event record before the forward FFT and after each of the three stages.
+void conv_execute(mdft_conv_s* h, void* p, cudaStream_t s, cudaEvent_t const* ev) {
+  auto mark = [&](int i) {
+    if (ev) mdft::cuda_check(cudaEventRecord(ev[i], s), "stage event record");
+  };
+  with_types(h->prec, [&](auto st, auto ct) {
+    using S = decltype(st);
+    using C = decltype(ct);
+    if constexpr (std::is_same<C, mdft::DF>::value) {
+      if (h->df_packed) {
+        mark(0);
+        conv_fft<S, C>(h, p, -1, s, false, true);
+        mark(1);
+        mdft::launch_oz<mdft::DF, C>(h->oz, static_cast<Cx<mdft::DF>*>(p), s);
+        mark(2);
+        conv_fft<S, C>(h, p, +1, s, true, false);
+        mark(3);
+        return;
+      }
+    }
+    mark(0);
+    conv_fft<S, C>(h, p, -1, s);
+    mark(1);
+    mdft::launch_oz<S, C>(h->oz, static_cast<Cx<S>*>(p), s);
+    mark(2);
+    conv_fft<S, C>(h, p, +1, s);
+    mark(3);
+  });
+}
+}  // namespace
+
 int mdft_conv_execute(mdft_conv_t h, void* p, void* stream) {
   return guarded([&] {
     throw_if(!h || !p, "NULL argument");
     check_device(h->device);
-    cudaStream_t s = as_stream(stream);
-    with_types(h->prec, [&](auto st, auto ct) {
-      using S = decltype(st);
-      using C = decltype(ct);
-      if constexpr (std::is_same<C, mdft::DF>::value) {
-        if (h->df_packed) {
-          conv_fft<S, C>(h, p, -1, s, false, true);
-          mdft::launch_oz<mdft::DF, C>(h->oz, static_cast<Cx<mdft::DF>*>(p), s);
-          conv_fft<S, C>(h, p, +1, s, true, false);
-          return;
-        }
-      }
-      conv_fft<S, C>(h, p, -1, s);
-      mdft::launch_oz<S, C>(h->oz, static_cast<Cx<S>*>(p), s);
-      conv_fft<S, C>(h, p, +1, s);
-    });
+    conv_execute(h, p, as_stream(stream), nullptr);
+  });
+}
+
+int mdft_conv_execute_timed(mdft_conv_t h, void* p, void* stream, void* const* events) {
+  return guarded([&] {
+    throw_if(!h || !p || !events, "NULL argument");
+    for (int i = 0; i < 4; ++i) throw_if(!events[i], "NULL event");
+    check_device(h->device);
+    conv_execute(h, p, as_stream(stream), reinterpret_cast<cudaEvent_t const*>(events));
   });
 }
 

@@ -182,6 +182,29 @@ def test_conv_execute(gpu_lib, n, box, mmax, mrso, prec):
     assert rel_err(_np(t), ref) < _tol(prec)
 
 
+@pytest.mark.parametrize("prec", PRECS)
+def test_conv_execute_timed_equals_execute(gpu_lib, prec):
+    """The stage-timed execute runs the same kernels: bit-identical output,
+    and its four events come in stream order."""
+    import torch
+    M = gpu_lib
+    n = (16, 12, 10)
+    o, conv, _, _ = _conv_pair(M, n, (20., 15., 12.), 3, 2, prec)
+    rng = np.random.default_rng(7)
+    shp = (o.np,) + tuple(n)
+    p = rng.uniform(0, 1, shp) + 1j * rng.uniform(0, 1, shp)
+    rd, cd = _dtypes(prec)
+    a, b = _t(p, cd), _t(p, cd)
+    conv.execute(a)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    conv.execute_timed(b, ev)
+    torch.cuda.synchronize()
+    assert torch.equal(a, b)
+    assert all(ev[i].elapsed_time(ev[i + 1]) >= 0.0 for i in range(3))
+    with pytest.raises(ValueError):
+        conv.execute_timed(b, ev[:3])
+
+
 def test_conv_tables_match_oracle(gpu_lib):
     M = gpu_lib
     o, conv, _, _ = _conv_pair(M, (6, 5, 4), (9., 8., 7.), 5, 2, "f64")
