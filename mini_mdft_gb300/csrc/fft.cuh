@@ -190,15 +190,50 @@ struct RList {};
 template <int N>
 struct FftRadices;
 template <> struct FftRadices<16> { using type = RList<4, 4>; };
-template <> struct FftRadices<32> { using type = RList<4, 4, 2>; };
-template <> struct FftRadices<64> { using type = RList<4, 4, 4>; };
-template <> struct FftRadices<128> { using type = RList<4, 4, 4, 2>; };
-template <> struct FftRadices<256> { using type = RList<4, 4, 4, 4>; };
+template <> struct FftRadices<32> { using type = RList<8, 4>; };
+template <> struct FftRadices<64> { using type = RList<8, 8>; };
+template <> struct FftRadices<128> { using type = RList<8, 4, 4>; };
+template <> struct FftRadices<256> { using type = RList<8, 8, 4>; };
 template <> struct FftRadices<48> { using type = RList<4, 4, 3>; };
-template <> struct FftRadices<96> { using type = RList<4, 4, 2, 3>; };
-template <> struct FftRadices<192> { using type = RList<4, 4, 4, 3>; };
+template <> struct FftRadices<96> { using type = RList<8, 4, 3>; };
+template <> struct FftRadices<192> { using type = RList<8, 8, 3>; };
 template <> struct FftRadices<80> { using type = RList<4, 4, 5>; };
-template <> struct FftRadices<160> { using type = RList<4, 4, 2, 5>; };
+template <> struct FftRadices<160> { using type = RList<8, 4, 5>; };
+
+// x * w for a twiddle w: the plain complex product, and for double-float
+// each component a.b + c.d as two exact FMA products whose high parts meet
+// in one TwoSum (19 FP32 instructions a component instead of 25)
+template <typename T>
+__device__ __forceinline__ Cx<T> cmul_tw(Cx<T> x, Cx<T> w) {
+  return x * w;
+}
+__device__ __forceinline__ DF df_dot2_pair(DF a, DF b, DF c, DF d) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  const float q = c.hi * d.hi;
+  float f = fmaf(c.hi, d.hi, -q);
+  f = fmaf(c.hi, d.lo, f);
+  f = fmaf(c.lo, d.hi, f);
+  const DF s = df_two_sum(p, q);
+  return df_fast_two_sum(s.hi, s.lo + (e + f));
+}
+template <>
+__device__ __forceinline__ Cx<DF> cmul_tw<DF>(Cx<DF> x, Cx<DF> w) {
+  return mkc<DF>(df_dot2_pair(x.re, w.re, -x.im, w.im), df_dot2_pair(x.re, w.im, x.im, w.re));
+}
+// the length-4 DFT on registers (forward: e^{-2 pi i nk/4})
+template <typename T, bool FWD>
+__device__ __forceinline__ void dft4(Cx<T>& v0, Cx<T>& v1, Cx<T>& v2, Cx<T>& v3) {
+  const Cx<T> a0 = v0 + v2, a1 = v0 - v2;
+  const Cx<T> b0 = v1 + v3, b1 = v1 - v3;
+  const Cx<T> jb = FWD ? mkc<T>(b1.im, -b1.re) : mkc<T>(-b1.im, b1.re);
+  v0 = a0 + b0;
+  v1 = a1 + jb;
+  v2 = a0 - b0;
+  v3 = a1 - jb;
+}
 
 template <typename T, bool FWD>
 __device__ __forceinline__ Cx<T> tw_at(const Cx<T>* tw, int idx) {
@@ -215,18 +250,40 @@ __device__ __forceinline__ void dft_small(Cx<T>* v, const Cx<T>* tw, int n) {
     v[0] = a + b;
     v[1] = a - b;
   } else if constexpr (R == 4) {
-    const Cx<T> a0 = v[0] + v[2], a1 = v[0] - v[2];
-    const Cx<T> b0 = v[1] + v[3], b1 = v[1] - v[3];
-    const Cx<T> jb = FWD ? mkc<T>(b1.im, -b1.re) : mkc<T>(-b1.im, b1.re);
-    v[0] = a0 + b0;
-    v[1] = a1 + jb;
-    v[2] = a0 - b0;
-    v[3] = a1 - jb;
+    dft4<T, FWD>(v[0], v[1], v[2], v[3]);
+  } else if constexpr (R == 8) {
+    // two length-4 DFTs (even and odd inputs) and the e^{-+2 pi i k/8}
+    // twiddles between them; 1/sqrt(2) from the twiddle table, tw[n/8]
+    Cx<T> e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+    Cx<T> o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+    dft4<T, FWD>(e0, e1, e2, e3);
+    dft4<T, FWD>(o0, o1, o2, o3);
+    const T h = tw[n / 8].re;
+    // forward: o1 (1 - i) h, o2 (-i), o3 (-1 - i) h; inverse: conjugates
+    if (FWD) {
+      o1 = mkc<T>((o1.re + o1.im) * h, (o1.im - o1.re) * h);
+      o2 = mkc<T>(o2.im, -o2.re);
+      o3 = mkc<T>((o3.im - o3.re) * h, -(o3.re + o3.im) * h);
+    } else {
+      o1 = mkc<T>((o1.re - o1.im) * h, (o1.im + o1.re) * h);
+      o2 = mkc<T>(-o2.im, o2.re);
+      o3 = mkc<T>(-(o3.re + o3.im) * h, (o3.re - o3.im) * h);
+    }
+    v[0] = e0 + o0;
+    v[4] = e0 - o0;
+    v[1] = e1 + o1;
+    v[5] = e1 - o1;
+    v[2] = e2 + o2;
+    v[6] = e2 - o2;
+    v[3] = e3 + o3;
+    v[7] = e3 - o3;
   } else if constexpr (R == 3) {
-    const T s3 = T(0.86602540378443864676372317075293618);
+    // sin(2 pi / 3) from the twiddle table, tw[n/3] = (-1/2, -sin(2 pi/3))
+    const T s3 = -tw[n / 3].im;
     const Cx<T> a = v[0], b = v[1], c = v[2];
     const Cx<T> bc = b + c;
-    const Cx<T> t = mkc<T>(a.re - T(0.5) * bc.re, a.im - T(0.5) * bc.im);
+    const Cx<T> hb = mkc<T>(bc.re * tw[n / 3].re, bc.im * tw[n / 3].re);  // -bc/2
+    const Cx<T> t = mkc<T>(a.re + hb.re, a.im + hb.im);
     const Cx<T> u = mkc<T>(s3 * (b.re - c.re), s3 * (b.im - c.im));
     v[0] = a + bc;
     if (FWD) {
@@ -271,7 +328,8 @@ __device__ __forceinline__ Cx<T>* stages(Cx<T>* in, Cx<T>* out, const Cx<T>* tw,
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const Cx<T> x = in[(j + r * NR) * LD + c];
-        v[r] = r == 0 ? x : x * tw_at<T, FWD>(tw, k * r * TWS);
+        // the first stage (Ns = 1) has unit twiddles
+        v[r] = (r == 0 || Ns == 1) ? x : cmul_tw(x, tw_at<T, FWD>(tw, k * r * TWS));
       }
       dft_small<T, R, FWD>(v, tw, N);
       const int d = (j / Ns) * Ns * R + k;
@@ -354,6 +412,21 @@ constexpr int fixed_cols() {
   return sizeof(Cx<C>) == 16 ? 16 : 32;
 }
 
+// threads per CTA: one per butterfly of the widest stage (N / smallest radix
+// butterflies per column), at most 256
+template <int R, int... Rest>
+constexpr int min_radix(RList<R, Rest...>) {
+  if constexpr (sizeof...(Rest) == 0)
+    return R;
+  else
+    return R < min_radix(RList<Rest...>{}) ? R : min_radix(RList<Rest...>{});
+}
+template <typename C, int N>
+constexpr int fixed_threads() {
+  constexpr int w = N / min_radix(typename FftRadices<N>::type{}) * fixed_cols<C>();
+  return w < 256 ? w : 256;
+}
+
 template <typename C, int N>
 size_t fixed_smem() {
   constexpr int LD = fixed_cols<C>() + 1;
@@ -373,10 +446,11 @@ void fixed_launch(const FftAxis& a, void* data, int sign, cudaStream_t s) {
   constexpr int COLS = fixed_cols<C>();
   const long long nb = (a.ncols + COLS - 1) / COLS;
   throw_if(nb > 0x7fffffffLL, "FFT batch too large", 4);
+  constexpr int T = fixed_threads<C, N>();
   if (sign < 0)
-    fft_fixed_kernel<Si, So, C, N, COLS, true><<<(unsigned)nb, 256, fixed_smem<C, N>(), s>>>(a, data);
+    fft_fixed_kernel<Si, So, C, N, COLS, true><<<(unsigned)nb, T, fixed_smem<C, N>(), s>>>(a, data);
   else
-    fft_fixed_kernel<Si, So, C, N, COLS, false><<<(unsigned)nb, 256, fixed_smem<C, N>(), s>>>(a, data);
+    fft_fixed_kernel<Si, So, C, N, COLS, false><<<(unsigned)nb, T, fixed_smem<C, N>(), s>>>(a, data);
 }
 
 #define MDFT_FIXED_SIZES(X) X(16) X(32) X(64) X(128) X(256) X(48) X(96) X(192) X(80) X(160)
