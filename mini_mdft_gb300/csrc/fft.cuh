@@ -340,8 +340,8 @@ __device__ __forceinline__ Cx<T>* stages(Cx<T>* in, Cx<T>* out, const Cx<T>* tw,
   return stages<T, N, LD, FWD, Ns * R>(out, in, tw, cols, cc, RList<Rest...>{});
 }
 
-template <typename Si, typename So, typename C, int N, int COLS, bool FWD>
-__global__ void __launch_bounds__(256)
+template <typename Si, typename So, typename C, int N, int COLS, bool FWD, int THREADS>
+__global__ void __launch_bounds__(THREADS)
 fft_fixed_kernel(const FftAxis A, void* __restrict__ vdata) {
   const Cx<Si>* din = static_cast<const Cx<Si>*>(vdata);
   Cx<So>* dout = static_cast<Cx<So>*>(vdata);
@@ -355,19 +355,48 @@ fft_fixed_kernel(const FftAxis A, void* __restrict__ vdata) {
   const int cc = (int)min((long long)COLS, A.ncols - c0);
   const long long S_ = A.S;
   for (int i = tid; i < N; i += bd) tw[i] = static_cast<const Cx<C>*>(A.tw)[i];
+  // full tiles: every load of a thread issued before its shared stores (one
+  // memory round trip per tile); THREADS is the launch's block size
+  constexpr int IT = N * COLS / THREADS;
+  static_assert(N * COLS % THREADS == 0, "tile and block size");
   if (S_ == 1) {
     const Cx<Si>* src = din + c0 * N;
-    for (int i = tid; i < N * cc; i += bd) {
-      const int c = i / N, j = i % N;
-      buf0[j * LD + c] = ld_c<C>(src[i]);
+    if (cc == COLS) {
+      Cx<Si> v[IT];
+#pragma unroll
+      for (int r = 0; r < IT; ++r) v[r] = src[tid + r * THREADS];
+#pragma unroll
+      for (int r = 0; r < IT; ++r) {
+        const int i = tid + r * THREADS, c = i / N, j = i % N;
+        buf0[j * LD + c] = ld_c<C>(v[r]);
+      }
+    } else {
+      for (int i = tid; i < N * cc; i += bd) {
+        const int c = i / N, j = i % N;
+        buf0[j * LD + c] = ld_c<C>(src[i]);
+      }
     }
   } else {
     const long long b = c0 / S_, s0 = c0 % S_;
     if (s0 + cc <= S_) {  // the tile's columns are one contiguous run per row
       const Cx<Si>* base = din + b * N * S_ + s0;
-      for (int i = tid; i < N * COLS; i += bd) {
-        const int j = i / COLS, c = i % COLS;
-        if (c < cc) buf0[j * LD + c] = ld_c<C>(base[(long long)j * S_ + c]);
+      if (cc == COLS) {
+        Cx<Si> v[IT];
+#pragma unroll
+        for (int r = 0; r < IT; ++r) {
+          const int i = tid + r * THREADS, j = i / COLS, c = i % COLS;
+          v[r] = base[(long long)j * S_ + c];
+        }
+#pragma unroll
+        for (int r = 0; r < IT; ++r) {
+          const int i = tid + r * THREADS, j = i / COLS, c = i % COLS;
+          buf0[j * LD + c] = ld_c<C>(v[r]);
+        }
+      } else {
+        for (int i = tid; i < N * COLS; i += bd) {
+          const int j = i / COLS, c = i % COLS;
+          if (c < cc) buf0[j * LD + c] = ld_c<C>(base[(long long)j * S_ + c]);
+        }
       }
     } else {
       for (int i = tid; i < N * COLS; i += bd) {
@@ -435,9 +464,10 @@ size_t fixed_smem() {
 
 template <typename Si, typename So, typename C, int N>
 void fixed_attr() {
-  allow_max_smem(fft_fixed_kernel<Si, So, C, N, fixed_cols<C>(), true>, fixed_smem<C, N>(),
+  constexpr int T = fixed_threads<C, N>();
+  allow_max_smem(fft_fixed_kernel<Si, So, C, N, fixed_cols<C>(), true, T>, fixed_smem<C, N>(),
                  "fft smem attribute");
-  allow_max_smem(fft_fixed_kernel<Si, So, C, N, fixed_cols<C>(), false>, fixed_smem<C, N>(),
+  allow_max_smem(fft_fixed_kernel<Si, So, C, N, fixed_cols<C>(), false, T>, fixed_smem<C, N>(),
                  "fft smem attribute");
 }
 
@@ -448,9 +478,9 @@ void fixed_launch(const FftAxis& a, void* data, int sign, cudaStream_t s) {
   throw_if(nb > 0x7fffffffLL, "FFT batch too large", 4);
   constexpr int T = fixed_threads<C, N>();
   if (sign < 0)
-    fft_fixed_kernel<Si, So, C, N, COLS, true><<<(unsigned)nb, T, fixed_smem<C, N>(), s>>>(a, data);
+    fft_fixed_kernel<Si, So, C, N, COLS, true, T><<<(unsigned)nb, T, fixed_smem<C, N>(), s>>>(a, data);
   else
-    fft_fixed_kernel<Si, So, C, N, COLS, false><<<(unsigned)nb, T, fixed_smem<C, N>(), s>>>(a, data);
+    fft_fixed_kernel<Si, So, C, N, COLS, false, T><<<(unsigned)nb, T, fixed_smem<C, N>(), s>>>(a, data);
 }
 
 #define MDFT_FIXED_SIZES(X) X(16) X(32) X(64) X(128) X(256) X(48) X(96) X(192) X(80) X(160)
