@@ -145,14 +145,16 @@ angl2proj_fast_kernel(const AngPlan P, const S* __restrict__ o, Cx<S>* __restric
       Y[f][0] = mkc<C>(s0, C(0));
 #pragma unroll
       for (int k = 1; k <= K; ++k) {
-        C re = r[0], im = C(0);
+        Acc<C> re, im;
+        acc_set(re, r[0]);
+        acc_zero(im);
 #pragma unroll
         for (int j = 1; j <= HPSI; ++j) {
           const Cx<C> t = ldtw<C>(P.tw_psi, (k * j) % NPSI);
-          re = re + (r[j] + r[NPSI - j]) * t.re;
-          im = im + (r[j] - r[NPSI - j]) * t.im;
+          acc_mac(re, r[j] + r[NPSI - j], t.re);
+          acc_mac(im, r[j] - r[NPSI - j], t.im);
         }
-        Y[f][k] = mkc<C>(re, im);
+        Y[f][k] = mkc<C>(acc_get(re), acc_get(im));
       }
     }
     Cx<C>* zt = Zs + (size_t)th * (K + 1) * NPHI * PTS + q;
@@ -164,13 +166,16 @@ angl2proj_fast_kernel(const AngPlan P, const S* __restrict__ o, Cx<S>* __restric
       zt[(0 + MMAX) * PTS] = mkc<C>(s0, C(0));
 #pragma unroll
       for (int k = 1; k <= HPHI; ++k) {
-        C re = Y[0][0].re, im = C(0);
+        Acc<C> are, aim;
+        acc_set(are, Y[0][0].re);
+        acc_zero(aim);
 #pragma unroll
         for (int j = 1; j <= HPHI; ++j) {
           const Cx<C> t = ldtw<C>(P.tw_phi, (k * j) % NPHI);
-          re = re + (Y[j][0].re + Y[NPHI - j][0].re) * t.re;
-          im = im + (Y[j][0].re - Y[NPHI - j][0].re) * t.im;
+          acc_mac(are, Y[j][0].re + Y[NPHI - j][0].re, t.re);
+          acc_mac(aim, Y[j][0].re - Y[NPHI - j][0].re, t.im);
         }
+        const C re = acc_get(are), im = acc_get(aim);
         // s_f(mup) = conj(o_hat(mup mod nphi)); mup = k and mup = -k
         zt[(k + MMAX) * PTS] = mkc<C>(re, -im);
         zt[(-k + MMAX) * PTS] = mkc<C>(re, im);
@@ -186,14 +191,21 @@ angl2proj_fast_kernel(const AngPlan P, const S* __restrict__ o, Cx<S>* __restric
       zk[(0 + MMAX) * PTS] = conj(s0);
 #pragma unroll
       for (int k = 1; k <= HPHI; ++k) {
-        Cx<C> Pk = Y[0][kp], Qk = mkc<C>(C(0), C(0));
+        Acc<C> pr, pi, qr, qi;
+        acc_set(pr, Y[0][kp].re);
+        acc_set(pi, Y[0][kp].im);
+        acc_zero(qr);
+        acc_zero(qi);
 #pragma unroll
         for (int j = 1; j <= HPHI; ++j) {
           const Cx<C> t = ldtw<C>(P.tw_phi, (k * j) % NPHI);  // (cos, -sin)
           const Cx<C> A = Y[j][kp] + Y[NPHI - j][kp], B = Y[j][kp] - Y[NPHI - j][kp];
-          Pk = mkc<C>(Pk.re + A.re * t.re, Pk.im + A.im * t.re);
-          Qk = mkc<C>(Qk.re + B.re * t.im, Qk.im + B.im * t.im);
+          acc_mac(pr, A.re, t.re);
+          acc_mac(pi, A.im, t.re);
+          acc_mac(qr, B.re, t.im);
+          acc_mac(qi, B.im, t.im);
         }
+        const Cx<C> Pk = mkc<C>(acc_get(pr), acc_get(pi)), Qk = mkc<C>(acc_get(qr), acc_get(qi));
         // X(k) = P + i Q', X(n-k) = P - i Q' with Q' = sum B (-sin) = Qk
         const Cx<C> Xk = mkc<C>(Pk.re - Qk.im, Pk.im + Qk.re);
         const Cx<C> Xn = mkc<C>(Pk.re + Qk.im, Pk.im - Qk.re);
@@ -210,13 +222,17 @@ angl2proj_fast_kernel(const AngPlan P, const S* __restrict__ o, Cx<S>* __restric
     if (q >= cnt) continue;
     const int mm = idx_s[ip], mupi = mm & 0xffff, mu2 = mm >> 16;
     const Cx<C>* z = Zs + ((size_t)mu2 * NPHI + mupi) * PTS + q;
-    Cx<C> sum = mkc<C>(C(0), C(0));
+    Acc<C> sre, sim;
+    acc_zero(sre);
+    acc_zero(sim);
 #pragma unroll
     for (int th = 0; th < NT; ++th) {
       const Cx<C> v = z[(size_t)th * (K + 1) * NPHI * PTS];
       const C c = coef_s[th * NP + ip];
-      sum = mkc<C>(sum.re + v.re * c, sum.im + v.im * c);
+      acc_mac(sre, v.re, c);
+      acc_mac(sim, v.im, c);
     }
+    const Cx<C> sum = mkc<C>(acc_get(sre), acc_get(sim));
     p[(long long)ip * P.N + pt0 + q] = mkc<S>(to_storage<S>(sum.re), to_storage<S>(sum.im));
   }
 }
@@ -265,7 +281,9 @@ proj2angl_fast_kernel(const AngPlan P, const Cx<S>* __restrict__ p, S* __restric
     for (int mup = -MMAX; mup <= MMAX; ++mup) {
 #pragma unroll
       for (int kp = 0; kp <= K; ++kp) {
-        Cx<C> s = mkc<C>(C(0), C(0));
+        Acc<C> sre, sim;
+        acc_zero(sre);
+        acc_zero(sim);
         const int a = mup < 0 ? -mup : mup, b = MRSO * kp;
         const int m0 = a > b ? a : b;
 #pragma unroll
@@ -273,8 +291,10 @@ proj2angl_fast_kernel(const AngPlan P, const Cx<S>* __restrict__ p, S* __restric
           const int ip = Sh::ip(m, mup, kp);
           const Cx<C> v = Ps[ip * PTS + q];
           const C c = coef[th * NP + ip];
-          s = mkc<C>(s.re + v.re * c, s.im + v.im * c);
+          acc_mac(sre, v.re, c);
+          acc_mac(sim, v.im, c);
         }
+        const Cx<C> s = mkc<C>(acc_get(sre), acc_get(sim));
         const int kf = mup >= 0 ? mup : mup + NPHI;
         oh[kf][kp] = conj(s);
       }
@@ -289,13 +309,16 @@ proj2angl_fast_kernel(const AngPlan P, const Cx<S>* __restrict__ p, S* __restric
 #pragma unroll
       for (int f = 1; f <= HPHI; ++f) {
         // Re sum_k oh(k) e^{+i 2 pi k f / n}, pairing k with n - k
-        C ca = oh[0][0].re, cb = C(0);
+        Acc<C> aa, ab;
+        acc_set(aa, oh[0][0].re);
+        acc_zero(ab);
 #pragma unroll
         for (int k = 1; k <= HPHI; ++k) {
           const Cx<C> t = ldtw<C>(P.tw_phi, (k * f) % NPHI);  // (cos, -sin)
-          ca = ca + (oh[k][0].re + oh[NPHI - k][0].re) * t.re;
-          cb = cb + (oh[k][0].im - oh[NPHI - k][0].im) * t.im;
+          acc_mac(aa, oh[k][0].re + oh[NPHI - k][0].re, t.re);
+          acc_mac(ab, oh[k][0].im - oh[NPHI - k][0].im, t.im);
         }
+        const C ca = acc_get(aa), cb = acc_get(ab);
         // Re(f) = ca + sum (im_k - im_{n-k}) sin = ca - cb ; Re(n-f) = ca + cb
         u0[f] = ca + cb;
         u0[NPHI - f] = ca - cb;
@@ -310,14 +333,21 @@ proj2angl_fast_kernel(const AngPlan P, const Cx<S>* __restrict__ p, S* __restric
       u[0][kp] = s0;
 #pragma unroll
       for (int f = 1; f <= HPHI; ++f) {
-        Cx<C> Pf = oh[0][kp], Qf = mkc<C>(C(0), C(0));
+        Acc<C> pr, pi, qr, qi;
+        acc_set(pr, oh[0][kp].re);
+        acc_set(pi, oh[0][kp].im);
+        acc_zero(qr);
+        acc_zero(qi);
 #pragma unroll
         for (int k = 1; k <= HPHI; ++k) {
           const Cx<C> t = ldtw<C>(P.tw_phi, (k * f) % NPHI);
           const Cx<C> A = oh[k][kp] + oh[NPHI - k][kp], B = oh[k][kp] - oh[NPHI - k][kp];
-          Pf = mkc<C>(Pf.re + A.re * t.re, Pf.im + A.im * t.re);
-          Qf = mkc<C>(Qf.re + B.re * t.im, Qf.im + B.im * t.im);
+          acc_mac(pr, A.re, t.re);
+          acc_mac(pi, A.im, t.re);
+          acc_mac(qr, B.re, t.im);
+          acc_mac(qi, B.im, t.im);
         }
+        const Cx<C> Pf = mkc<C>(acc_get(pr), acc_get(pi)), Qf = mkc<C>(acc_get(qr), acc_get(qi));
         // backward: X(f) = P - i Q', X(n-f) = P + i Q', Q' = sum B (-sin) = Qf
         u[f][kp] = mkc<C>(Pf.re + Qf.im, Pf.im - Qf.re);
         u[NPHI - f][kp] = mkc<C>(Pf.re - Qf.im, Pf.im + Qf.re);
@@ -329,13 +359,15 @@ proj2angl_fast_kernel(const AngPlan P, const Cx<S>* __restrict__ p, S* __restric
     for (int f = 0; f < NPHI; ++f) {
 #pragma unroll
       for (int j = 0; j < NPSI; ++j) {
-        C v = u0[f];
+        Acc<C> v;
+        acc_set(v, u0[f]);
 #pragma unroll
         for (int kp = 1; kp <= K; ++kp) {
           const Cx<C> e = ldtw<C>(P.tw_psi, (kp * j) % NPSI);  // (cos, -sin)
-          v = v + C(2) * (u[f][kp].re * e.re + u[f][kp].im * e.im);
+          acc_mac(v, twice(u[f][kp].re), e.re);
+          acc_mac(v, twice(u[f][kp].im), e.im);
         }
-        out[f * NPSI + j] = v;
+        out[f * NPSI + j] = acc_get(v);
       }
     }
   }

@@ -103,10 +103,10 @@ __host__ __device__ __forceinline__ bool df_abs_lt(DF x, float e) {
 }
 
 // double <-> double-float conversions built from the IEEE bit fields with
-// integer and FP32 instructions only: the hardware double<->float conversions
-// and the FP64 add they would need share this GPU's narrow FP64 pipe, and
-// even an untaken fallback branch costs FP64 issue slots once the compiler
-// predicates it.  Host and device run the same code.
+// integer and FP32 instructions: the hardware double<->float conversions run
+// on this GPU's narrow FP64 pipe, and even an untaken fallback branch costs
+// FP64 issue slots once the compiler predicates it.  Host and device run the
+// same code.
 __host__ __device__ __forceinline__ unsigned long long bits_of(double x) {
 #ifdef __CUDA_ARCH__
   return (unsigned long long)__double_as_longlong(x);
@@ -208,54 +208,11 @@ __host__ __device__ __forceinline__ double f2d_bits(float f) {
   return double_of(s | ((unsigned long long)(ex + 896u) << 52) | (fr << 29));
 }
 
-// (hi, lo) -> double: the two significands aligned in a 64-bit integer,
-// added, and rounded to 53 bits (to nearest, ties away from zero); equal to
-// the rounded sum hi + lo except on exact ties.
-__host__ __device__ __forceinline__ double df_to_double_bits(DF a) {
-  const unsigned uh = bits_of(a.hi), ul = bits_of(a.lo);
-  const unsigned eh = (uh >> 23) & 0xffu, el = (ul >> 23) & 0xffu;
-  if (eh == 0xffu || (ul << 1) == 0) return f2d_bits(a.hi);  // inf/NaN, or lo = 0
-  if (el == 0xffu || (uh << 1) == 0) return f2d_bits(a.lo);
-  // signed significands (subnormals: exponent 1, no implicit bit)
-  const long long mh = (long long)((uh & 0x7fffffu) | (eh ? 0x800000u : 0u));
-  const long long ml = (long long)((ul & 0x7fffffu) | (el ? 0x800000u : 0u));
-  const int xh = eh ? (int)eh : 1, xl = el ? (int)el : 1;
-  long long big = (uh >> 31) ? -mh : mh, small = (ul >> 31) ? -ml : ml;
-  int xb = xh, d = xh - xl;
-  if (d < 0) {
-    const long long t = big;
-    big = small;
-    small = t;
-    xb = xl;
-    d = -d;
-  }
-  // |each term| < 2^61; the shifted-out bits of the smaller term leave a
-  // sticky half unit, so S = 2 (big + small >> d) + sticky fits in 63 bits
-  // and rounds as the exact sum does
-  long long S = big * (1ll << 37);
-  bool sticky = false;
-  if (d < 62) {
-    const long long t = small * (1ll << 37);
-    S += t >> d;
-    sticky = (t & ((1ll << d) - 1)) != 0;
-  } else {
-    sticky = small != 0;
-  }
-  S = 2 * S + (sticky ? 1 : 0);
-  if (S == 0) return 0.0;
-  const unsigned long long sign = S < 0 ? 0x8000000000000000ull : 0ull;
-  unsigned long long U = S < 0 ? (unsigned long long)(-S) : (unsigned long long)S;
-  int top = 63 - clz64(U);  // value = U 2^(xb - 188)
-  if (top > 52) {
-    U += 1ull << (top - 53);  // round half away from zero
-    if (U >> (top + 1)) ++top;
-    U >>= top - 52;
-  } else {
-    U <<= 52 - top;
-  }
-  const unsigned long long be = (unsigned long long)(top + xb + 835);  // 836..1151
-  return double_of(sign | (be << 52) | (U & 0x000fffffffffffffull));
-}
+// (hi, lo) -> double: both halves widened exactly from their bits, then one
+// FP64 add, which rounds hi + lo correctly.  One FP64 instruction per value
+// (the narrow pipe is otherwise idle in the double-float kernels) costs far
+// less issue time than aligning and rounding the pair in 64-bit integers.
+__host__ __device__ __forceinline__ double df_to_double(DF a) { return f2d_bits(a.hi) + f2d_bits(a.lo); }
 
 // Sums of products.  For float and double a plain multiply-add chain (the
 // order of the scalar code it replaces).  For double-float a compensated dot
@@ -281,6 +238,23 @@ __host__ __device__ __forceinline__ void acc_zero(Acc<C>& a) {
 __host__ __device__ __forceinline__ void acc_zero(Acc<DF>& a) {
   a.hi = 0.f;
   a.lo = 0.f;
+}
+template <typename C>
+__host__ __device__ __forceinline__ void acc_set(Acc<C>& a, C v) {
+  a.s = v;
+}
+__host__ __device__ __forceinline__ void acc_set(Acc<DF>& a, DF v) {
+  a.hi = v.hi;
+  a.lo = v.lo;
+}
+// 2 x, exact
+template <typename C>
+__host__ __device__ __forceinline__ C twice(C x) {
+  return x + x;
+}
+template <>
+__host__ __device__ __forceinline__ DF twice<DF>(DF x) {
+  return DF(2.f * x.hi, 2.f * x.lo);
 }
 template <typename C>
 __host__ __device__ __forceinline__ void acc_mac(Acc<C>& a, C x, C y) {
@@ -352,7 +326,7 @@ __host__ __device__ __forceinline__ S to_storage(C x) {
 template <>
 __host__ __device__ __forceinline__ double to_storage<double, DF>(DF x) {
 #ifdef __CUDA_ARCH__
-  return df_to_double_bits(x);
+  return df_to_double(x);
 #else
   return (double)x;
 #endif

@@ -4,7 +4,7 @@ checked on the host: df_bits_check.cu includes the same header, and its
 functions are __host__ __device__, so the host build runs the device code
 path.  f2d_bits must equal the hardware float->double conversion bit for
 bit; df_from_double_bits must hold x to 2^-47 in the double-float range and
-map the rest to truncated floats, +-inf or NaN; df_to_double_bits must round
+map the rest to truncated floats, +-inf or NaN; df_to_double must round
 hi + lo to the nearest double."""
 import os
 import shutil
