@@ -95,6 +95,12 @@ int mdft_grid_opmap(mdft_grid_t g, int* p, int* m, int* mup, int* mu,
  * Constructor (MDFT_OrientationProjectionTransform.hpp:217-257): uploads the
  * Wigner-d/quadrature tables to the current device. */
 int mdft_opt_create(mdft_opt_t* out, mdft_grid_t g, int precision);
+/* Batched plan: one call transforms `batch` same-shape fields stored back to
+ * back, o (batch, nx*ny*nz, ntheta, nphi, npsi) and p (np, batch, nx, ny, nz).
+ * No counterpart in the reference (one field per call there); it lets a
+ * server run many small same-shape jobs as one set of launches.  batch in
+ * [1, 65535], batch * nx*ny*nz < 2^31.  mdft_opt_create = batch 1. */
+int mdft_opt_create_batched(mdft_opt_t* out, mdft_grid_t g, int precision, int batch);
 int mdft_opt_destroy(mdft_opt_t h);
 /* angl2proj(o, p), MDFT_OrientationProjectionTransform.hpp:270-380:
  * real o -> complex p. */
@@ -119,6 +125,13 @@ int mdft_opt_angl2proj_from_xi(mdft_opt_t h, const void* xi, double rho0,
 int mdft_conv_create(mdft_conv_t* out, mdft_grid_t g, const int* luc_index,
                      const double* luc, int np_luc, int nq, double dq,
                      int precision);
+/* Batched plan (see mdft_opt_create_batched): execute, fft and kspace act on
+ * p (np, batch, nx, ny, nz), every field with the same c(q) table.  Needs the
+ * lane-per-pair k-space kernel (mmax <= 6).  No counterpart in the
+ * reference.  mdft_conv_create = batch 1. */
+int mdft_conv_create_batched(mdft_conv_t* out, mdft_grid_t g, const int* luc_index,
+                             const double* luc, int np_luc, int nq, double dq,
+                             int precision, int batch);
 /* Same, reading the Luc text file (ReadCLuc.hpp:40-260). */
 int mdft_conv_create_from_file(mdft_conv_t* out, mdft_grid_t g,
                                const char* path, int np_luc, int precision);

@@ -35,11 +35,13 @@ SIGNATURES = {
     "mdft_grid_angular": (i32, [vp, dp, dp, dp]),
     "mdft_grid_opmap": (i32, [vp, ip, ip, ip, ip, ip, dp]),
     "mdft_opt_create": (i32, [C.POINTER(vp), vp, i32]),
+    "mdft_opt_create_batched": (i32, [C.POINTER(vp), vp, i32, i32]),
     "mdft_opt_destroy": (i32, [vp]),
     "mdft_opt_angl2proj": (i32, [vp, vp, vp, vp]),
     "mdft_opt_proj2angl": (i32, [vp, vp, vp, vp]),
     "mdft_opt_angl2proj_from_xi": (i32, [vp, vp, f64, vp, vp]),
     "mdft_conv_create": (i32, [C.POINTER(vp), vp, ip, dp, i32, i32, f64, i32]),
+    "mdft_conv_create_batched": (i32, [C.POINTER(vp), vp, ip, dp, i32, i32, f64, i32, i32]),
     "mdft_conv_create_from_file": (i32, [C.POINTER(vp), vp, C.c_char_p, i32, i32]),
     "mdft_conv_destroy": (i32, [vp]),
     "mdft_conv_execute": (i32, [vp, vp, vp]),

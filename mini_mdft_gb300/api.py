@@ -179,12 +179,15 @@ class OrientationProjectionTransform:
     tensors passed to angl2proj/proj2angl must match it (float64/complex128
     for "f64" and "f64df")."""
 
-    def __init__(self, spatial_grid, angular_grid, map=None, precision="f64"):
+    def __init__(self, spatial_grid, angular_grid, map=None, precision="f64", batch=1):
         sg, ag = spatial_grid, angular_grid
         self._g = _GridHandle(sg.m_n_nodes, sg.m_length, ag.m_mmax, ag.m_molrotsymorder)
         self.precision = _precision_arg(precision)
+        self.batch = int(batch)
         h = C.c_void_p()
-        check(lib().mdft_opt_create(C.byref(h), self._g.h, self.precision))
+        # batch > 1: `batch` same-shape fields per call, stored back to back
+        # (mdft_opt_create_batched; no counterpart in the reference)
+        check(lib().mdft_opt_create_batched(C.byref(h), self._g.h, self.precision, self.batch))
         self.h = h
         g = self._g
         self.N = g.nx * g.ny * g.nz
@@ -203,21 +206,21 @@ class OrientationProjectionTransform:
 
     def angl2proj(self, o, p):
         rd, cd = self._dtypes()
-        _check_field(o, self.N * self.no, rd, "o")
-        _check_field(p, self.N * self.np, cd, "p")
+        _check_field(o, self.N * self.batch * self.no, rd, "o")
+        _check_field(p, self.N * self.batch * self.np, cd, "p")
         check(lib().mdft_opt_angl2proj(self.h, _dptr(o), _dptr(p), _stream()))
 
     def angl2proj_from_xi(self, xi, rho0, p):
         """get_delta_rho fused into angl2proj (delta_rho never stored)."""
         rd, cd = self._dtypes()
-        _check_field(xi, self.N * self.no, rd, "xi")
-        _check_field(p, self.N * self.np, cd, "p")
+        _check_field(xi, self.N * self.batch * self.no, rd, "xi")
+        _check_field(p, self.N * self.batch * self.np, cd, "p")
         check(lib().mdft_opt_angl2proj_from_xi(self.h, _dptr(xi), float(rho0), _dptr(p), _stream()))
 
     def proj2angl(self, p, o):
         rd, cd = self._dtypes()
-        _check_field(o, self.N * self.no, rd, "o")
-        _check_field(p, self.N * self.np, cd, "p")
+        _check_field(o, self.N * self.batch * self.no, rd, "o")
+        _check_field(p, self.N * self.batch * self.np, cd, "p")
         check(lib().mdft_opt_proj2angl(self.h, _dptr(p), _dptr(o), _stream()))
 
 
@@ -225,20 +228,24 @@ class Convolution:
     """Convolution(filename, spatial_grid, angular_grid, map, np_luc)."""
 
     def __init__(self, filename, spatial_grid, angular_grid, map=None, np_luc=None,
-                 precision="f64", _table=None):
+                 precision="f64", _table=None, batch=1):
         sg, ag = spatial_grid, angular_grid
         self._g = _GridHandle(sg.m_n_nodes, sg.m_length, ag.m_mmax, ag.m_molrotsymorder)
         self.precision = _precision_arg(precision)
+        self.batch = int(batch)
         h = C.c_void_p()
         if _table is not None:
             idx, tab, dq = _table
             idx = np.ascontiguousarray(idx, np.int32)
             tab = np.ascontiguousarray(tab, np.complex128)
             np_luc_, nq = tab.shape
-            check(lib().mdft_conv_create(C.byref(h), self._g.h, _np_i(idx),
-                                         tab.ctypes.data_as(C.POINTER(C.c_double)),
-                                         np_luc_, nq, float(dq), self.precision))
+            check(lib().mdft_conv_create_batched(C.byref(h), self._g.h, _np_i(idx),
+                                                 tab.ctypes.data_as(C.POINTER(C.c_double)),
+                                                 np_luc_, nq, float(dq), self.precision,
+                                                 self.batch))
         else:
+            if self.batch != 1:
+                raise ValueError("batched plans are built from a table (Convolution.from_table)")
             check(lib().mdft_conv_create_from_file(C.byref(h), self._g.h,
                                                    str(filename).encode(), int(np_luc),
                                                    self.precision))
@@ -254,10 +261,12 @@ class Convolution:
 
     @classmethod
     def from_table(cls, luc_index, table, dq, spatial_grid, angular_grid, map=None,
-                   precision="f64"):
-        """Same operator from a c(q) table already in memory (Luc layout)."""
+                   precision="f64", batch=1):
+        """Same operator from a c(q) table already in memory (Luc layout).
+        batch > 1: p holds `batch` same-shape fields, (np, batch, nx, ny, nz)
+        (mdft_conv_create_batched; no counterpart in the reference)."""
         return cls(None, spatial_grid, angular_grid, map, None, precision,
-                   _table=(luc_index, table, dq))
+                   _table=(luc_index, table, dq), batch=batch)
 
     def __del__(self):
         if getattr(self, "h", None) and _lib._lib is not None:
@@ -269,7 +278,7 @@ class Convolution:
         return (torch.complex64,) if self.precision == MDFT_F32 else (torch.complex128,)
 
     def execute(self, deltarho_p):
-        _check_field(deltarho_p, self.N * self.np, self._cdt(), "deltarho_p")
+        _check_field(deltarho_p, self.N * self.batch * self.np, self._cdt(), "deltarho_p")
         check(lib().mdft_conv_execute(self.h, _dptr(deltarho_p), _stream()))
 
     def execute_timed(self, deltarho_p, events):
@@ -278,7 +287,7 @@ class Convolution:
         before the forward FFT and after the forward FFT, the k-space step and
         the inverse FFT (mdft_conv_execute_timed).  No counterpart in the
         reference; it times the kernels execute() itself runs."""
-        _check_field(deltarho_p, self.N * self.np, self._cdt(), "deltarho_p")
+        _check_field(deltarho_p, self.N * self.batch * self.np, self._cdt(), "deltarho_p")
         if len(events) != 4:
             raise ValueError("execute_timed needs four events")
         for e in events:
@@ -288,11 +297,11 @@ class Convolution:
         check(lib().mdft_conv_execute_timed(self.h, _dptr(deltarho_p), _stream(), arr))
 
     def fft(self, p, sign):
-        _check_field(p, self.N * self.np, self._cdt(), "p")
+        _check_field(p, self.N * self.batch * self.np, self._cdt(), "p")
         check(lib().mdft_conv_fft(self.h, _dptr(p), int(sign), _stream()))
 
     def kspace(self, p):
-        _check_field(p, self.N * self.np, self._cdt(), "p")
+        _check_field(p, self.N * self.batch * self.np, self._cdt(), "p")
         check(lib().mdft_conv_kspace(self.h, _dptr(p), _stream()))
 
     def gamma_p_map(self):

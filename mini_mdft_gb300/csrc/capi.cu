@@ -109,6 +109,7 @@ struct mdft_opt_s {
   mdft::Grid g;
   int prec;
   int device;
+  int batch = 1;  // same-shape fields per call, stored back to back
   DevBuf coef_a2p, coef_p2a, tw_phi, tw_psi, ip_m, ip_mup, ip_mu2, pmap;
   mdft::AngPlan plan{};
   explicit mdft_opt_s(const mdft::Grid& gg) : g(gg) {}
@@ -118,6 +119,7 @@ struct mdft_conv_s {
   mdft::Grid g;
   int prec;
   int device;
+  int batch = 1;  // same-shape fields per call, p laid out (np, batch, nx, ny, nz)
   int npairs = 0, nq = 0;
   double dq = 0;
   std::vector<int> pair_list;                 // reference order (getter)
@@ -158,7 +160,7 @@ void opt_build(mdft_opt_s* h) {
   h->ip_mu2.upload(g.mu2.data(), sizeof(int) * np);
   h->pmap.upload(g.p.data(), sizeof(int) * g.p.size());
   mdft::AngPlan& P = h->plan;
-  P.N = g.N();
+  P.N = g.N() * h->batch;
   P.ntheta = g.ntheta;
   P.nphi = g.nphi;
   P.npsi = g.npsi;
@@ -249,6 +251,8 @@ void conv_build(mdft_conv_s* h, const mdft::LucTable& t) {
   O.nq = need;
   O.npairs = h->npairs;
   O.N = g.N();
+  O.nbatch = h->batch;
+  O.pstride = g.N() * h->batch;
   O.dq = t.dq;
   O.pairs = h->pairs.as<int4>();
   O.kx = h->kx.as<double>();
@@ -359,7 +363,7 @@ void conv_build(mdft_conv_s* h, const mdft::LucTable& t) {
     mdft::oz_build_rtab<T>(O, h->rtab);
     O.rtab = h->rtab.ptr;
   }
-  const long long N = g.N(), np = g.np;
+  const long long N = g.N(), np = (long long)g.np * h->batch;  // transforms per axis scale with the batch
   fft_axis_build<S, T>(h->az, h->tw_z, g.nz, 1, np * g.nx * g.ny);
   fft_axis_build<S, T>(h->ay, h->tw_y, g.ny, g.nz, np * g.nx * (long long)g.nz);
   fft_axis_build<S, T>(h->ax, h->tw_x, g.nx, (long long)g.ny * g.nz, np * (long long)g.ny * g.nz);
@@ -497,11 +501,18 @@ int mdft_grid_opmap(mdft_grid_t h, int* p, int* m, int* mup, int* mu, int* mu2, 
 }
 
 int mdft_opt_create(mdft_opt_t* out, mdft_grid_t g, int precision) {
+  return mdft_opt_create_batched(out, g, precision, 1);
+}
+
+int mdft_opt_create_batched(mdft_opt_t* out, mdft_grid_t g, int precision, int batch) {
   return guarded([&] {
     throw_if(!out || !g, "NULL argument");
     *out = nullptr;
     check_prec(precision);
+    throw_if(batch < 1 || batch > 65535, "batch must be 1..65535");
+    throw_if((long long)batch * g->g.N() >= (1LL << 31), "batch times grid points must stay below 2^31", 4);
     auto h = std::make_unique<mdft_opt_s>(g->g);
+    h->batch = batch;
     h->prec = precision;
     h->device = current_device();
     with_types(precision, [&](auto st, auto ct) { opt_build<decltype(st), decltype(ct)>(h.get()); });
@@ -550,12 +561,16 @@ int mdft_opt_proj2angl(mdft_opt_t h, const void* p, void* o, void* stream) {
   });
 }
 
-static int conv_create_impl(mdft_conv_t* out, mdft_grid_t g, const mdft::LucTable& t, int precision) {
+static int conv_create_impl(mdft_conv_t* out, mdft_grid_t g, const mdft::LucTable& t, int precision,
+                            int batch = 1) {
   return guarded([&] {
     throw_if(!out || !g, "NULL argument");
     *out = nullptr;
     check_prec(precision);
+    throw_if(batch < 1 || batch > 65535, "batch must be 1..65535");
+    throw_if((long long)batch * g->g.N() >= (1LL << 31), "batch times grid points must stay below 2^31", 4);
     auto h = std::make_unique<mdft_conv_s>(g->g);
+    h->batch = batch;
     h->prec = precision;
     h->device = current_device();
     with_types(precision, [&](auto st, auto ct) { conv_build<decltype(st), decltype(ct)>(h.get(), t); });
@@ -565,6 +580,11 @@ static int conv_create_impl(mdft_conv_t* out, mdft_grid_t g, const mdft::LucTabl
 
 int mdft_conv_create(mdft_conv_t* out, mdft_grid_t g, const int* luc_index, const double* luc,
                      int np_luc, int nq, double dq, int precision) {
+  return mdft_conv_create_batched(out, g, luc_index, luc, np_luc, nq, dq, precision, 1);
+}
+
+int mdft_conv_create_batched(mdft_conv_t* out, mdft_grid_t g, const int* luc_index, const double* luc,
+                             int np_luc, int nq, double dq, int precision, int batch) {
   mdft::LucTable t;
   int rc = guarded([&] {
     throw_if(!luc_index || !luc, "NULL argument");
@@ -580,7 +600,7 @@ int mdft_conv_create(mdft_conv_t* out, mdft_grid_t g, const int* luc_index, cons
     if (out) *out = nullptr;
     return rc;
   }
-  return conv_create_impl(out, g, t, precision);
+  return conv_create_impl(out, g, t, precision, batch);
 }
 
 int mdft_conv_create_from_file(mdft_conv_t* out, mdft_grid_t g, const char* path, int np_luc,

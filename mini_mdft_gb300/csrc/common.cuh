@@ -458,6 +458,10 @@ void launch_fft_axis(const FftAxis& a, void* data, int sign, cudaStream_t s);
 struct OzPlan {
   int nx, ny, nz, np, mmax, mrso, K, np_new, nq, npairs;
   long long N;
+  // batched plans: nbatch same-shape fields, p laid out (np, nbatch, N), so
+  // the projection stride is pstride = nbatch N and field b starts at b N
+  int nbatch;
+  long long pstride;
   double dq;
   const int4* pairs;       // (npairs) ix, iy, iz, 0 -- sorted by q's linear index
   const double* kx;        // (nx)

@@ -565,8 +565,9 @@ oz_lane_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
     }
   }
   const int4 info = P.pinfo[pair];
-  const long long N = P.N;
-  const long long lown = side ? info.y : info.x;
+  // projection stride; field blockIdx.y of a batched plan starts at y N
+  const long long N = P.pstride;
+  const long long lown = (side ? info.y : info.x) + (long long)blockIdx.y * P.N;
   // the q side does not store at self-paired k-points: the -q store wins
   const bool store = valid && (side == 1 || info.x != info.y);
   // Half table Rh(l, m, j) = R(l, m, j) for j >= 0; for m1 < 0,
@@ -747,7 +748,9 @@ oz_lane1_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
     }
   }
   const int4 info = P.pinfo[pair];
-  const long long N = P.N, lq = info.x, lmq = info.y;
+  // projection stride; field blockIdx.y of a batched plan starts at y N
+  const long long N = P.pstride, lq = info.x + (long long)blockIdx.y * P.N,
+                  lmq = info.y + (long long)blockIdx.y * P.N;
   const Cx<C>* Rt = static_cast<const Cx<C>*>(P.rtab) + blk * (long long)P.nR * 32 + lane;
 #define RT(l, m, m1) Rt[(roff(l) + ((m) + (l)) * (2 * (l) + 1) + ((m1) + (l))) * 32]
 
@@ -906,6 +909,7 @@ void oz_plan_finish(OzPlan& P) {
   // per SM; otherwise the warp-per-pair kernel (R computed on the fly).
   const size_t per_warp = lane_smem_per_warp<C>(P.np);
   P.lane_path = (P.mmax <= kLaneMaxMmax && per_warp <= 64 * 1024 && P.N < (1LL << 31)) ? 1 : 0;
+  throw_if(!P.lane_path && P.nbatch != 1, "batched plans need mmax <= 6 and the lane-per-pair OZ kernel", 4);
   if (P.lane_path) {
     P.warps_per_cta = lane_warps(per_warp, split_pairs<C>());
     P.smem = per_warp * P.warps_per_cta;
@@ -959,7 +963,8 @@ void launch_oz(const OzPlan& P, Cx<S>* p, cudaStream_t s) {
     const long long ngrp = (P.npairs + per_warp_pairs - 1) / per_warp_pairs;
     const long long nb = (ngrp + P.warps_per_cta - 1) / P.warps_per_cta;
     throw_if(nb > 0x7fffffffLL, "too many k-space pairs", 4);
-    const dim3 grid((unsigned)nb), block(32 * P.warps_per_cta);
+    throw_if(P.nbatch < 1 || P.nbatch > 65535, "batch must be 1..65535", 4);
+    const dim3 grid((unsigned)nb, (unsigned)P.nbatch), block(32 * P.warps_per_cta);
     switch (P.mmax) {
       case 1: lane_launch_one<S, C, 1>(P, p, grid, block, s); break;
       case 2: lane_launch_one<S, C, 2>(P, p, grid, block, s); break;
@@ -975,6 +980,7 @@ void launch_oz(const OzPlan& P, Cx<S>* p, cudaStream_t s) {
   if constexpr (std::is_same<S, DF>::value) {
     throw Error(4, "internal: packed storage needs the lane path");
   } else {
+    throw_if(P.nbatch != 1, "batched plans need mmax <= 6 and the lane-per-pair OZ kernel", 4);
     const long long nb = (P.npairs + P.warps_per_cta - 1) / P.warps_per_cta;
     oz_kernel<S><<<(unsigned)nb, 32 * P.warps_per_cta, P.smem, s>>>(P, p);
     launch_check("oz kernel launch");

@@ -316,3 +316,46 @@ def test_energy_cproj_pipeline_32cubed(gpu_lib, prec):
     ff = M.get_delta_f(xt, vexc, torch.from_numpy(w), df, rho0, pref)
     assert rel_err(_np(df), df_ref) < tol
     assert abs(ff - ff_ref) <= (1e-6 if prec == "f32" else 1e-12) * abs(ff_ref)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("n,box,mmax,mrso", [((12, 10, 8), (12., 10., 9.), 3, 2),
+                                             ((6, 7, 8), (9., 9., 9.), 2, 1),
+                                             ((8, 6, 10), (12., 9., 15.), 5, 2)])
+def test_batched_plans_equal_single_fields(gpu_lib, n, box, mmax, mrso, prec):
+    """A batched plan (B same-shape fields per call: o stored back to back, p
+    as (np, B, nx, ny, nz)) gives every field exactly what the single-field
+    plan gives it."""
+    import torch
+    M = gpu_lib
+    B = 3
+    o = O.Oracle(n, box, mmax, mrso)
+    dq = 0.01
+    idx, tab = I.synthetic_cq(mmax, mrso, o.nq_for_dq(dq) + 2, dq)
+    sg, ag = M.SpatialGrid(n, box), M.AngularGrid(mmax, mrso)
+    opt1 = M.OrientationProjectionTransform(sg, ag, precision=prec)
+    conv1 = M.Convolution.from_table(idx, tab, dq, sg, ag, precision=prec)
+    optb = M.OrientationProjectionTransform(sg, ag, precision=prec, batch=B)
+    convb = M.Convolution.from_table(idx, tab, dq, sg, ag, precision=prec, batch=B)
+    rd, cd = _dtypes(prec)
+    rng = np.random.default_rng(5)
+    fields = [_t(rng.uniform(-0.1, 0.1, (o.N, o.ntheta, o.nphi, o.npsi)), rd) for _ in range(B)]
+    singles_p, singles_v = [], []
+    for f in fields:
+        p = torch.zeros((o.np,) + tuple(n), dtype=cd, device="cuda")
+        v = torch.zeros_like(f)
+        opt1.angl2proj(f, p)
+        conv1.execute(p)
+        opt1.proj2angl(p, v)
+        singles_p.append(p)
+        singles_v.append(v)
+    ob = torch.cat(fields)
+    pb = torch.zeros((o.np, B) + tuple(n), dtype=cd, device="cuda")
+    vb = torch.zeros_like(ob)
+    optb.angl2proj(ob, pb)
+    convb.execute(pb)
+    optb.proj2angl(pb, vb)
+    torch.cuda.synchronize()
+    for b in range(B):
+        assert torch.equal(pb[:, b], singles_p[b])
+        assert torch.equal(vb[b * o.N:(b + 1) * o.N], singles_v[b])
