@@ -126,9 +126,8 @@ int mdft_conv_create(mdft_conv_t* out, mdft_grid_t g, const int* luc_index,
                      const double* luc, int np_luc, int nq, double dq,
                      int precision);
 /* Batched plan (see mdft_opt_create_batched): execute, fft and kspace act on
- * p (np, batch, nx, ny, nz), every field with the same c(q) table.  Needs the
- * lane-per-pair k-space kernel (mmax <= 6).  No counterpart in the
- * reference.  mdft_conv_create = batch 1. */
+ * p (np, batch, nx, ny, nz), every field with the same c(q) table.  No
+ * counterpart in the reference.  mdft_conv_create = batch 1. */
 int mdft_conv_create_batched(mdft_conv_t* out, mdft_grid_t g, const int* luc_index,
                              const double* luc, int np_luc, int nq, double dq,
                              int precision, int batch);

@@ -238,9 +238,10 @@ oz_kernel(const OzPlan P, Cx<T>* __restrict__ p) {
   }
 
   // ---- 2. load gamma(q), gamma(-q) ------------------------------------------
-  const long long N = P.N;
-  const long long lq = ((long long)ix * P.ny + iy) * P.nz + iz;
-  const long long lmq = ((long long)ixm * P.ny + iym) * P.nz + izm;
+  // projection stride; field blockIdx.y of a batched plan starts at y N
+  const long long N = P.pstride, f0 = (long long)blockIdx.y * P.N;
+  const long long lq = ((long long)ix * P.ny + iy) * P.nz + iz + f0;
+  const long long lmq = ((long long)ixm * P.ny + iym) * P.nz + izm + f0;
   for (int ip = lane; ip < np; ip += 32) {
     gq[ip] = p[(long long)ip * N + lq];
     gmq[ip] = p[(long long)ip * N + lmq];
@@ -909,7 +910,6 @@ void oz_plan_finish(OzPlan& P) {
   // per SM; otherwise the warp-per-pair kernel (R computed on the fly).
   const size_t per_warp = lane_smem_per_warp<C>(P.np);
   P.lane_path = (P.mmax <= kLaneMaxMmax && per_warp <= 64 * 1024 && P.N < (1LL << 31)) ? 1 : 0;
-  throw_if(!P.lane_path && P.nbatch != 1, "batched plans need mmax <= 6 and the lane-per-pair OZ kernel", 4);
   if (P.lane_path) {
     P.warps_per_cta = lane_warps(per_warp, split_pairs<C>());
     P.smem = per_warp * P.warps_per_cta;
@@ -980,9 +980,9 @@ void launch_oz(const OzPlan& P, Cx<S>* p, cudaStream_t s) {
   if constexpr (std::is_same<S, DF>::value) {
     throw Error(4, "internal: packed storage needs the lane path");
   } else {
-    throw_if(P.nbatch != 1, "batched plans need mmax <= 6 and the lane-per-pair OZ kernel", 4);
     const long long nb = (P.npairs + P.warps_per_cta - 1) / P.warps_per_cta;
-    oz_kernel<S><<<(unsigned)nb, 32 * P.warps_per_cta, P.smem, s>>>(P, p);
+    throw_if(P.nbatch < 1 || P.nbatch > 65535, "batch must be 1..65535", 4);
+    oz_kernel<S><<<dim3((unsigned)nb, (unsigned)P.nbatch), 32 * P.warps_per_cta, P.smem, s>>>(P, p);
     launch_check("oz kernel launch");
   }
 }
