@@ -195,6 +195,44 @@ int mdft_get_delta_f_noalloc(const void* xi, const void* vexc, const double* w,
                              double rho0, double prefactor, int precision,
                              void* stream);
 
+/* ---- job server -----------------------------------------------------------
+ * No counterpart in the reference (which evaluates one field per call).  A
+ * server takes jobs from any host thread and runs them on the device that was
+ * current at create, on its own worker thread:
+ *   - a job is one field xi (nx*ny*nz, ntheta, nphi, npsi) on one grid with
+ *     one registered solvent; each of its n_steps steps evaluates the cproj
+ *     excess energy and gradient at xi (get_delta_rho, angl2proj,
+ *     Convolution::execute, proj2angl, get_delta_f: src/mini-mdft.hpp:137-183)
+ *     and moves xi by -step * gradient;
+ *   - jobs with the same solvent and grid advance together with batched
+ *     launches (up to max_batch per group), replayed from CUDA graphs;
+ *   - groups are created only within hbm_budget_bytes of device memory
+ *     (0: 80 % of the free memory at create); jobs wait until theirs fits.
+ * Fields are host arrays in the server's precision (double for MDFT_F64 and
+ * MDFT_F64_DF, float for MDFT_F32). */
+typedef struct mdft_server_s* mdft_server_t;
+int mdft_server_create(mdft_server_t* out, int precision, int max_batch, size_t hbm_budget_bytes);
+/* Fails every unfinished job, waits for the worker, frees the device memory. */
+int mdft_server_destroy(mdft_server_t s);
+/* A solvent: its angular grid (mmax <= 6), c(q) table as for
+ * mdft_conv_create, bulk density rho0 and the energy prefactor of
+ * get_delta_f. */
+int mdft_server_add_solvent(mdft_server_t s, int mmax, int mrso, const int* luc_index,
+                            const double* luc, int np_luc, int nq, double dq,
+                            double rho0, double prefactor, int* solvent_id);
+/* Queues a job (xi0 is copied; n_steps <= 4096) and returns at once. */
+int mdft_server_submit(mdft_server_t s, int solvent_id, int nx, int ny, int nz, double lx,
+                       double ly, double lz, const void* xi0, int n_steps, double step,
+                       long long* job_id);
+/* Blocks until the job is done, then hands over its final xi (host, may be
+ * NULL), the energy of every step (n_steps doubles, may be NULL) and its
+ * latency from submit (seconds, may be NULL).  Each job is waited for once. */
+int mdft_server_wait(mdft_server_t s, long long job_id, void* xi_out, double* ff_out,
+                     double* latency_s);
+/* out[0..5]: jobs done, jobs done per second since the first submit, p50 and
+ * p99 latency (s), job groups held, peak device bytes of the groups. */
+int mdft_server_stats(mdft_server_t s, double* out);
+
 #ifdef __cplusplus
 }
 #endif

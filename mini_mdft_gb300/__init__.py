@@ -12,6 +12,7 @@ from .api import (  # noqa: F401
     MdftError,
     OrientationProjectionMap,
     OrientationProjectionTransform,
+    Server,
     SpatialGrid,
     get_delta_f,
     get_delta_rho,

@@ -354,3 +354,79 @@ def get_delta_f(xi, vexc, w, delta_f, rho0, prefactor, ff_out=None):
     if ff_out is not None:
         return ff_out
     return float(ff.item())
+
+
+class Server:
+    """Job server (mdft_server_*; no counterpart in the reference).
+
+    Jobs (one field xi on one grid with one registered solvent) run n_steps
+    steps of the cproj excess energy and gradient followed by
+    xi <- xi - step * gradient; same-shape jobs advance together in batched,
+    graph-replayed steps on the server's worker thread.  Fields are numpy
+    arrays of the server's precision (float64 for "f64"/"f64df", float32 for
+    "f32")."""
+
+    def __init__(self, precision="f64df", max_batch=8, hbm_budget_bytes=0):
+        self.precision = _precision_arg(precision)
+        self._dt = np.float32 if self.precision == MDFT_F32 else np.float64
+        h = C.c_void_p()
+        check(lib().mdft_server_create(C.byref(h), self.precision, int(max_batch),
+                                       int(hbm_budget_bytes)))
+        self.h = h
+        self._solvents = {}
+        self._jobs = {}
+
+    def close(self):
+        if getattr(self, "h", None) and _lib._lib is not None:
+            _lib._lib.mdft_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def add_solvent(self, mmax, mrso, luc_index, table, dq, rho0, prefactor):
+        idx = np.ascontiguousarray(luc_index, np.int32)
+        tab = np.ascontiguousarray(table, np.complex128)
+        np_luc, nq = tab.shape
+        sid = C.c_int()
+        check(lib().mdft_server_add_solvent(self.h, int(mmax), int(mrso), _np_i(idx),
+                                            tab.ctypes.data_as(C.POINTER(C.c_double)), np_luc, nq,
+                                            float(dq), float(rho0), float(prefactor), C.byref(sid)))
+        ntheta, nphi, npsi = mmax + 1, 2 * mmax + 1, 2 * (mmax // mrso) + 1
+        self._solvents[sid.value] = (ntheta, nphi, npsi)
+        return sid.value
+
+    def submit(self, solvent, n_nodes, length, xi0, n_steps, step):
+        """Queues a job and returns its id at once."""
+        nx, ny, nz = (int(v) for v in n_nodes)
+        ntheta, nphi, npsi = self._solvents[solvent]
+        x = np.ascontiguousarray(xi0, self._dt)
+        if x.size != nx * ny * nz * ntheta * nphi * npsi:
+            raise ValueError("xi0 has %d values, the job needs %d"
+                             % (x.size, nx * ny * nz * ntheta * nphi * npsi))
+        jid = C.c_longlong()
+        check(lib().mdft_server_submit(self.h, int(solvent), nx, ny, nz, *(float(v) for v in length),
+                                       x.ctypes.data_as(C.c_void_p), int(n_steps), float(step),
+                                       C.byref(jid)))
+        self._jobs[jid.value] = (x.shape, int(n_steps))
+        return jid.value
+
+    def wait(self, job):
+        """(final xi, energies of every step, latency in s) of a job."""
+        shape, n_steps = self._jobs.pop(job, (None, 0))
+        lat = C.c_double()
+        if shape is None:  # not submitted here, or already waited for: the server says which
+            check(lib().mdft_server_wait(self.h, C.c_longlong(job), None, None, C.byref(lat)))
+            return None, None, lat.value
+        xi = np.empty(shape, self._dt)
+        ff = np.empty(n_steps, np.float64)
+        check(lib().mdft_server_wait(self.h, C.c_longlong(job), xi.ctypes.data_as(C.c_void_p),
+                                     ff.ctypes.data_as(C.POINTER(C.c_double)), C.byref(lat)))
+        return xi, ff, lat.value
+
+    def stats(self):
+        """dict: done, solves_per_s, p50_s, p99_s, groups, peak_bytes."""
+        out = np.zeros(6, np.float64)
+        check(lib().mdft_server_stats(self.h, out.ctypes.data_as(C.POINTER(C.c_double))))
+        keys = ("done", "solves_per_s", "p50_s", "p99_s", "groups", "peak_bytes")
+        return dict(zip(keys, out.tolist()))

@@ -16,6 +16,7 @@
 
 #include "../../include/mdft_gb300.h"
 #include "common.cuh"
+#include "handles.hpp"
 
 using mdft::Cx;
 using mdft::DevBuf;
@@ -99,40 +100,6 @@ int mdft::record_error(int code, const std::string& msg) {
   g_last_error = msg;
   return code;
 }
-
-struct mdft_grid_s {
-  mdft::Grid g;
-  explicit mdft_grid_s(const mdft::Grid& gg) : g(gg) {}
-};
-
-struct mdft_opt_s {
-  mdft::Grid g;
-  int prec;
-  int device;
-  int batch = 1;  // same-shape fields per call, stored back to back
-  DevBuf coef_a2p, coef_p2a, tw_phi, tw_psi, ip_m, ip_mup, ip_mu2, pmap;
-  mdft::AngPlan plan{};
-  explicit mdft_opt_s(const mdft::Grid& gg) : g(gg) {}
-};
-
-struct mdft_conv_s {
-  mdft::Grid g;
-  int prec;
-  int device;
-  int batch = 1;  // same-shape fields per call, p laid out (np, batch, nx, ny, nz)
-  int npairs = 0, nq = 0;
-  double dq = 0;
-  std::vector<int> pair_list;                 // reference order (getter)
-  std::vector<std::complex<double>> mnq;      // (np_new, nq) (getter)
-  DevBuf pairs, kx, ky, kz, rot, pmap, ip_m, ip_mup, ip_mu2, ia_map, ctab, tw_x, tw_y, tw_z;
-  DevBuf pinfo, palpha, ia_start, rtab, ceff;  // lane-per-pair OZ path
-  // double-float form: the projections stay packed DF pairs between the
-  // passes of execute() (needs the lane OZ path and one axis longer than 1)
-  bool df_packed = false;
-  mdft::OzPlan oz{};
-  mdft::FftAxis ax{}, ay{}, az{};
-  explicit mdft_conv_s(const mdft::Grid& gg) : g(gg) {}
-};
 
 namespace {
 
@@ -378,18 +345,36 @@ void conv_build(mdft_conv_s* h, const mdft::LucTable& t) {
 // backward).  In the double-float form the passes of one chain keep the data
 // as packed DF pairs: the first pass converts from `in_packed` storage, the
 // last converts to `out_packed` storage.
+// The launch descriptors of a convolution plan restricted to its first k
+// fields: the FFT passes cover k of the batch's transforms and the k-space
+// kernel k fields, with p laid out (np, k, N).
+struct ConvLaunch {
+  mdft::FftAxis ax, ay, az;
+  mdft::OzPlan oz;
+};
+ConvLaunch conv_launch(const mdft_conv_s* h, int k) {
+  throw_if(k < 1 || k > h->batch, "active fields must be 1.." + std::to_string(h->batch));
+  ConvLaunch L{h->ax, h->ay, h->az, h->oz};
+  if (k != h->batch) {
+    for (mdft::FftAxis* a : {&L.ax, &L.ay, &L.az}) a->ncols = a->ncols / h->batch * k;
+    L.oz.nbatch = k;
+    L.oz.pstride = h->oz.N * k;
+  }
+  return L;
+}
+
 template <typename S, typename T>
-void conv_fft(mdft_conv_s* h, void* p, int sign, cudaStream_t s, bool in_packed = false,
+void conv_fft(ConvLaunch& L, void* p, int sign, cudaStream_t s, bool in_packed = false,
               bool out_packed = false) {
   mdft::FftAxis* order[3];
   if (sign < 0) {
-    order[0] = &h->az;
-    order[1] = &h->ay;
-    order[2] = &h->ax;
+    order[0] = &L.az;
+    order[1] = &L.ay;
+    order[2] = &L.ax;
   } else {
-    order[0] = &h->ax;
-    order[1] = &h->ay;
-    order[2] = &h->az;
+    order[0] = &L.ax;
+    order[1] = &L.ay;
+    order[2] = &L.az;
   }
   if constexpr (std::is_same<T, mdft::DF>::value) {
     mdft::FftAxis* live[3];
@@ -628,7 +613,8 @@ int mdft_conv_fft(mdft_conv_t h, void* p, int sign, void* stream) {
     throw_if(sign != -1 && sign != 1, "sign must be -1 or +1");
     check_device(h->device);
     with_types(h->prec, [&](auto st, auto ct) {
-      conv_fft<decltype(st), decltype(ct)>(h, p, sign, as_stream(stream));
+      ConvLaunch L = conv_launch(h, h->batch);
+      conv_fft<decltype(st), decltype(ct)>(L, p, sign, as_stream(stream));
     });
   });
 }
@@ -647,31 +633,32 @@ int mdft_conv_kspace(mdft_conv_t h, void* p, void* stream) {
 namespace {
 // execute(): forward FFT, k-space step, inverse FFT.  ev (optional) receives
 // an event record before the forward FFT and after each of the three stages.
-void conv_execute(mdft_conv_s* h, void* p, cudaStream_t s, cudaEvent_t const* ev) {
+void conv_execute(mdft_conv_s* h, void* p, cudaStream_t s, cudaEvent_t const* ev, int k = 0) {
   auto mark = [&](int i) {
     if (ev) mdft::cuda_check(cudaEventRecord(ev[i], s), "stage event record");
   };
+  ConvLaunch L = conv_launch(h, k > 0 ? k : h->batch);
   with_types(h->prec, [&](auto st, auto ct) {
     using S = decltype(st);
     using C = decltype(ct);
     if constexpr (std::is_same<C, mdft::DF>::value) {
       if (h->df_packed) {
         mark(0);
-        conv_fft<S, C>(h, p, -1, s, false, true);
+        conv_fft<S, C>(L, p, -1, s, false, true);
         mark(1);
-        mdft::launch_oz<mdft::DF, C>(h->oz, static_cast<Cx<mdft::DF>*>(p), s);
+        mdft::launch_oz<mdft::DF, C>(L.oz, static_cast<Cx<mdft::DF>*>(p), s);
         mark(2);
-        conv_fft<S, C>(h, p, +1, s, true, false);
+        conv_fft<S, C>(L, p, +1, s, true, false);
         mark(3);
         return;
       }
     }
     mark(0);
-    conv_fft<S, C>(h, p, -1, s);
+    conv_fft<S, C>(L, p, -1, s);
     mark(1);
-    mdft::launch_oz<S, C>(h->oz, static_cast<Cx<S>*>(p), s);
+    mdft::launch_oz<S, C>(L.oz, static_cast<Cx<S>*>(p), s);
     mark(2);
-    conv_fft<S, C>(h, p, +1, s);
+    conv_fft<S, C>(L, p, +1, s);
     mark(3);
   });
 }
@@ -757,3 +744,35 @@ int mdft_get_delta_f(const void* xi, const void* vexc, const double* w, void* de
 }
 
 }  // extern "C"
+
+// ---- stages on the first k fields of a batched plan (the job server) -------
+namespace mdft {
+namespace detail {
+
+void angl2proj_fields(mdft_opt_s* h, const void* o, bool from_xi, double rho0, void* p, int k,
+                      cudaStream_t s) {
+  throw_if(k < 1 || k > h->batch, "active fields must be 1.." + std::to_string(h->batch));
+  AngPlan P = h->plan;
+  P.N = h->g.N() * k;
+  with_types(h->prec, [&](auto st, auto ct) {
+    using S = decltype(st);
+    launch_angl2proj<S, decltype(ct)>(P, static_cast<const S*>(o), static_cast<Cx<S>*>(p), from_xi, rho0, s);
+  });
+}
+
+void proj2angl_fields(mdft_opt_s* h, const void* p, void* o, int k, cudaStream_t s) {
+  throw_if(k < 1 || k > h->batch, "active fields must be 1.." + std::to_string(h->batch));
+  AngPlan P = h->plan;
+  P.N = h->g.N() * k;
+  with_types(h->prec, [&](auto st, auto ct) {
+    using S = decltype(st);
+    launch_proj2angl<S, decltype(ct)>(P, static_cast<const Cx<S>*>(p), static_cast<S*>(o), s);
+  });
+}
+
+void execute_fields(mdft_conv_s* h, void* p, int k, cudaStream_t s) { conv_execute(h, p, s, nullptr, k); }
+
+int current_device() { return ::current_device(); }
+
+}  // namespace detail
+}  // namespace mdft

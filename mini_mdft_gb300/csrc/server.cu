@@ -1,0 +1,641 @@
+// server.cu -- a job server for the excess-functional path.
+//
+// Jobs arrive from any host thread (mdft_server_submit) and are run by one
+// worker thread that owns the GPU work:
+//   * a job is one field on one grid with one solvent; each of its steps
+//     evaluates the cproj excess energy and gradient at xi (get_delta_rho
+//     fused into angl2proj, Convolution::execute, proj2angl, get_delta_f,
+//     the stage sequence of Solver::energy_cproj_mrso,
+//     src/mini-mdft.hpp:137-183) and then moves xi a fixed step down the
+//     gradient; the job returns the energy of every step and its final xi;
+//   * jobs with the same solvent and grid share a group: plans built once for
+//     `max_batch` fields and a resident arena holding every field's xi, so
+//     the group advances all its active jobs (compacted into the first k
+//     slots) with one set of batched launches per step;
+//   * each group step is replayed from a CUDA graph captured for its active
+//     count k (the first step at a given k runs directly, which also checks
+//     the launches, and a failed capture falls back to direct launches);
+//   * a group is created only while the device memory of all groups stays
+//     within the server's budget; groups without jobs are released, least
+//     recently used first, when a new one does not fit;
+//   * the server records every job's latency (submit to result) for p50/p99.
+// No counterpart in the reference, which evaluates one field at a time.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <tuple>
+#include <vector>
+
+#include "handles.hpp"
+
+using mdft::Error;
+using mdft::throw_if;
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+template <typename T>
+__global__ void descent_kernel(T* __restrict__ xi, const T* __restrict__ df, const double* __restrict__ alpha,
+                               long long per_field, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int f = (int)(i / per_field);
+    xi[i] = xi[i] - (T)alpha[f] * df[i];
+  }
+}
+
+// trace[j][step_j] = energy of slot j, step_j advanced (j < k)
+__global__ void trace_kernel(const double* __restrict__ ff_cur, double* __restrict__ trace,
+                             int* __restrict__ step_ctr, int k, int cap) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= k) return;
+  const int s = step_ctr[j];
+  if (s < cap) trace[(long long)j * cap + s] = ff_cur[j];
+  step_ctr[j] = s + 1;
+}
+
+void ck(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw Error(e == cudaErrorMemoryAllocation ? MDFT_ERR_NOMEM : MDFT_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+  }
+}
+void ckr(int rc, const char* what) {
+  if (rc != MDFT_OK) throw Error(rc, std::string(what) + ": " + mdft_last_error());
+}
+
+struct Solvent {
+  int mmax, mrso, np_luc, nq;
+  double dq, rho0, prefactor;
+  std::vector<int> luc_index;
+  std::vector<double> luc;
+};
+
+struct Job {
+  long long id = 0;
+  int solvent = 0;
+  int n[3] = {0, 0, 0};
+  double len[3] = {0, 0, 0};
+  std::vector<unsigned char> xi;  // initial field on submit, final field when done
+  std::vector<double> ff;         // energy of every step
+  int n_steps = 0;
+  double step = 0;
+  int state = 0;  // 0 queued, 1 running, 2 done, -1 failed
+  int code = 0;
+  std::string error;
+  Clock::time_point t_submit, t_done;
+  int slot = -1, steps_done = 0;
+};
+
+using Key = std::tuple<int, int, int, int, double, double, double>;
+
+struct DevPtr {
+  void* p = nullptr;
+  ~DevPtr() {
+    if (p) cudaFree(p);
+  }
+  void alloc(size_t bytes, const char* what) { ck(cudaMalloc(&p, bytes ? bytes : 1), what); }
+  template <typename T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+struct Group {
+  Key key;
+  int B = 1, k = 0, prec = MDFT_F64, cap = 0;
+  long long N = 0;
+  int no = 0, np = 0;
+  size_t elem = 8, bytes = 0;
+  double rho0 = 0, prefactor = 0;
+  mdft_grid_t grid = nullptr;
+  mdft_opt_t opt = nullptr;
+  mdft_conv_t conv = nullptr;
+  DevPtr xi, vexc, df, p, w, ff_cur, trace, step_ctr, alpha, scratch;
+  size_t scratch_per_slot = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<std::shared_ptr<Job>> slots;  // active jobs, slot i = field i
+  std::map<int, cudaGraphExec_t> graphs;    // per active count; null: run directly
+  std::map<int, int> seen;                  // steps run directly at each active count
+  Clock::time_point last_used;
+  ~Group() {
+    for (auto& g : graphs)
+      if (g.second) cudaGraphExecDestroy(g.second);
+    if (stream) cudaStreamDestroy(stream);
+    if (conv) mdft_conv_destroy(conv);
+    if (opt) mdft_opt_destroy(opt);
+    if (grid) mdft_grid_destroy(grid);
+  }
+};
+
+}  // namespace
+
+struct mdft_server_s {
+  int device = 0, prec = MDFT_F64, max_batch = 1, trace_cap = 4096;
+  size_t budget = 0, in_use = 0;  // in_use: worker only
+  std::atomic<size_t> peak{0};
+  std::atomic<int> n_groups{0};
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<std::shared_ptr<Job>> incoming;
+  std::map<long long, std::shared_ptr<Job>> jobs;
+  std::vector<Solvent> solvents;
+  long long next_id = 1;
+  bool stop = false;
+  std::thread worker;
+  // statistics (under mu)
+  std::vector<double> latencies;
+  bool any_submit = false;
+  Clock::time_point t_first_submit, t_last_done;
+  // worker-only state
+  std::vector<std::shared_ptr<Job>> pending;
+  std::map<Key, std::unique_ptr<Group>> groups;
+
+  void run();
+  void admit();
+  Group* group_for(const Job& j);
+  void step(Group& g);
+  void enqueue_step(Group& g, int k);
+  void finish(Group& g, int slot);
+  void fail_group(Group& g, const std::string& msg, int code);
+  void fail_job(const std::shared_ptr<Job>& j, const std::string& msg, int code);
+};
+
+namespace {
+
+size_t field_bytes(const Group& g) { return (size_t)g.N * g.no * g.elem; }
+
+}  // namespace
+
+void mdft_server_s::fail_job(const std::shared_ptr<Job>& j, const std::string& msg, int code) {
+  std::lock_guard<std::mutex> lk(mu);
+  j->state = -1;
+  j->code = code ? code : MDFT_ERR_INVALID;
+  j->error = msg;
+  j->t_done = Clock::now();
+  cv_done.notify_all();
+}
+
+void mdft_server_s::fail_group(Group& g, const std::string& msg, int code) {
+  for (auto& j : g.slots) fail_job(j, msg, code);
+  g.slots.clear();
+  g.k = 0;
+}
+
+Group* mdft_server_s::group_for(const Job& j) {
+  const Key key{j.solvent, j.n[0], j.n[1], j.n[2], j.len[0], j.len[1], j.len[2]};
+  auto it = groups.find(key);
+  if (it != groups.end()) return it->second.get();
+  Solvent sv;
+  {
+    std::lock_guard<std::mutex> lk(mu);  // add_solvent may grow the list meanwhile
+    sv = solvents[j.solvent];
+  }
+  // footprint: plans (measured) + arena (computed); admit only within budget
+  auto g = std::make_unique<Group>();
+  g->key = key;
+  g->B = max_batch;
+  g->prec = prec;
+  g->cap = trace_cap;
+  g->elem = prec == MDFT_F32 ? 4 : 8;
+  g->rho0 = sv.rho0;
+  g->prefactor = sv.prefactor;
+  ckr(mdft_grid_create(&g->grid, j.n[0], j.n[1], j.n[2], j.len[0], j.len[1], j.len[2], sv.mmax, sv.mrso),
+      "job grid");
+  int info[11];
+  ckr(mdft_grid_info(g->grid, info), "grid info");
+  g->N = (long long)j.n[0] * j.n[1] * j.n[2];
+  g->no = info[8];
+  g->np = info[9];
+  const size_t fb = field_bytes(*g);
+  const size_t nbp = mdft::delta_f_partials((size_t)g->N, g->no);
+  g->scratch_per_slot = (sizeof(double2) * nbp + 256 + 255) / 256 * 256;
+  const size_t arena = 3 * fb * g->B + (size_t)g->np * g->N * 2 * g->elem * g->B +
+                       g->scratch_per_slot * g->B + (size_t)g->B * (g->cap + 3) * 8 + 8 * g->no;
+  // a rough bound on the plans before building them: the R(q) table and
+  // pair data dominate (about 1 KB per grid point at mmax <= 6)
+  const size_t plan_guess = (size_t)g->N * 1024;
+  if (in_use + arena + plan_guess > budget) {
+    // release idle groups, least recently used first
+    std::vector<std::pair<Clock::time_point, Key>> idle;
+    for (auto& kv : groups)
+      if (kv.second->k == 0) idle.push_back({kv.second->last_used, kv.first});
+    std::sort(idle.begin(), idle.end());
+    for (auto& e : idle) {
+      if (in_use + arena + plan_guess <= budget) break;
+      in_use -= groups[e.second]->bytes;
+      groups.erase(e.second);
+      n_groups.store((int)groups.size());
+    }
+    if (in_use + arena + plan_guess > budget) {
+      bool busy = false;
+      for (auto& kv : groups) busy = busy || kv.second->k > 0;
+      if (!busy)
+        throw Error(MDFT_ERR_NOMEM, "job needs about " + std::to_string((arena + plan_guess) >> 20) +
+                                        " MiB of device memory, over the server's budget of " +
+                                        std::to_string(budget >> 20) + " MiB");
+      return nullptr;  // wait for running groups to finish
+    }
+  }
+  size_t free0 = 0, free1 = 0, total = 0;
+  ck(cudaMemGetInfo(&free0, &total), "cudaMemGetInfo");
+  ckr(mdft_opt_create_batched(&g->opt, g->grid, prec, g->B), "job plan (angular)");
+  ckr(mdft_conv_create_batched(&g->conv, g->grid, sv.luc_index.data(), sv.luc.data(), sv.np_luc, sv.nq, sv.dq,
+                               prec, g->B),
+      "job plan (convolution)");
+  g->xi.alloc(fb * g->B, "server arena");
+  g->vexc.alloc(fb * g->B, "server arena");
+  g->df.alloc(fb * g->B, "server arena");
+  g->p.alloc((size_t)g->np * g->N * 2 * g->elem * g->B, "server arena");
+  g->scratch.alloc(g->scratch_per_slot * g->B, "server arena");
+  g->trace.alloc((size_t)g->B * g->cap * 8, "server arena");
+  g->ff_cur.alloc((size_t)g->B * 8, "server arena");
+  g->alpha.alloc((size_t)g->B * 8, "server arena");
+  g->step_ctr.alloc((size_t)g->B * 4, "server arena");
+  g->w.alloc((size_t)g->no * 8, "server arena");
+  std::vector<double> th(info[5]), wth(info[5]), w(g->no);
+  ckr(mdft_grid_angular(g->grid, th.data(), wth.data(), w.data()), "angular weights");
+  ck(cudaMemcpy(g->w.p, w.data(), 8 * g->no, cudaMemcpyHostToDevice), "weights upload");
+  ck(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  ck(cudaMemGetInfo(&free1, &total), "cudaMemGetInfo");
+  g->bytes = free0 > free1 ? free0 - free1 : arena;
+  in_use += g->bytes;
+  if (in_use > peak.load()) peak.store(in_use);
+  Group* raw = g.get();
+  groups.emplace(key, std::move(g));
+  n_groups.store((int)groups.size());
+  return raw;
+}
+
+void mdft_server_s::admit() {
+  std::vector<std::shared_ptr<Job>> keep;
+  for (auto& j : pending) {
+    Group* g = nullptr;
+    try {
+      g = group_for(*j);
+    } catch (const Error& e) {
+      fail_job(j, e.what(), e.code);
+      continue;
+    }
+    if (!g || g->k >= g->B) {
+      keep.push_back(j);
+      continue;
+    }
+    const int slot = g->k;
+    try {
+      const size_t fb = field_bytes(*g);
+      ck(cudaMemcpyAsync(g->xi.as<unsigned char>() + fb * slot, j->xi.data(), fb, cudaMemcpyHostToDevice,
+                         g->stream),
+         "job field upload");
+      ck(cudaMemcpyAsync(g->alpha.as<double>() + slot, &j->step, 8, cudaMemcpyHostToDevice, g->stream),
+         "job step upload");
+      ck(cudaMemsetAsync(g->step_ctr.as<int>() + slot, 0, 4, g->stream), "job counter reset");
+      ck(cudaStreamSynchronize(g->stream), "job admission");
+    } catch (const Error& e) {
+      fail_job(j, e.what(), e.code);
+      continue;
+    }
+    j->slot = slot;
+    j->steps_done = 0;
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      j->state = 1;
+    }
+    g->slots.push_back(j);
+    g->k += 1;
+    g->last_used = Clock::now();
+  }
+  pending.swap(keep);
+}
+
+void mdft_server_s::enqueue_step(Group& g, int k) {
+  cudaStream_t s = g.stream;
+  mdft::detail::angl2proj_fields(g.opt, g.xi.p, true, g.rho0, g.p.p, k, s);
+  mdft::detail::execute_fields(g.conv, g.p.p, k, s);
+  mdft::detail::proj2angl_fields(g.opt, g.p.p, g.vexc.p, k, s);
+  // the energy reduction's completion counters start at zero
+  ck(cudaMemsetAsync(g.scratch.p, 0, g.scratch_per_slot * k, s), "energy scratch reset");
+  const size_t fb = field_bytes(g);
+  for (int j = 0; j < k; ++j) {
+    unsigned char* sc = g.scratch.as<unsigned char>() + g.scratch_per_slot * j;
+    if (g.elem == 8)
+      mdft::launch_delta_f<double>(
+          reinterpret_cast<const double*>(g.xi.as<unsigned char>() + fb * j),
+          reinterpret_cast<const double*>(g.vexc.as<unsigned char>() + fb * j), g.w.as<double>(),
+          reinterpret_cast<double*>(g.df.as<unsigned char>() + fb * j), g.ff_cur.as<double>() + j, (size_t)g.N,
+          g.no, g.rho0, g.prefactor, sc, s);
+    else
+      mdft::launch_delta_f<float>(
+          reinterpret_cast<const float*>(g.xi.as<unsigned char>() + fb * j),
+          reinterpret_cast<const float*>(g.vexc.as<unsigned char>() + fb * j), g.w.as<double>(),
+          reinterpret_cast<float*>(g.df.as<unsigned char>() + fb * j), g.ff_cur.as<double>() + j, (size_t)g.N,
+          g.no, g.rho0, g.prefactor, sc, s);
+  }
+  trace_kernel<<<(k + 127) / 128, 128, 0, s>>>(g.ff_cur.as<double>(), g.trace.as<double>(), g.step_ctr.as<int>(), k,
+                                                g.cap);
+  mdft::launch_check("server trace kernel launch");
+  const long long per_field = g.N * g.no, n = per_field * k;
+  const unsigned nb = (unsigned)std::min<long long>((n + 255) / 256, 152LL * 16);
+  if (g.elem == 8)
+    descent_kernel<double><<<nb, 256, 0, s>>>(g.xi.as<double>(), g.df.as<double>(), g.alpha.as<double>(),
+                                              per_field, n);
+  else
+    descent_kernel<float><<<nb, 256, 0, s>>>(g.xi.as<float>(), g.df.as<float>(), g.alpha.as<double>(), per_field,
+                                             n);
+  mdft::launch_check("server descent kernel launch");
+}
+
+void mdft_server_s::step(Group& g) {
+  const int k = g.k;
+  auto it = g.graphs.find(k);
+  if (it != g.graphs.end() && it->second) {
+    ck(cudaGraphLaunch(it->second, g.stream), "cudaGraphLaunch");
+    return;
+  }
+  if (it == g.graphs.end() && g.seen[k] >= 1) {
+    // capture this active count once; on any failure run it directly from now on
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool ok = cudaStreamBeginCapture(g.stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+      try {
+        enqueue_step(g, k);
+      } catch (const Error&) {
+        ok = false;
+      }
+      ok = (cudaStreamEndCapture(g.stream, &graph) == cudaSuccess) && ok && graph;
+      ok = ok && cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+      if (graph) cudaGraphDestroy(graph);
+    }
+    cudaGetLastError();
+    g.graphs[k] = ok ? exec : nullptr;
+    if (ok) {
+      ck(cudaGraphLaunch(exec, g.stream), "cudaGraphLaunch");
+      return;
+    }
+  }
+  g.seen[k] += 1;
+  enqueue_step(g, k);
+}
+
+void mdft_server_s::finish(Group& g, int slot) {
+  std::shared_ptr<Job> j = g.slots[slot];
+  const size_t fb = field_bytes(g);
+  std::vector<unsigned char> xi(fb);
+  std::vector<double> ff(j->n_steps);
+  ck(cudaMemcpyAsync(xi.data(), g.xi.as<unsigned char>() + fb * slot, fb, cudaMemcpyDeviceToHost, g.stream),
+     "job field download");
+  ck(cudaMemcpyAsync(ff.data(), g.trace.as<double>() + (size_t)slot * g.cap, 8 * (size_t)j->n_steps,
+                     cudaMemcpyDeviceToHost, g.stream),
+     "job energies download");
+  // keep the active slots compact: the last one moves into the freed slot
+  const int last = g.k - 1;
+  if (slot != last) {
+    ck(cudaMemcpyAsync(g.xi.as<unsigned char>() + fb * slot, g.xi.as<unsigned char>() + fb * last, fb,
+                       cudaMemcpyDeviceToDevice, g.stream),
+       "slot move");
+    ck(cudaMemcpyAsync(g.trace.as<double>() + (size_t)slot * g.cap, g.trace.as<double>() + (size_t)last * g.cap,
+                       8 * (size_t)g.cap, cudaMemcpyDeviceToDevice, g.stream),
+       "slot move");
+    ck(cudaMemcpyAsync(g.alpha.as<double>() + slot, g.alpha.as<double>() + last, 8, cudaMemcpyDeviceToDevice,
+                       g.stream),
+       "slot move");
+    ck(cudaMemcpyAsync(g.step_ctr.as<int>() + slot, g.step_ctr.as<int>() + last, 4, cudaMemcpyDeviceToDevice,
+                       g.stream),
+       "slot move");
+    g.slots[slot] = g.slots[last];
+    g.slots[slot]->slot = slot;
+  }
+  ck(cudaStreamSynchronize(g.stream), "job completion");
+  g.slots.pop_back();
+  g.k -= 1;
+  g.last_used = Clock::now();
+  std::lock_guard<std::mutex> lk(mu);
+  j->xi.swap(xi);
+  j->ff.swap(ff);
+  j->state = 2;
+  j->t_done = Clock::now();
+  latencies.push_back(std::chrono::duration<double>(j->t_done - j->t_submit).count());
+  t_last_done = j->t_done;
+  cv_done.notify_all();
+}
+
+void mdft_server_s::run() {
+  cudaSetDevice(device);
+  for (;;) {
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      auto busy = [&] {
+        for (auto& kv : groups)
+          if (kv.second->k > 0) return true;
+        return false;
+      };
+      cv_work.wait(lk, [&] { return stop || !incoming.empty() || busy() || !pending.empty(); });
+      if (stop) return;
+      while (!incoming.empty()) {
+        pending.push_back(incoming.front());
+        incoming.pop_front();
+      }
+    }
+    admit();
+    std::vector<Group*> live;
+    for (auto& kv : groups)
+      if (kv.second->k > 0) live.push_back(kv.second.get());
+    if (live.empty()) {
+      // queued jobs that cannot be placed yet and nothing running: wait for news
+      std::unique_lock<std::mutex> lk(mu);
+      cv_work.wait_for(lk, std::chrono::milliseconds(2), [&] { return stop || !incoming.empty(); });
+      continue;
+    }
+    for (Group* g : live) {
+      try {
+        step(*g);
+      } catch (const Error& e) {
+        fail_group(*g, e.what(), e.code);
+      }
+    }
+    for (Group* g : live) {
+      if (g->k == 0) continue;
+      try {
+        ck(cudaStreamSynchronize(g->stream), "server step");
+        for (auto& j : g->slots) j->steps_done += 1;
+        for (int s = g->k - 1; s >= 0; --s)
+          if (g->slots[s]->steps_done >= g->slots[s]->n_steps) finish(*g, s);
+      } catch (const Error& e) {
+        fail_group(*g, e.what(), e.code);
+      }
+    }
+  }
+}
+
+// ---- C ABI --------------------------------------------------------------------
+namespace {
+template <typename F>
+int sguard(F&& f) {
+  try {
+    f();
+    return MDFT_OK;
+  } catch (const Error& e) {
+    return mdft::record_error(e.code, e.what());
+  } catch (const std::bad_alloc&) {
+    return mdft::record_error(MDFT_ERR_NOMEM, "host allocation failed");
+  } catch (const std::exception& e) {
+    return mdft::record_error(MDFT_ERR_INVALID, e.what());
+  }
+}
+}  // namespace
+
+int mdft_server_create(mdft_server_t* out, int precision, int max_batch, size_t hbm_budget_bytes) {
+  return sguard([&] {
+    throw_if(!out, "NULL argument");
+    *out = nullptr;
+    throw_if(precision != MDFT_F64 && precision != MDFT_F32 && precision != MDFT_F64_DF,
+             "precision must be MDFT_F64, MDFT_F32 or MDFT_F64_DF");
+    throw_if(max_batch < 1 || max_batch > 1024, "max_batch must be 1..1024");
+    auto s = std::make_unique<mdft_server_s>();
+    s->device = mdft::detail::current_device();
+    s->prec = precision;
+    s->max_batch = max_batch;
+    size_t free_b = 0, total = 0;
+    ck(cudaMemGetInfo(&free_b, &total), "cudaMemGetInfo");
+    s->budget = hbm_budget_bytes ? hbm_budget_bytes : free_b / 10 * 8;
+    mdft_server_s* raw = s.get();
+    s->worker = std::thread([raw] { raw->run(); });
+    *out = s.release();
+  });
+}
+
+int mdft_server_destroy(mdft_server_t s) {
+  if (!s) return MDFT_OK;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+    for (auto& kv : s->jobs)
+      if (kv.second->state == 0 || kv.second->state == 1) {
+        kv.second->state = -1;
+        kv.second->code = MDFT_ERR_INVALID;
+        kv.second->error = "server destroyed";
+      }
+    s->cv_done.notify_all();
+  }
+  s->cv_work.notify_all();
+  if (s->worker.joinable()) s->worker.join();
+  cudaSetDevice(s->device);
+  delete s;
+  return MDFT_OK;
+}
+
+int mdft_server_add_solvent(mdft_server_t s, int mmax, int mrso, const int* luc_index, const double* luc,
+                            int np_luc, int nq, double dq, double rho0, double prefactor, int* solvent_id) {
+  return sguard([&] {
+    throw_if(!s || !luc_index || !luc || !solvent_id, "NULL argument");
+    throw_if(mmax < 1 || mmax > 6 || mrso < 1, "solvent needs 1 <= mmax <= 6 and mrso >= 1");
+    throw_if(np_luc <= 0 || nq <= 1 || !(dq > 0), "invalid c(q) table extents");
+    Solvent sv;
+    sv.mmax = mmax;
+    sv.mrso = mrso;
+    sv.np_luc = np_luc;
+    sv.nq = nq;
+    sv.dq = dq;
+    sv.rho0 = rho0;
+    sv.prefactor = prefactor;
+    sv.luc_index.assign(luc_index, luc_index + 5 * (size_t)np_luc);
+    sv.luc.assign(luc, luc + 2 * (size_t)np_luc * nq);
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->solvents.push_back(std::move(sv));
+    *solvent_id = (int)s->solvents.size() - 1;
+  });
+}
+
+int mdft_server_submit(mdft_server_t s, int solvent_id, int nx, int ny, int nz, double lx, double ly, double lz,
+                       const void* xi0, int n_steps, double step, long long* job_id) {
+  return sguard([&] {
+    throw_if(!s || !xi0 || !job_id, "NULL argument");
+    throw_if(nx < 1 || ny < 1 || nz < 1 || !(lx > 0) || !(ly > 0) || !(lz > 0), "invalid grid");
+    throw_if(n_steps < 1 || n_steps > s->trace_cap, "n_steps must be 1.." + std::to_string(s->trace_cap));
+    auto j = std::make_shared<Job>();
+    int no = 0;
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      throw_if(solvent_id < 0 || solvent_id >= (int)s->solvents.size(), "unknown solvent");
+      const Solvent& sv = s->solvents[solvent_id];
+      const int nt = sv.mmax + 1, nphi = 2 * sv.mmax + 1, npsi = 2 * (sv.mmax / sv.mrso) + 1;
+      no = nt * nphi * npsi;
+    }
+    const size_t elem = s->prec == MDFT_F32 ? 4 : 8;
+    const size_t bytes = (size_t)nx * ny * nz * no * elem;
+    j->solvent = solvent_id;
+    j->n[0] = nx;
+    j->n[1] = ny;
+    j->n[2] = nz;
+    j->len[0] = lx;
+    j->len[1] = ly;
+    j->len[2] = lz;
+    j->xi.assign(static_cast<const unsigned char*>(xi0), static_cast<const unsigned char*>(xi0) + bytes);
+    j->n_steps = n_steps;
+    j->step = step;
+    j->t_submit = Clock::now();
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      j->id = s->next_id++;
+      if (!s->any_submit) {
+        s->any_submit = true;
+        s->t_first_submit = j->t_submit;
+      }
+      s->jobs[j->id] = j;
+      s->incoming.push_back(j);
+      *job_id = j->id;
+    }
+    s->cv_work.notify_all();
+  });
+}
+
+int mdft_server_wait(mdft_server_t s, long long job_id, void* xi_out, double* ff_out, double* latency_s) {
+  return sguard([&] {
+    throw_if(!s, "NULL argument");
+    std::shared_ptr<Job> j;
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->jobs.find(job_id);
+    throw_if(it == s->jobs.end(), "unknown job (or its result was already taken)");
+    j = it->second;
+    s->cv_done.wait(lk, [&] { return j->state == 2 || j->state == -1; });
+    s->jobs.erase(it);
+    if (j->state == -1) throw Error(j->code, j->error);
+    if (xi_out) std::memcpy(xi_out, j->xi.data(), j->xi.size());
+    if (ff_out) std::memcpy(ff_out, j->ff.data(), sizeof(double) * j->ff.size());
+    if (latency_s) *latency_s = std::chrono::duration<double>(j->t_done - j->t_submit).count();
+  });
+}
+
+int mdft_server_stats(mdft_server_t s, double* out) {
+  return sguard([&] {
+    throw_if(!s || !out, "NULL argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    std::vector<double> l = s->latencies;
+    std::sort(l.begin(), l.end());
+    auto pct = [&](double q) {
+      if (l.empty()) return 0.0;
+      const size_t i = (size_t)std::min<double>((double)l.size() - 1, std::ceil(q * l.size()) - 1);
+      return l[i];
+    };
+    const double span =
+        l.empty() ? 0.0 : std::chrono::duration<double>(s->t_last_done - s->t_first_submit).count();
+    out[0] = (double)l.size();
+    out[1] = span > 0 ? l.size() / span : 0.0;
+    out[2] = pct(0.50);
+    out[3] = pct(0.99);
+    out[4] = (double)s->n_groups.load();
+    out[5] = (double)s->peak.load();
+  });
+}

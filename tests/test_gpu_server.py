@@ -1,0 +1,115 @@
+"""The job server (mdft_server_*): jobs of several shapes and uneven lengths,
+submitted from several host threads, must return exactly what the same
+steps give through the operator API one field at a time (the server batches
+same-shape jobs, replays captured graphs and compacts finished slots, none of
+which may change a job's numbers), and the latency statistics must cover
+every job."""
+import threading
+
+import numpy as np
+import pytest
+
+from mini_mdft_gb300 import inputs as I
+
+pytestmark = pytest.mark.gpu
+
+DQ = 0.01
+# (grid, box, mmax, mrso): two shapes share a solvent, one has its own
+SHAPES = [((12, 10, 8), (12., 10., 9.), 3, 2), ((8, 8, 8), (10., 10., 10.), 3, 2),
+          ((6, 7, 5), (9., 9., 8.), 2, 1)]
+
+
+def _solvent_table(mmax, mrso):
+    nq = max(I.nq_for(n, box, DQ) for n, box, m, r in SHAPES if (m, r) == (mmax, mrso))
+    return I.synthetic_cq(mmax, mrso, nq + 2, DQ)
+
+
+def _direct(M, n, box, mmax, mrso, table, rho0, pref, xi0, n_steps, step, prec):
+    """The job's steps through the operator API, one field."""
+    import torch
+    idx, tab = table
+    sg, ag = M.SpatialGrid(n, box), M.AngularGrid(mmax, mrso)
+    opt = M.OrientationProjectionTransform(sg, ag, precision=prec)
+    conv = M.Convolution.from_table(idx, tab, DQ, sg, ag, precision=prec)
+    rd, cd = (torch.float32, torch.complex64) if prec == "f32" else (torch.float64, torch.complex128)
+    xi = torch.from_numpy(xi0).to("cuda", rd)
+    w = torch.from_numpy(ag.m_w)
+    p = torch.zeros((ag.m_np,) + tuple(n), dtype=cd, device="cuda")
+    vexc, df = torch.zeros_like(xi), torch.zeros_like(xi)
+    ffs = []
+    for _ in range(n_steps):
+        opt.angl2proj_from_xi(xi, rho0, p)
+        conv.execute(p)
+        opt.proj2angl(p, vexc)
+        ffs.append(M.get_delta_f(xi, vexc, w, df, rho0, pref))
+        xi = xi - step * df
+    torch.cuda.synchronize()
+    return xi.cpu().numpy(), np.array(ffs)
+
+
+@pytest.mark.parametrize("prec", ["f64", "f64df", "f32"])
+def test_server_jobs_match_operator_api(gpu_lib, prec):
+    M = gpu_lib
+    rho0, pref = I.tip3p_constants(2)
+    srv = M.Server(precision=prec, max_batch=3)
+    tables = {}
+    solvent = {}
+    for n, box, mmax, mrso in SHAPES:
+        if (mmax, mrso) not in solvent:
+            tables[(mmax, mrso)] = _solvent_table(mmax, mrso)
+            idx, tab = tables[(mmax, mrso)]
+            solvent[(mmax, mrso)] = srv.add_solvent(mmax, mrso, idx, tab, DQ, rho0, pref)
+    rng = np.random.default_rng(11)
+    jobs = []
+    for i in range(9):  # shape 0 gets 5 jobs: more than one batch of 3
+        n, box, mmax, mrso = SHAPES[[0, 0, 1, 0, 2, 0, 1, 0, 2][i]]
+        nt, nphi, npsi, _, _ = I.angular_counts(mmax, mrso)
+        xi0 = rng.uniform(0.9, 1.1, (n[0] * n[1] * n[2], nt, nphi, npsi))
+        if prec == "f32":
+            xi0 = xi0.astype(np.float32)
+        jobs.append(dict(shape=(n, box, mmax, mrso), xi0=xi0, n_steps=int(rng.integers(2, 7)),
+                         step=float(rng.uniform(1e-3, 5e-3))))
+    ids = [None] * len(jobs)
+
+    def submit(lo, hi):
+        for i in range(lo, hi):
+            j = jobs[i]
+            n, box, mmax, mrso = j["shape"]
+            ids[i] = srv.submit(solvent[(mmax, mrso)], n, box, j["xi0"], j["n_steps"], j["step"])
+
+    threads = [threading.Thread(target=submit, args=(a, a + 3)) for a in (0, 3, 6)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    tol_xi, tol_ff = (1e-5, 1e-5) if prec == "f32" else (1e-12, 1e-12)
+    for i, j in enumerate(jobs):
+        xi, ff, lat = srv.wait(ids[i])
+        n, box, mmax, mrso = j["shape"]
+        xr, fr = _direct(M, n, box, mmax, mrso, tables[(mmax, mrso)], rho0, pref, j["xi0"],
+                         j["n_steps"], j["step"], prec)
+        assert lat > 0
+        assert np.all(np.isfinite(ff)) and len(ff) == j["n_steps"]
+        assert np.max(np.abs(ff - fr)) <= tol_ff * np.max(np.abs(fr))
+        assert np.max(np.abs(xi - xr)) <= tol_xi * np.max(np.abs(xr))
+    st = srv.stats()
+    assert st["done"] == len(jobs)
+    assert 0 < st["p50_s"] <= st["p99_s"]
+    assert st["solves_per_s"] > 0 and st["groups"] == len(SHAPES) and st["peak_bytes"] > 0
+    srv.close()
+
+
+def test_server_budget_too_small(gpu_lib):
+    M = gpu_lib
+    rho0, pref = I.tip3p_constants(2)
+    srv = M.Server(precision="f64", max_batch=2, hbm_budget_bytes=1 << 20)
+    idx, tab = _solvent_table(3, 2)
+    sid = srv.add_solvent(3, 2, idx, tab, DQ, rho0, pref)
+    n, box = (12, 10, 8), (12., 10., 9.)
+    xi0 = np.ones((n[0] * n[1] * n[2], 4, 7, 3))
+    jid = srv.submit(sid, n, box, xi0, 2, 1e-3)
+    with pytest.raises(M.MdftError, match="budget"):
+        srv.wait(jid)
+    with pytest.raises(M.MdftError, match="unknown job"):
+        srv.wait(jid)
+    srv.close()
