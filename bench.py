@@ -48,6 +48,7 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serving", action="store_true", help="skip the job-server leg")
     ap.add_argument("--mode", choices=["full", "steps"], default="full",
                     help="steps: only W warm-up + K timed FP64 and FP32 round trips "
                          "(a short, fixed launch sequence for ncu captures)")
@@ -337,6 +338,81 @@ def read_traffic(kernel):
     return None
 
 
+SERVING = dict(shapes=[((32, 32, 32), (20.0, 20.0, 20.0), 20), ((64, 64, 64), (30.0, 30.0, 30.0), 4)],
+               mmax=3, mrso=2, steps=(5, 15), step=2e-3, max_batch=8)
+
+
+def serving_run(prec):
+    """The job server on a stream of solvation-style jobs of uneven sizes and
+    lengths (SERVING: 20 jobs on 32^3 / 20 A and 4 on 64^3 / 30 A, mmax 3,
+    5-14 steps each, all submitted at once after one warm-up job per shape),
+    and the same jobs one at a time through the operator API."""
+    import numpy as np
+    import torch
+
+    import mini_mdft_gb300 as M
+    from mini_mdft_gb300 import inputs as I
+    mmax, mrso, dq = SERVING["mmax"], SERVING["mrso"], 0.01
+    rho0, pref = I.tip3p_constants(mrso)
+    nq = max(I.nq_for(n, box, dq) for n, box, _ in SERVING["shapes"])
+    idx, tab = I.synthetic_cq(mmax, mrso, nq, dq)
+    nt, nphi, npsi, _, _ = I.angular_counts(mmax, mrso)
+    dt = np.float32 if prec == "f32" else np.float64
+    rng = np.random.default_rng(4)
+    fields = {n: rng.uniform(0.9, 1.1, (n[0] * n[1] * n[2], nt, nphi, npsi)).astype(dt)
+              for n, _, _ in SERVING["shapes"]}
+    jobs = []
+    for n, box, count in SERVING["shapes"]:
+        jobs += [(n, box, int(rng.integers(*SERVING["steps"]))) for _ in range(count)]
+    order = rng.permutation(len(jobs))
+    jobs = [jobs[i] for i in order]
+    srv = M.Server(precision=prec, max_batch=SERVING["max_batch"])
+    sid = srv.add_solvent(mmax, mrso, idx, tab, dq, rho0, pref)
+    for n, box, _ in SERVING["shapes"]:  # warm-up: plans, arenas
+        srv.wait(srv.submit(sid, n, box, fields[n], 2, SERVING["step"]))
+    t0 = time.perf_counter()
+    ids = [srv.submit(sid, n, box, fields[n], k, SERVING["step"]) for n, box, k in jobs]
+    lats = [srv.wait(i)[2] for i in ids]
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    # the same jobs one at a time, operator API on the caller's stream
+    plans = {}
+    for n, box, _ in SERVING["shapes"]:
+        sg, ag = M.SpatialGrid(n, box), M.AngularGrid(mmax, mrso)
+        plans[n] = (M.OrientationProjectionTransform(sg, ag, precision=prec),
+                    M.Convolution.from_table(idx, tab, dq, sg, ag, precision=prec),
+                    torch.from_numpy(ag.m_w), ag.m_np)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for n, box, k in jobs:
+        opt, conv, w, np_ = plans[n]
+        xi = torch.from_numpy(fields[n]).cuda()
+        p = torch.zeros((np_,) + tuple(n), dtype=torch.complex64 if prec == "f32" else torch.complex128,
+                        device="cuda")
+        vexc, df = torch.zeros_like(xi), torch.zeros_like(xi)
+        for _ in range(k):
+            opt.angl2proj_from_xi(xi, rho0, p)
+            conv.execute(p)
+            opt.proj2angl(p, vexc)
+            M.get_delta_f(xi, vexc, w, df, rho0, pref)
+            xi -= SERVING["step"] * df
+        xi.cpu()
+    seq = time.perf_counter() - t1
+    lats.sort()
+    steps = sum(k for _, _, k in jobs)
+    return {
+        "metric": "served solves/s", "value": len(jobs) / wall, "unit": "solves/s",
+        "p50_ms": 1e3 * lats[len(lats) // 2], "p99_ms": 1e3 * lats[min(len(lats) - 1, int(0.99 * len(lats)))],
+        "applies_per_s": steps / wall, "jobs": len(jobs), "steps": steps, "form": prec,
+        "workload": "%d jobs (20 x 32^3/20 A, 4 x 64^3/30 A; mmax 3, mrso 2; 5-14 steps each, "
+                    "each step = energy + gradient + descent), submitted at once from host arrays; "
+                    "max_batch %d" % (len(jobs), SERVING["max_batch"]),
+        "graph_steps": st["graph_steps"], "direct_steps": st["direct_steps"],
+        "sequential_solves_per_s": len(jobs) / seq,
+    }
+
+
 def cpu_round_trip_rate(seconds_target=12.0, max_reps=20):
     """The oracle's round trip on this host's cores: (applies/s, reps, cores)."""
     import numpy as np
@@ -560,6 +636,8 @@ def run_ours(args):
         "forms": {f: form_entry(f) for f in forms},
         "mixed": dict(form_entry("f32"), speedup_vs_f64_form=form_secs[head] / form_secs["f32"]),
     }
+    if rank == 0 and not args.no_serving:
+        out["serving"] = serving_run(head)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         rate, reps, cores, el = cpu_round_trip_rate()
         out["cpu_baseline"] = {"value": rate, "unit": "applies/s", "cores": cores, "kind": "port",

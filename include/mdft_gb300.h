@@ -229,8 +229,9 @@ int mdft_server_submit(mdft_server_t s, int solvent_id, int nx, int ny, int nz, 
  * latency from submit (seconds, may be NULL).  Each job is waited for once. */
 int mdft_server_wait(mdft_server_t s, long long job_id, void* xi_out, double* ff_out,
                      double* latency_s);
-/* out[0..5]: jobs done, jobs done per second since the first submit, p50 and
- * p99 latency (s), job groups held, peak device bytes of the groups. */
+/* out[0..7]: jobs done, jobs done per second since the first submit, p50 and
+ * p99 latency (s), job groups held, peak device bytes of the groups, group
+ * steps replayed from captured graphs, group steps launched directly. */
 int mdft_server_stats(mdft_server_t s, double* out);
 
 #ifdef __cplusplus

@@ -425,8 +425,10 @@ class Server:
         return xi, ff, lat.value
 
     def stats(self):
-        """dict: done, solves_per_s, p50_s, p99_s, groups, peak_bytes."""
-        out = np.zeros(6, np.float64)
+        """dict: done, solves_per_s, p50_s, p99_s, groups, peak_bytes,
+        graph_steps, direct_steps."""
+        out = np.zeros(8, np.float64)
         check(lib().mdft_server_stats(self.h, out.ctypes.data_as(C.POINTER(C.c_double))))
-        keys = ("done", "solves_per_s", "p50_s", "p99_s", "groups", "peak_bytes")
+        keys = ("done", "solves_per_s", "p50_s", "p99_s", "groups", "peak_bytes", "graph_steps",
+                "direct_steps")
         return dict(zip(keys, out.tolist()))

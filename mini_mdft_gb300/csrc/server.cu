@@ -146,6 +146,7 @@ struct mdft_server_s {
   size_t budget = 0, in_use = 0;  // in_use: worker only
   std::atomic<size_t> peak{0};
   std::atomic<int> n_groups{0};
+  std::atomic<long long> graph_steps{0}, direct_steps{0};
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<std::shared_ptr<Job>> incoming;
@@ -361,6 +362,7 @@ void mdft_server_s::step(Group& g) {
   auto it = g.graphs.find(k);
   if (it != g.graphs.end() && it->second) {
     ck(cudaGraphLaunch(it->second, g.stream), "cudaGraphLaunch");
+    graph_steps += 1;
     return;
   }
   if (it == g.graphs.end() && g.seen[k] >= 1) {
@@ -382,11 +384,13 @@ void mdft_server_s::step(Group& g) {
     g.graphs[k] = ok ? exec : nullptr;
     if (ok) {
       ck(cudaGraphLaunch(exec, g.stream), "cudaGraphLaunch");
+      graph_steps += 1;
       return;
     }
   }
   g.seen[k] += 1;
   enqueue_step(g, k);
+  direct_steps += 1;
 }
 
 void mdft_server_s::finish(Group& g, int slot) {
@@ -637,5 +641,7 @@ int mdft_server_stats(mdft_server_t s, double* out) {
     out[3] = pct(0.99);
     out[4] = (double)s->n_groups.load();
     out[5] = (double)s->peak.load();
+    out[6] = (double)s->graph_steps.load();
+    out[7] = (double)s->direct_steps.load();
   });
 }
