@@ -82,12 +82,51 @@ struct Solvent {
   std::vector<double> luc;
 };
 
+// Page-locked host buffers for the job fields, kept for reuse: copies to and
+// from pageable memory are staged by the driver at a fraction of the link's
+// bandwidth, and page-locking on every job would cost more than the copy.
+class PinnedPool {
+ public:
+  ~PinnedPool() {
+    for (auto& kv : free_)
+      for (void* p : kv.second) cudaFreeHost(p);
+  }
+  void* get(size_t bytes) {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      auto it = free_.find(bytes);
+      if (it != free_.end() && !it->second.empty()) {
+        void* p = it->second.back();
+        it->second.pop_back();
+        return p;
+      }
+    }
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, bytes ? bytes : 1, cudaHostAllocDefault) != cudaSuccess) {
+      cudaGetLastError();
+      throw Error(MDFT_ERR_NOMEM, "page-locked host allocation failed");
+    }
+    return p;
+  }
+  void put(void* p, size_t bytes) {
+    if (!p) return;
+    std::lock_guard<std::mutex> lk(mu_);
+    free_[bytes].push_back(p);
+  }
+
+ private:
+  std::mutex mu_;
+  std::map<size_t, std::vector<void*>> free_;
+};
+
 struct Job {
   long long id = 0;
   int solvent = 0;
   int n[3] = {0, 0, 0};
   double len[3] = {0, 0, 0};
-  std::vector<unsigned char> xi;  // initial field on submit, final field when done
+  // initial field on submit, final field when done (page-locked, from the pool)
+  void* xi = nullptr;
+  size_t xi_bytes = 0;
   std::vector<double> ff;         // energy of every step
   int n_steps = 0;
   double step = 0;
@@ -152,6 +191,7 @@ struct mdft_server_s {
   std::deque<std::shared_ptr<Job>> incoming;
   std::map<long long, std::shared_ptr<Job>> jobs;
   std::vector<Solvent> solvents;
+  PinnedPool pinned;
   long long next_id = 1;
   bool stop = false;
   std::thread worker;
@@ -296,8 +336,7 @@ void mdft_server_s::admit() {
     const int slot = g->k;
     try {
       const size_t fb = field_bytes(*g);
-      ck(cudaMemcpyAsync(g->xi.as<unsigned char>() + fb * slot, j->xi.data(), fb, cudaMemcpyHostToDevice,
-                         g->stream),
+      ck(cudaMemcpyAsync(g->xi.as<unsigned char>() + fb * slot, j->xi, fb, cudaMemcpyHostToDevice, g->stream),
          "job field upload");
       ck(cudaMemcpyAsync(g->alpha.as<double>() + slot, &j->step, 8, cudaMemcpyHostToDevice, g->stream),
          "job step upload");
@@ -396,9 +435,9 @@ void mdft_server_s::step(Group& g) {
 void mdft_server_s::finish(Group& g, int slot) {
   std::shared_ptr<Job> j = g.slots[slot];
   const size_t fb = field_bytes(g);
-  std::vector<unsigned char> xi(fb);
   std::vector<double> ff(j->n_steps);
-  ck(cudaMemcpyAsync(xi.data(), g.xi.as<unsigned char>() + fb * slot, fb, cudaMemcpyDeviceToHost, g.stream),
+  // the final field goes back into the job's page-locked buffer
+  ck(cudaMemcpyAsync(j->xi, g.xi.as<unsigned char>() + fb * slot, fb, cudaMemcpyDeviceToHost, g.stream),
      "job field download");
   ck(cudaMemcpyAsync(ff.data(), g.trace.as<double>() + (size_t)slot * g.cap, 8 * (size_t)j->n_steps,
                      cudaMemcpyDeviceToHost, g.stream),
@@ -426,7 +465,6 @@ void mdft_server_s::finish(Group& g, int slot) {
   g.k -= 1;
   g.last_used = Clock::now();
   std::lock_guard<std::mutex> lk(mu);
-  j->xi.swap(xi);
   j->ff.swap(ff);
   j->state = 2;
   j->t_done = Clock::now();
@@ -536,6 +574,10 @@ int mdft_server_destroy(mdft_server_t s) {
   s->cv_work.notify_all();
   if (s->worker.joinable()) s->worker.join();
   cudaSetDevice(s->device);
+  for (auto& kv : s->jobs) {  // results never collected: their buffers go back to the pool
+    s->pinned.put(kv.second->xi, kv.second->xi_bytes);
+    kv.second->xi = nullptr;
+  }
   delete s;
   return MDFT_OK;
 }
@@ -586,7 +628,9 @@ int mdft_server_submit(mdft_server_t s, int solvent_id, int nx, int ny, int nz, 
     j->len[0] = lx;
     j->len[1] = ly;
     j->len[2] = lz;
-    j->xi.assign(static_cast<const unsigned char*>(xi0), static_cast<const unsigned char*>(xi0) + bytes);
+    j->xi = s->pinned.get(bytes);
+    j->xi_bytes = bytes;
+    std::memcpy(j->xi, xi0, bytes);
     j->n_steps = n_steps;
     j->step = step;
     j->t_submit = Clock::now();
@@ -615,8 +659,17 @@ int mdft_server_wait(mdft_server_t s, long long job_id, void* xi_out, double* ff
     j = it->second;
     s->cv_done.wait(lk, [&] { return j->state == 2 || j->state == -1; });
     s->jobs.erase(it);
+    lk.unlock();
+    struct Release {  // the buffer returns to the pool however this ends
+      mdft_server_s* s;
+      std::shared_ptr<Job> j;
+      ~Release() {
+        s->pinned.put(j->xi, j->xi_bytes);
+        j->xi = nullptr;
+      }
+    } rel{s, j};
     if (j->state == -1) throw Error(j->code, j->error);
-    if (xi_out) std::memcpy(xi_out, j->xi.data(), j->xi.size());
+    if (xi_out) std::memcpy(xi_out, j->xi, j->xi_bytes);
     if (ff_out) std::memcpy(ff_out, j->ff.data(), sizeof(double) * j->ff.size());
     if (latency_s) *latency_s = std::chrono::duration<double>(j->t_done - j->t_submit).count();
   });
