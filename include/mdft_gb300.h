@@ -159,6 +159,20 @@ int mdft_conv_gamma_p_map(mdft_conv_t h, int* map);
 /* mnmunukhi_q() as (np_new, nq) complex double, host copy. */
 int mdft_conv_mnmunukhi_q(mdft_conv_t h, double* tab);
 
+/* ---- c(q) files ---------------------------------------------------------------
+ * IO::LucData (common/IO/MDFT_ReadCLuc.hpp:40-260) on the host, no GPU work.
+ * mdft_luc_read: reads the first int(qmax/dq + 0.5) + 2 q rows of a Luc text
+ * file (the rows a grid with that |q_max| needs); with luc_index or luc NULL
+ * it only returns nq and dq (call it first to size the arrays).  luc_index is
+ * 5 x np_luc ints, luc (np_luc, nq) complex double.
+ * mdft_luc_write: writes a table in the layout the reader parses (no
+ * counterpart in the reference, which only reads; it lets a producer of
+ * c(q) tables hand them to the reference or to this library as files). */
+int mdft_luc_read(const char* path, int np_luc, double qmax, int* luc_index, double* luc,
+                  int* nq, double* dq);
+int mdft_luc_write(const char* path, const int* luc_index, const double* luc, int np_luc,
+                   int nq, double dq, const char* header);
+
 /* ---- energy ---------------------------------------------------------------
  * get_delta_rho(exec, xi, delta_rho, rho0), MDFT_Solvent.hpp:578-596:
  * delta_rho[i] = rho0 (xi[i]^2 - 1) over n elements.  precision selects

@@ -16,6 +16,8 @@ from .api import (  # noqa: F401
     SpatialGrid,
     get_delta_f,
     get_delta_rho,
+    luc_read,
+    luc_write,
 )
 from ._lib import LIB_PATH, lib  # noqa: F401
 

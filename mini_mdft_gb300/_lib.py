@@ -51,6 +51,8 @@ SIGNATURES = {
     "mdft_conv_info": (i32, [vp, ip, dp]),
     "mdft_conv_gamma_p_map": (i32, [vp, ip]),
     "mdft_conv_mnmunukhi_q": (i32, [vp, dp]),
+    "mdft_luc_read": (i32, [C.c_char_p, i32, f64, ip, dp, ip, dp]),
+    "mdft_luc_write": (i32, [C.c_char_p, ip, dp, i32, i32, f64, C.c_char_p]),
     "mdft_get_delta_rho": (i32, [vp, vp, sz, f64, i32, vp]),
     "mdft_get_delta_f": (i32, [vp, vp, vp, vp, vp, sz, i32, f64, f64, i32, vp]),
     "mdft_get_delta_f_noalloc": (i32, [vp, vp, vp, vp, vp, sz, i32, f64, f64, i32, vp]),

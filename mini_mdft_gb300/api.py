@@ -432,3 +432,25 @@ class Server:
         keys = ("done", "solves_per_s", "p50_s", "p99_s", "groups", "peak_bytes", "graph_steps",
                 "direct_steps")
         return dict(zip(keys, out.tolist()))
+
+
+def luc_read(path, np_luc, qmax):
+    """IO::LucData: (luc_index (5, np_luc) int32, table (np_luc, nq) complex128,
+    dq) with the first int(qmax/dq + 0.5) + 2 q rows (mdft_luc_read)."""
+    nq, dq = C.c_int(), C.c_double()
+    check(lib().mdft_luc_read(str(path).encode(), int(np_luc), float(qmax), None, None,
+                              C.byref(nq), C.byref(dq)))
+    idx = np.zeros((5, np_luc), np.int32)
+    tab = np.zeros((np_luc, nq.value), np.complex128)
+    check(lib().mdft_luc_read(str(path).encode(), int(np_luc), float(qmax), _np_i(idx),
+                              tab.ctypes.data_as(C.POINTER(C.c_double)), C.byref(nq), C.byref(dq)))
+    return idx, tab, dq.value
+
+
+def luc_write(path, luc_index, table, dq, header="c(q) table"):
+    """Writes a c(q) table in the Luc text layout (mdft_luc_write)."""
+    idx = np.ascontiguousarray(luc_index, np.int32)
+    tab = np.ascontiguousarray(table, np.complex128)
+    np_luc, nq = tab.shape
+    check(lib().mdft_luc_write(str(path).encode(), _np_i(idx), tab.ctypes.data_as(C.POINTER(C.c_double)),
+                               np_luc, nq, float(dq), header.encode()))

@@ -776,3 +776,35 @@ int current_device() { return ::current_device(); }
 
 }  // namespace detail
 }  // namespace mdft
+
+// ---- c(q) files ------------------------------------------------------------------
+int mdft_luc_read(const char* path, int np_luc, double qmax, int* luc_index, double* luc, int* nq,
+                  double* dq) {
+  return guarded([&] {
+    throw_if(!path || !nq || !dq, "NULL argument");
+    throw_if(!(qmax > 0), "qmax must be positive");
+    const mdft::LucTable t = mdft::read_luc_file(path, np_luc, qmax);
+    *nq = t.nq;
+    *dq = t.dq;
+    if (luc_index && luc) {
+      std::memcpy(luc_index, t.index.data(), sizeof(int) * t.index.size());
+      std::memcpy(luc, t.tab.data(), sizeof(double) * 2 * t.tab.size());
+    }
+  });
+}
+
+int mdft_luc_write(const char* path, const int* luc_index, const double* luc, int np_luc, int nq, double dq,
+                   const char* header) {
+  return guarded([&] {
+    throw_if(!path || !luc_index || !luc, "NULL argument");
+    throw_if(np_luc <= 0 || nq <= 0 || !(dq > 0), "invalid c(q) table extents");
+    mdft::LucTable t;
+    t.np_luc = np_luc;
+    t.nq = nq;
+    t.dq = dq;
+    t.index.assign(luc_index, luc_index + 5 * (size_t)np_luc);
+    t.tab.resize((size_t)np_luc * nq);
+    std::memcpy(t.tab.data(), luc, sizeof(double) * 2 * t.tab.size());
+    mdft::write_luc_file(path, t, header ? header : "c(q) table");
+  });
+}

@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <fstream>
 #include <limits>
@@ -290,6 +291,39 @@ LucTable read_luc_file(const std::string& path, int np_luc, double qmaxwanted) {
     throw_if(q > qmaxwanted + 2.0 * t.dq, "q > qmaxwanted in file.", 3);
   }
   return t;
+}
+
+void write_luc_file(const std::string& path, const LucTable& t, const std::string& header) {
+  throw_if(t.np_luc <= 0 || t.nq <= 0 || !(t.dq > 0), "invalid c(q) table extents");
+  throw_if(t.index.size() != (size_t)5 * t.np_luc || t.tab.size() != (size_t)t.np_luc * t.nq,
+           "c(q) table arrays do not match their extents");
+  std::FILE* f = std::fopen(path.c_str(), "w");
+  throw_if(!f, "cannot open " + path + " for writing", 3);
+  std::string line;
+  char buf[80];
+  auto put = [&](const std::string& x) { std::fputs(x.c_str(), f); };
+  put("# " + header + "\n");
+  for (int i = 0; i < 9; ++i) put("#\n");
+  put("# projection indices\n");
+  const char* names[5] = {"m", "n", "mu", "nu", "khi"};
+  for (int row = 0; row < 5; ++row) {
+    line = names[row];
+    for (int i = 0; i < t.np_luc; ++i) line += " " + std::to_string(t.index[(size_t)row * t.np_luc + i]);
+    put(line + "\n");
+  }
+  put("# q  c(q) for each projection\n");
+  for (int iq = 0; iq < t.nq; ++iq) {
+    std::snprintf(buf, sizeof buf, "%.17g", iq * t.dq);
+    line = buf;
+    for (int ip = 0; ip < t.np_luc; ++ip) {
+      const std::complex<double> z = t.tab[(size_t)ip * t.nq + iq];
+      std::snprintf(buf, sizeof buf, " (%.17g,%.17g)", z.real(), z.imag());
+      line += buf;
+    }
+    put(line + "\n");
+  }
+  const bool ok = std::ferror(f) == 0;
+  throw_if(std::fclose(f) != 0 || !ok, "error writing " + path, 3);
 }
 
 std::vector<std::complex<double>> reorder_luc(const Grid& g, const LucTable& t, int nq) {

@@ -77,6 +77,11 @@ struct LucTable {
 // Reads the Luc text file (ReadCLuc.hpp:123-259) keeping the first
 // int(qmaxwanted/dq + 0.5) + 2 rows.
 LucTable read_luc_file(const std::string& path, int np_luc, double qmaxwanted);
+// Writes a table in the same text layout (ReadCLuc.hpp:123-187 parses it):
+// ten free lines (the first holds `header`), a label line, the five index
+// rows m, n, mu, nu, khi, a label line, then one row 'q (re,im) ...' per q
+// with q = iq dq; values printed with 17 significant digits (exact round trip).
+void write_luc_file(const std::string& path, const LucTable& t, const std::string& header);
 
 // Reorder + sign fold into mnmunukhi_q (np_new, nq_used)
 // (common/MDFT_Convolution.hpp:239-311).

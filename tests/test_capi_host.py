@@ -109,3 +109,27 @@ def test_generators_are_seeded():
     assert a.min() >= -0.1 and a.max() <= 0.1
     x = I.synthetic_xi(10, 3, 2)
     assert x.min() >= 0.9 and x.max() <= 1.1
+
+
+def test_luc_write_read_round_trip(L, tmp_path):
+    """C++ Luc writer and reader (host only): the written file is the one the
+    Python writer produces, byte for byte, both readers get the table back
+    exactly, and a smaller |q_max| keeps int(qmax/dq + 0.5) + 2 rows."""
+    import mini_mdft_gb300 as M
+    idx, tab = I.synthetic_cq(3, 2, 40, 0.01)
+    a, b = tmp_path / "cpp.luc", tmp_path / "py.luc"
+    M.luc_write(a, idx, tab, 0.01, header="synthetic c(q) table")
+    I.write_luc_file(str(b), idx, tab, 0.01, header="synthetic c(q) table")
+    assert a.read_bytes() == b.read_bytes()
+    i2, t2, dq2 = I.read_luc_file(str(a), idx.shape[1])
+    assert np.array_equal(i2, idx) and np.array_equal(t2, tab) and abs(dq2 - 0.01) < 1e-15
+    qmax = 0.37
+    i3, t3, dq3 = M.luc_read(a, idx.shape[1], qmax)
+    nq = int(qmax / dq3 + 0.5) + 2
+    assert np.array_equal(i3, idx) and t3.shape == (idx.shape[1], nq)
+    assert np.array_equal(t3, tab[:, :nq])
+    with pytest.raises(M.MdftError, match="does not exist") as e:
+        M.luc_read(tmp_path / "missing", idx.shape[1], qmax)
+    assert e.value.code == 3
+    with pytest.raises(M.MdftError, match="fewer q rows"):
+        M.luc_read(a, idx.shape[1], 1.0)
