@@ -223,16 +223,50 @@ template <>
 __device__ __forceinline__ Cx<DF> cmul_tw<DF>(Cx<DF> x, Cx<DF> w) {
   return mkc<DF>(df_dot2_pair(x.re, w.re, -x.im, w.im), df_dot2_pair(x.re, w.im, x.im, w.re));
 }
-// the length-4 DFT on registers (forward: e^{-2 pi i nk/4})
-template <typename T, bool FWD>
+// Sums inside a butterfly: for double-float the pair is left unnormalised
+// (hi = fl(a.hi + b.hi), lo = its rounding error + a.lo + b.lo, still the
+// exact sum up to the lo additions); the butterfly's outputs are normalised.
+// The error stays bounded relative to the operands, the norm-wise bound of
+// FFT error analysis.
+template <typename T>
+__device__ __forceinline__ Cx<T> lz_add(Cx<T> a, Cx<T> b) {
+  return a + b;
+}
+template <typename T>
+__device__ __forceinline__ Cx<T> lz_sub(Cx<T> a, Cx<T> b) {
+  return a - b;
+}
+__device__ __forceinline__ DF df_add_lazy(DF a, DF b) {
+  const DF s = df_two_sum(a.hi, b.hi);
+  return DF(s.hi, s.lo + (a.lo + b.lo));
+}
+template <>
+__device__ __forceinline__ Cx<DF> lz_add<DF>(Cx<DF> a, Cx<DF> b) {
+  return mkc<DF>(df_add_lazy(a.re, b.re), df_add_lazy(a.im, b.im));
+}
+template <>
+__device__ __forceinline__ Cx<DF> lz_sub<DF>(Cx<DF> a, Cx<DF> b) {
+  return mkc<DF>(df_add_lazy(a.re, -b.re), df_add_lazy(a.im, -b.im));
+}
+
+// the length-4 DFT on registers (forward: e^{-2 pi i nk/4}); LAZY leaves
+// the outputs unnormalised too (they feed another layer of sums)
+template <typename T, bool FWD, bool LAZY = false>
 __device__ __forceinline__ void dft4(Cx<T>& v0, Cx<T>& v1, Cx<T>& v2, Cx<T>& v3) {
-  const Cx<T> a0 = v0 + v2, a1 = v0 - v2;
-  const Cx<T> b0 = v1 + v3, b1 = v1 - v3;
+  const Cx<T> a0 = lz_add(v0, v2), a1 = lz_sub(v0, v2);
+  const Cx<T> b0 = lz_add(v1, v3), b1 = lz_sub(v1, v3);
   const Cx<T> jb = FWD ? mkc<T>(b1.im, -b1.re) : mkc<T>(-b1.im, b1.re);
-  v0 = a0 + b0;
-  v1 = a1 + jb;
-  v2 = a0 - b0;
-  v3 = a1 - jb;
+  if (LAZY) {
+    v0 = lz_add(a0, b0);
+    v1 = lz_add(a1, jb);
+    v2 = lz_sub(a0, b0);
+    v3 = lz_sub(a1, jb);
+  } else {
+    v0 = a0 + b0;
+    v1 = a1 + jb;
+    v2 = a0 - b0;
+    v3 = a1 - jb;
+  }
 }
 
 template <typename T, bool FWD>
@@ -256,18 +290,20 @@ __device__ __forceinline__ void dft_small(Cx<T>* v, const Cx<T>* tw, int n) {
     // twiddles between them; 1/sqrt(2) from the twiddle table, tw[n/8]
     Cx<T> e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
     Cx<T> o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
-    dft4<T, FWD>(e0, e1, e2, e3);
-    dft4<T, FWD>(o0, o1, o2, o3);
+    dft4<T, FWD, true>(e0, e1, e2, e3);
+    dft4<T, FWD, true>(o0, o1, o2, o3);
     const T h = tw[n / 8].re;
     // forward: o1 (1 - i) h, o2 (-i), o3 (-1 - i) h; inverse: conjugates
+    const Cx<T> o1s = lz_add(o1, mkc<T>(o1.im, -o1.re)), o3s = lz_add(o3, mkc<T>(-o3.im, o3.re));
     if (FWD) {
-      o1 = mkc<T>((o1.re + o1.im) * h, (o1.im - o1.re) * h);
+      o1 = mkc<T>(o1s.re * h, o1s.im * h);  // (re + im, im - re) h
       o2 = mkc<T>(o2.im, -o2.re);
-      o3 = mkc<T>((o3.im - o3.re) * h, -(o3.re + o3.im) * h);
+      o3 = mkc<T>(-o3s.re * h, -o3s.im * h);  // (im - re, -(re + im)) h
     } else {
-      o1 = mkc<T>((o1.re - o1.im) * h, (o1.im + o1.re) * h);
+      const Cx<T> o1c = lz_add(o1, mkc<T>(-o1.im, o1.re)), o3c = lz_add(o3, mkc<T>(o3.im, -o3.re));
+      o1 = mkc<T>(o1c.re * h, o1c.im * h);  // (re - im, im + re) h
       o2 = mkc<T>(-o2.im, o2.re);
-      o3 = mkc<T>(-(o3.re + o3.im) * h, (o3.re - o3.im) * h);
+      o3 = mkc<T>(-o3c.re * h, -o3c.im * h);  // (-(re + im), re - im) h
     }
     v[0] = e0 + o0;
     v[4] = e0 - o0;
