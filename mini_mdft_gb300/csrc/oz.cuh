@@ -535,6 +535,14 @@ constexpr int oz_split_regs() {
              : 16384 / (32 * ((2 * (oz_split_threads<C, MMAX, MRSO>() / 32) + 3) / 4)) / 8 * 8;
 }
 
+// Loops over the rows of one rotation block: fully unrolled for FP32 up to
+// mmax 3, where one iteration holds little arithmetic and unrolling lets the
+// loads of later rows overlap the current one (larger blocks would spill);
+// rolled for double-float, whose arithmetic per row already covers the load
+// latency and whose unrolled code would crowd the instruction cache.
+template <typename C, int MMAX>
+constexpr int kOzUnroll = (sizeof(C) == 4 && MMAX <= 3) ? 2 * MMAX + 1 : 1;
+
 // MRSO > 0: the molecule's rotational symmetry order fixed at compile time
 // (every loop over nu unrolled, so the c(|q|) loads of a projection can be
 // issued together); MRSO = 0: read from the plan.
@@ -601,7 +609,7 @@ oz_lane_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
         if (flip) v = mkc<C>(-v.re, -v.im);
         D[ipx(m, 0, mu2) * 32 + lane] = v;
       }
-#pragma unroll 1
+#pragma unroll(kOzUnroll<C, MMAX>)
       for (int j = 1; j <= m; ++j) {
         // direct: sum_b g_b h_b; mirrored: sum_b (-1)^(m+b+j) g_{2m-b} conj(h_b)
         CAcc<C> xd, xm;
@@ -660,7 +668,7 @@ oz_lane_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
       CAcc<C> acc[2 * MMAX + 1];
 #pragma unroll
       for (int a = 0; a <= 2 * m; ++a) cacc_zero(acc[a]);
-#pragma unroll 1
+#pragma unroll(kOzUnroll<C, MMAX>)
       for (int k = -m; k <= m; ++k) {
         const int ak = k < 0 ? -k : k;
         CAcc<C> sacc;
