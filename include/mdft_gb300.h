@@ -209,6 +209,12 @@ int mdft_get_delta_f_noalloc(const void* xi, const void* vexc, const double* w,
                              double rho0, double prefactor, int precision,
                              void* stream);
 
+/* Diagnostics: number of waits on asynchronous copies (the tensor-memory-
+ * access tiles of the FFT) that ran out of time on the current device since
+ * the library was loaded; such a kernel leaves its tile untouched, so a
+ * non-zero count means wrong results.  No counterpart in the reference. */
+int mdft_wait_timeouts(int* count);
+
 /* ---- job server -----------------------------------------------------------
  * No counterpart in the reference (which evaluates one field per call).  A
  * server takes jobs from any host thread and runs them on the device that was

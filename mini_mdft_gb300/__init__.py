@@ -18,6 +18,7 @@ from .api import (  # noqa: F401
     get_delta_rho,
     luc_read,
     luc_write,
+    wait_timeouts,
 )
 from ._lib import LIB_PATH, lib  # noqa: F401
 

@@ -454,3 +454,12 @@ def luc_write(path, luc_index, table, dq, header="c(q) table"):
     np_luc, nq = tab.shape
     check(lib().mdft_luc_write(str(path).encode(), _np_i(idx), tab.ctypes.data_as(C.POINTER(C.c_double)),
                                np_luc, nq, float(dq), header.encode()))
+
+
+def wait_timeouts():
+    """Waits on asynchronous FFT tile copies that ran out of time on the
+    current device since the library was loaded (mdft_wait_timeouts); must
+    stay 0."""
+    c = C.c_int()
+    check(lib().mdft_wait_timeouts(C.byref(c)))
+    return c.value

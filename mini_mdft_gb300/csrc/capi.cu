@@ -808,3 +808,11 @@ int mdft_luc_write(const char* path, const int* luc_index, const double* luc, in
     mdft::write_luc_file(path, t, header ? header : "c(q) table");
   });
 }
+
+int mdft_wait_timeouts(int* count) {
+  return guarded([&] {
+    throw_if(!count, "NULL argument");
+    mdft::cuda_check(cudaMemcpy(count, mdft::fft_wait_error_counter(), sizeof(int), cudaMemcpyDeviceToHost),
+                     "read wait counter");
+  });
+}

@@ -441,8 +441,13 @@ struct FftAxis {
   int cols;       // transforms per CTA
   size_t smem;
   int fixed;      // 1: compile-time-length kernel for n, 0: runtime-radix kernel
+  int tma;        // 1: S > 1 tiles may move by tensor-memory-access copies
+  int* err;       // device counter of timed-out copy waits (this device's)
   const void* tw;  // (n) Cx<T> : exp(-2 pi i t / n)
 };
+// The current device's counter of timed-out waits on asynchronous copies in
+// the FFT kernels (allocated on first use; call outside stream capture).
+int* fft_wait_error_counter();
 bool fft_factor(int n, FftAxis& a);  // false if n has a prime factor > 13
 // Si / So: storage type of the tile on load / store (the same size, in
 // place); the double-float form keeps the projections as packed DF pairs

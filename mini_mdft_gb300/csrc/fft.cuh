@@ -17,6 +17,10 @@
 #pragma once
 #include <type_traits>
 
+#include <cuda.h>
+
+#include <cstdint>
+
 #include "common.cuh"
 
 namespace mdft {
@@ -559,12 +563,200 @@ void fixed_dispatch(const FftAxis& a, void* data, int sign, cudaStream_t s) {
 
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// Tensor-memory-access (TMA) tiles for the strided axes (S > 1).  A CTA's
+// tile is COLS adjacent columns of one run of S columns: as a 3-D tensor
+// (S, n, ncols / S) of 8-byte words it is the box (COLS w, n, 1), w words
+// per complex value, which lands in shared memory as the dense [n][COLS]
+// tile the Stockham stages read row by row (conflict-free without padding).
+// One thread issues the load, completing on an mbarrier, and, after every
+// thread has fenced its writes to the async proxy, the store of the result.
+// Columns past the end of a run are filled with zeros on load and clipped on
+// store by the copy engine.  The wait is bounded: a copy that does not land
+// in time is counted in A.err, waited for once more (bounded), and the CTA
+// returns without touching its tile.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned phase, long long limit) {
+  for (long long i = 0; i < limit; ++i) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(bar), "r"(phase)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+constexpr long long kTmaWaitLimit = 1LL << 22;
+
+template <typename Si, typename So, typename C, int N, int COLS, bool FWD, int THREADS>
+__global__ void __launch_bounds__(THREADS)
+fft_tma_kernel(const __grid_constant__ CUtensorMap tm, const FftAxis A, long long tiles_per_run) {
+  static_assert(sizeof(Cx<Si>) == sizeof(Cx<C>) && sizeof(Cx<So>) == sizeof(Cx<C>), "in-place tile");
+  constexpr int W = (int)(sizeof(Cx<Si>) / 8);  // 8-byte words per complex value
+  constexpr int TILE = N * COLS;
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  unsigned char* sm = sm_raw + ((128u - (smem_u32(sm_raw) & 127u)) & 127u);  // 128-byte aligned tile
+  Cx<C>* buf0 = reinterpret_cast<Cx<C>*>(sm);
+  Cx<C>* buf1 = buf0 + TILE;
+  Cx<C>* tw = buf1 + TILE;
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(tw + N);
+  const int tid = threadIdx.x;
+  const long long run = (long long)blockIdx.x / tiles_per_run;
+  const int x0 = (int)((long long)blockIdx.x - run * tiles_per_run) * COLS * W;
+  const unsigned bar_a = smem_u32(bar);
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_a) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (tid == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_a),
+                 "r"((unsigned)(TILE * sizeof(Cx<Si>)))
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(buf0)),
+        "l"(reinterpret_cast<unsigned long long>(&tm)), "r"(x0), "r"(0), "r"((int)run), "r"(bar_a)
+        : "memory");
+  }
+  for (int i = tid; i < N; i += THREADS) tw[i] = static_cast<const Cx<C>*>(A.tw)[i];
+  const bool late = !mbar_wait(bar_a, 0, kTmaWaitLimit);
+  if (__syncthreads_or(late)) {
+    if (tid == 0) {
+      atomicAdd(A.err, 1);
+      mbar_wait(bar_a, 0, kTmaWaitLimit);  // the copy may still be writing the tile
+    }
+    return;
+  }
+  if constexpr (!std::is_same<Si, C>::value) {
+#pragma unroll
+    for (int r = 0; r < TILE / THREADS; ++r) {
+      const int i = tid + r * THREADS;
+      const Cx<Si> v = reinterpret_cast<const Cx<Si>*>(buf0)[i];
+      buf0[i] = ld_c<C>(v);
+    }
+  }
+  Cx<C>* res = stages<C, N, COLS, FWD, 1>(buf0, buf1, tw, COLS, COLS, typename FftRadices<N>::type{});
+  __syncthreads();
+  if constexpr (!std::is_same<So, C>::value) {
+#pragma unroll
+    for (int r = 0; r < TILE / THREADS; ++r) {
+      const int i = tid + r * THREADS;
+      const Cx<C> v = res[i];
+      reinterpret_cast<Cx<So>*>(res)[i] = st_c<So>(v);
+    }
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  __syncthreads();
+  if (tid == 0) {
+    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(
+                     reinterpret_cast<unsigned long long>(&tm)),
+                 "r"(x0), "r"(0), "r"((int)run), "r"(smem_u32(res))
+                 : "memory");
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+    asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+  }
+}
+
+template <typename C, int N>
+size_t tma_smem() {
+  return sizeof(Cx<C>) * ((size_t)2 * N * fixed_cols<C>() + N) + 16 + 128;
+}
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+inline EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      f = nullptr;
+    }
+    return reinterpret_cast<EncodeTiledFn>(f);
+  }();
+  return fn;
+}
+
+// Launches the TMA kernel for this axis and data pointer; false when the
+// tile rules do not hold here (the caller then uses the plain kernel).
+template <typename Si, typename So, typename C, int N>
+bool tma_launch(const FftAxis& a, void* data, int sign, cudaStream_t s) {
+  constexpr int COLS = fixed_cols<C>();
+  constexpr int T = fixed_threads<C, N>();
+  const size_t csize = sizeof(Cx<Si>), W = csize / 8;
+  if (!a.tma || a.S <= 1 || a.ncols % a.S != 0) return false;
+  if (reinterpret_cast<uintptr_t>(data) % 16 != 0 || (a.S * csize) % 16 != 0) return false;
+  const long long runs = a.ncols / a.S, tiles_per_run = (a.S + COLS - 1) / COLS;
+  // grid and tile coordinates are 32-bit signed
+  if (runs > 0x7fffffffLL || tiles_per_run * runs > 0x7fffffffLL || a.S * (long long)W > 0x7fffffffLL) return false;
+  EncodeTiledFn enc = encode_tiled();
+  if (!enc) return false;
+  CUtensorMap tm;
+  const cuuint64_t dim[3] = {(cuuint64_t)(a.S * W), (cuuint64_t)N, (cuuint64_t)runs};
+  const cuuint64_t stride[2] = {(cuuint64_t)(a.S * csize), (cuuint64_t)(a.S * csize * N)};
+  const cuuint32_t box[3] = {(cuuint32_t)(COLS * W), (cuuint32_t)N, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  if (enc(&tm, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, data, dim, stride, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  const unsigned grid = (unsigned)(tiles_per_run * runs);
+  if (sign < 0)
+    fft_tma_kernel<Si, So, C, N, COLS, true, T><<<grid, T, tma_smem<C, N>(), s>>>(tm, a, tiles_per_run);
+  else
+    fft_tma_kernel<Si, So, C, N, COLS, false, T><<<grid, T, tma_smem<C, N>(), s>>>(tm, a, tiles_per_run);
+  return true;
+}
+
+template <typename Si, typename So, typename C>
+bool tma_dispatch(const FftAxis& a, void* data, int sign, cudaStream_t s) {
+  switch (a.n) {
+#define X(N) \
+  case N:    \
+    return tma_launch<Si, So, C, N>(a, data, sign, s);
+    MDFT_FIXED_SIZES(X)
+#undef X
+  }
+  return false;
+}
+
+template <typename Si, typename So, typename C>
+void tma_setup(int n) {
+  switch (n) {
+#define X(N)                                                                                                    \
+  case N:                                                                                                       \
+    allow_max_smem(fft_tma_kernel<Si, So, C, N, fixed_cols<C>(), true, fixed_threads<C, N>()>, tma_smem<C, N>(), \
+                   "fft smem attribute");                                                                       \
+    allow_max_smem(fft_tma_kernel<Si, So, C, N, fixed_cols<C>(), false, fixed_threads<C, N>()>,                 \
+                   tma_smem<C, N>(), "fft smem attribute");                                                     \
+    return;
+    MDFT_FIXED_SIZES(X)
+#undef X
+  }
+}
+
 template <typename Si, typename So, typename C>
 void fft_axis_finish(FftAxis& a) {
+  a.tma = 0;
+  a.err = nullptr;
   if (fixed_supported(a.n)) {
     a.fixed = 1;
     a.cols = fixed_cols<C>();
     fixed_setup<Si, So, C>(a.n, a.smem);
+    if (a.S > 1) {
+      a.err = fft_wait_error_counter();
+      tma_setup<Si, So, C>(a.n);
+      a.tma = 1;
+    }
     return;
   }
   a.fixed = 0;
@@ -592,7 +784,7 @@ void launch_fft_axis(const FftAxis& a, void* data, int sign, cudaStream_t s) {
   }
   clear_stale_error();
   if (a.fixed) {
-    fixed_dispatch<Si, So, C>(a, data, sign, s);
+    if (!tma_dispatch<Si, So, C>(a, data, sign, s)) fixed_dispatch<Si, So, C>(a, data, sign, s);
     launch_check("fft kernel launch");
     return;
   }

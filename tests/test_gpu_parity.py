@@ -359,3 +359,9 @@ def test_batched_plans_equal_single_fields(gpu_lib, n, box, mmax, mrso, prec):
     for b in range(B):
         assert torch.equal(pb[:, b], singles_p[b])
         assert torch.equal(vb[b * o.N:(b + 1) * o.N], singles_v[b])
+
+
+def test_no_copy_wait_timed_out(gpu_lib):
+    """Every asynchronous tile copy of the FFTs above landed in time (a wait
+    that runs out leaves its tile untouched and is counted)."""
+    assert gpu_lib.wait_timeouts() == 0
