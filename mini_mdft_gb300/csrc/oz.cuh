@@ -585,19 +585,7 @@ oz_lane_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
   const Cx<C>* Rt = static_cast<const Cx<C>*>(P.rtab) + (pair >> 5) * (long long)P.nR * 32 + (pair & 31);
 #define RH(l, m, j) Rt[(hoff(l) + ((m) + (l)) * ((l) + 1) + (j)) * 32]
 
-  // this side's projections into the lane's shared column first, the loads
-  // in flight together (one memory round trip instead of one per block)
-  {
-    constexpr int NPC = MRSO > 0 ? oz_np(MMAX, MRSO) : 0;  // compile-time count when known
-    const int npl = MRSO > 0 ? NPC : np;
-#pragma unroll 8
-    for (int ip = 0; ip < npl; ++ip) {
-      const Cx<S> u = p[(long long)ip * N + lown];
-      D[ip * 32 + lane] = mkc<C>(to_compute<C>(u.re), to_compute<C>(u.im));
-    }
-  }
-  // rotation to the q frame (MDFT_Convolution.hpp:427-443), block by block
-  // and in place (a block's inputs are read before its outputs are written):
+  // rotation to the q frame (MDFT_Convolution.hpp:427-443), block by block:
   // D(m, k) = sum_a g_a R(m, a - m, ks k) with ks = +1 on the q side and -1
   // on the -q side.  For j = |k| > 0 one side needs column +j (direct) and
   // the other column -j (mirrored), both from the row Rh(m, ., j).
@@ -608,7 +596,10 @@ oz_lane_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
     for (int mu2 = 0; mu2 <= m / mrso; ++mu2) {
       Cx<C> g[2 * MMAX + 1];
 #pragma unroll
-      for (int a = 0; a <= 2 * m; ++a) g[a] = D[ipx(m, a - m, mu2) * 32 + lane];
+      for (int a = 0; a <= 2 * m; ++a) {
+        const Cx<S> u = p[(long long)ipx(m, a - m, mu2) * N + lown];
+        g[a] = mkc<C>(to_compute<C>(u.re), to_compute<C>(u.im));
+      }
       {  // k = 0: column 0 on both sides
         CAcc<C> x;
         cacc_zero(x);
