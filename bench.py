@@ -482,6 +482,25 @@ FORM_NAMES = {
 }
 
 
+def max_over_ranks(secs, dist, device):
+    """The slowest rank's time (replicas: the job ends when the last one
+    does); barrier, then an all-reduce MAX over the process group."""
+    if not dist:
+        return secs
+    import torch
+    import torch.distributed as tdist
+    tdist.barrier()
+    t = torch.tensor([secs], dtype=torch.float64, device=device)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_value(ws, steps, secs):
+    """Round trips per second of the whole job: every rank runs `steps`
+    replica round trips, the job takes the slowest rank's `secs`."""
+    return ws * steps / secs
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -532,12 +551,8 @@ def run_ours(args):
     torch.cuda.synchronize()
     secs = timed_steps(Ph, K, flush)
     torch.cuda.synchronize()
-    if dist:
-        tdist.barrier()
-        t = torch.tensor([secs], dtype=torch.float64, device="cuda")
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        secs = float(t.item())
-    value = ws * K / secs
+    secs = max_over_ranks(secs, dist, "cuda")
+    value = whole_job_value(ws, K, secs)
     # the other forms, same protocol
     form_secs = {head: secs}
     for f in forms:
@@ -546,9 +561,11 @@ def run_ours(args):
         for _ in range(W):
             step(P[f])
         torch.cuda.synchronize()
-        form_secs[f] = timed_steps(P[f], K, flush)
+        form_secs[f] = max_over_ranks(timed_steps(P[f], K, flush), dist, "cuda")
     # e2e through the C ABI with host buffers, headline form
     e2e_secs, e2e_serial, h2d, d2h = e2e_steps(Ph, K, max(2, W // 2))
+    e2e_secs = max_over_ranks(e2e_secs, dist, "cuda")
+    e2e_serial = max_over_ranks(e2e_serial, dist, "cuda")
     clk = clocks.stop()
 
     st = {f: stage_times(P[f], 10, flush) for f in forms}
@@ -591,7 +608,7 @@ def run_ours(args):
 
     def form_entry(f):
         bytes_rt = algorithmic_bytes(s, 4 if f == "f32" else 8)["round_trip"]
-        e = {"value": ws * K / form_secs[f], "unit": "applies/s", "arithmetic": FORM_NAMES[f],
+        e = {"value": whole_job_value(ws, K, form_secs[f]), "unit": "applies/s", "arithmetic": FORM_NAMES[f],
              "ms_per_step": form_secs[f] / K * 1e3,
              "round_trip_hbm_frac": bytes_rt / (form_secs[f] / K) / 1e9 / hbm_peak,
              "stages_ms": {k: v * 1e3 for k, v in st[f].items()}}
@@ -615,11 +632,11 @@ def run_ours(args):
                       "s~U(0.5,4), seed 2, dq 0.01, nq %d" % I.nq_for(
                           WORKLOAD["n"], WORKLOAD["box"], WORKLOAD["dq"]),
         },
-        "e2e": {"value": ws * K / e2e_secs, "unit": "applies/s",
+        "e2e": {"value": whole_job_value(ws, K, e2e_secs), "unit": "applies/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "copies": "pinned host buffers; H2D, round trip and D2H on three streams, "
                           "double-buffered so copies overlap neighbouring steps",
-                "serial_value": ws * K / e2e_serial},
+                "serial_value": whole_job_value(ws, K, e2e_serial)},
         "gpu_launches": kernels_per_step * K,
         "clocks": clk,
         "roofline": {
