@@ -103,9 +103,7 @@ angl2proj_kernel(const AngPlan P, const S* __restrict__ o, Cx<S>* __restrict__ p
   // Stage the contiguous tile of o (and fold in get_delta_rho if asked).
   const S* src = o + pt0 * no;
   for (int i = tid; i < cnt * no; i += bd) {
-    C v = to_compute<C>(src[i]);
-    if (FROM_XI) v = rho0 * (v * v - C(1));
-    ot[i] = v;
+    ot[i] = FROM_XI ? rho0 * to_compute<C>(xi_sq_minus_one(src[i])) : to_compute<C>(src[i]);
   }
   __syncthreads();
 

@@ -122,9 +122,7 @@ angl2proj_fast_kernel(const AngPlan P, const S* __restrict__ o, Cx<S>* __restric
       const int i = tid + r * A2P_THREADS;
       if (i < n) {
         const int q = i / NO, j = i - q * NO;
-        C x = to_compute<C>(v[r]);
-        if (FROM_XI) x = rho0 * (x * x - C(1));
-        ot[q * LDO + j] = x;
+        ot[q * LDO + j] = FROM_XI ? rho0 * to_compute<C>(xi_sq_minus_one(v[r])) : to_compute<C>(v[r]);
       }
     }
   }

@@ -159,17 +159,30 @@ __host__ __device__ __forceinline__ int clz64(unsigned long long x) {
 #endif
 }
 
-// x -> (hi, lo): hi is x truncated to 24 significant bits, lo the next 24
-// bits (truncated); |x - (hi + lo)| < 2^-47 |x| for 2^-73 <= |x| < 2^128.
-// Smaller |x| keep hi only (x truncated to float, subnormal or zero), larger
-// ones become +-inf; NaN stays NaN.
+// x -> (hi, lo): hi is x rounded to 24 significant bits (to nearest, ties
+// up), lo the signed remainder rounded to 24 bits by the integer-to-float
+// conversion, so |x - (hi + lo)| <= 2^-48 |x| without bias for
+// 2^-73 <= |x| < 2^127 (2^127 <= |x| < 2^128: hi truncated, lo the next 24
+// bits truncated, 2^-47).  Smaller |x| keep hi only (x truncated to float,
+// subnormal or zero), larger ones become +-inf; NaN stays NaN.
 __host__ __device__ __forceinline__ DF df_from_double_bits(double x) {
   const unsigned long long b = bits_of(x);
   const unsigned hi32 = (unsigned)(b >> 32), lo32 = (unsigned)b;
   const unsigned e = (hi32 >> 20) & 0x7ffu;  // biased exponent
   const unsigned sign = hi32 & 0x80000000u;
   const unsigned m23 = ((hi32 & 0x000fffffu) << 3) | (lo32 >> 29);  // top 23 fraction bits
-  if (e >= 950u && e <= 1150u) {
+  if (e >= 950u && e <= 1149u) {
+    // the low 29 fraction bits decide the rounding of hi; a carry out of the
+    // fraction moves into the exponent field by itself
+    const unsigned low = lo32 & 0x1fffffffu;
+    const unsigned up = low >= 0x10000000u ? 1u : 0u;
+    const float h = float_of(sign | (((e - 896u) << 23) + m23 + up));
+    const int r = (int)low - (int)(up << 29);        // |r| <= 2^28, units 2^(e - 1075)
+    const float scale = float_of((e - 948u) << 23);  // 2^(e - 1075), a normal float
+    const float l = (float)r * scale;
+    return DF(h, sign ? -l : l);
+  }
+  if (e == 1150u) {
     const float h = float_of(sign | ((e - 896u) << 23) | m23);
     const unsigned r = lo32 & 0x1fffffffu;  // remaining 29 fraction bits
     float l = 0.f;
@@ -305,6 +318,13 @@ template <typename C>
 __host__ __device__ __forceinline__ Cx<C> cacc_get(const CAcc<C>& s) {
   return mkc<C>(acc_get(s.re), acc_get(s.im));
 }
+
+// xi^2 - 1 of get_delta_rho in the storage type by one fused multiply-add:
+// for xi near 1 the difference cancels, so it is formed before any
+// conversion to the arithmetic type (double-float keeps 48 bits of the
+// small result instead of 48 bits of xi^2).
+__host__ __device__ __forceinline__ double xi_sq_minus_one(double x) { return fma(x, x, -1.0); }
+__host__ __device__ __forceinline__ float xi_sq_minus_one(float x) { return fmaf(x, x, -1.0f); }
 
 // Storage <-> compute conversions (identity unless the compute type is DF).
 template <typename C, typename S>

@@ -55,8 +55,24 @@ static void check_from_double(double x) {
   }
   const long double s = (long double)d.hi + (long double)d.lo;
   const long double err = std::fabs(s - (long double)x);
-  if (err > std::ldexp((long double)ax, -47)) fail("from_double error", x, (double)s, x);
+  // rounded split below 2^127, truncated split in [2^127, 2^128)
+  const int bound = ax < std::ldexp(1.0, 127) ? -48 : -47;
+  if (err > std::ldexp((long double)ax, bound)) fail("from_double error", x, (double)s, x);
   if (d.hi + d.lo != d.hi) fail("from_double not normalised", x, d.lo, 0.0);
+}
+
+// the rounded split carries no bias: the mean signed relative error over many
+// values stays far below the 2^-49 a truncating split would show
+static void check_from_double_unbiased() {
+  long double sum = 0;
+  const int n = 2000000;
+  for (int k = 0; k < n; ++k) {
+    const double x = mdft::double_of((next_u64() & 0x000fffffffffffffull) | (1023ull << 52));  // [1, 2)
+    const DF d = mdft::df_from_double_bits(x);
+    sum += ((long double)d.hi + (long double)d.lo - (long double)x) / (long double)x;
+  }
+  const long double mean = sum / n;
+  if (std::fabs(mean) > std::ldexp(1.0L, -56)) fail("from_double biased", (double)mean, 0, 0);
 }
 
 static void check_to_double(DF a, bool exact_ref) {
@@ -101,6 +117,7 @@ int main() {
       check_from_double(mdft::double_of(b));
       ++n_from;
     }
+  check_from_double_unbiased();
   // df_to_double: normalised pairs over the float exponent range and
   // every gap between hi and lo, zero/subnormal/inf parts, unnormalised pairs
   for (int k = 0; k < 4000000; ++k) {
