@@ -256,10 +256,11 @@ void conv_build(mdft_conv_s* h, const mdft::LucTable& t) {
     // MDFT_Convolution.hpp:449-455 (FP64, host, no contraction), and the
     // singular mid-k flag of :507-509.
     O.npairs_pad = ((long long)h->npairs + 31) / 32 * 32;
-    // R entries per pair: all sum_l (2l+1)^2 for the unsplit FP64 kernel,
-    // the m1 >= 0 half, sum_l (2l+1)(l+1), for the split FP32 / double-float one
+    // R entries per pair: all sum_l (2l+1)^2 complex ones for the unsplit
+    // FP64 kernel; for the split FP32 / double-float one the real factor of
+    // the m1 >= 0 half, sum_l (2l+1)(l+1), and the mmax phase powers (re, im)
     O.nR = std::is_same<T, double>::value ? (g.mmax + 1) * (2 * g.mmax + 1) * (2 * g.mmax + 3) / 3
-                                          : (g.mmax + 1) * (g.mmax + 2) * (4 * g.mmax + 3) / 6;
+                                          : (g.mmax + 1) * (g.mmax + 2) * (4 * g.mmax + 3) / 6 + 2 * g.mmax;
     std::vector<int4> info((size_t)O.npairs_pad, make_int4(0, 0, 0, 0));
     std::vector<T> alpha((size_t)O.npairs_pad, T(0));
     std::vector<double> alpha_d((size_t)O.npairs_pad, 0.0);

@@ -314,9 +314,23 @@ __host__ __device__ __forceinline__ void cacc_macc(CAcc<C>& s, Cx<C> x, Cx<C> y)
   acc_mac(s.im, -x.re, y.im);
   acc_mac(s.im, x.im, y.re);
 }
+// s += x y for a real y: half the products of a complex y
+template <typename C>
+__host__ __device__ __forceinline__ void cacc_mac_r(CAcc<C>& s, Cx<C> x, C y) {
+  acc_mac(s.re, x.re, y);
+  acc_mac(s.im, x.im, y);
+}
 template <typename C>
 __host__ __device__ __forceinline__ Cx<C> cacc_get(const CAcc<C>& s) {
   return mkc<C>(acc_get(s.re), acc_get(s.im));
+}
+// x y as one two-term sum per component
+template <typename C>
+__host__ __device__ __forceinline__ Cx<C> cx_mul(Cx<C> x, Cx<C> y) {
+  CAcc<C> s;
+  cacc_zero(s);
+  cacc_mac(s, x, y);
+  return cacc_get(s);
 }
 
 // xi^2 - 1 of get_delta_rho in the storage type by one fused multiply-add:
@@ -507,11 +521,13 @@ struct OzPlan {
   // Lane-per-pair path: per-pair geometry computed once at plan creation.
   int lane_path;           // 1: oz_lane_kernel, 0: warp-per-pair fallback
   long long npairs_pad;    // npairs rounded up to a multiple of 32
-  int nR;                  // R entries per pair in rtab (full or m1 >= 0 half)
+  int nR;                  // entries per pair in rtab (see oz_build_rtab)
   const int4* pinfo;       // (npairs_pad) lq, lmq, iq, singular (padding: zeros)
   const void* palpha;      // (npairs_pad) T interpolation weight of row iq+1
   const int* ia_start;     // (np) first OZ coefficient of each projection
-  const void* rtab;        // (npairs_pad/32, nR, 32) Cx<T>: R(q) of 32 pairs, lane fastest
+  // (npairs_pad/32, nR, 32), lane fastest: R(q) of 32 pairs as Cx<double>
+  // (FP64 arithmetic), or the real factor and phase powers of R as T
+  const void* rtab;
 };
 template <typename S, typename C>
 void oz_plan_finish(OzPlan& P);

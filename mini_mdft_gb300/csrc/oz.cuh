@@ -472,22 +472,61 @@ __global__ void rot_table_kernel(const OzPlan P, Cx<double>* __restrict__ rt64) 
   rot_recursion(q0, q1, q2, P.mmax, A, B, Cc, D, R);
 }
 
-// Half table of the split lane kernel from the FP64 table: per block of 32
-// pairs the entries Rh(l, m, j) = R(l, m, j), j = 0..l, at hoff(l) +
-// (m + l)(l + 1) + j, converted to C.
+// e^{-i phi} of the frame of rot_recursion: r1_y + i r1_x with r1 = z x q
+// normalised, (0, sign qz, 0) on the z axis and (0, 1, 0) at q = 0.  In that
+// frame R(l, m, m1) = w^m d(l, m, m1) with d real (the Euler factorisation
+// R = e^{-i m phi} d(theta); the third angle is zero).
+__device__ __forceinline__ Cx<double> frame_phase(double q0, double q1, double q2) {
+  double x, y;  // r1 before normalisation
+  if (q0 != 0.0 || q1 != 0.0) {
+    x = -q1;
+    y = q0;
+  } else {
+    x = 0.0;
+    y = q2 == 0.0 ? 1.0 : q2;
+  }
+  const double n = sqrt(x * x + y * y);
+  return mkc<double>(y / n, x / n);
+}
+
+// Table of the split lane kernel from the FP64 table, one thread per padded
+// pair: per block of 32 pairs the real entries d(l, m, j) = Re(w^-m R(l, m, j)),
+// j = 0..l, at hoff(l) + (m + l)(l + 1) + j (the m1 < 0 half follows from
+// d(l, -m, -m1) = (-1)^(m+m1) d(l, m, m1)), then w^k, k = 1..mmax, as
+// (re, im) at hoff(mmax + 1) + 2 (k - 1); all converted to C.
 template <typename C>
-__global__ void rot_table_half(const Cx<double>* __restrict__ full, Cx<C>* __restrict__ half,
-                               long long nblk, int mmax, int nfull, int nhalf) {
-  const long long n = nblk * nhalf * 32;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const long long t = i >> 5, blk = t / nhalf;
-    const int lane = (int)(i & 31), e = (int)(t - blk * nhalf);
-    int l = 0;
-    while (l < mmax && hoff(l + 1) <= e) ++l;
-    const int r = e - hoff(l), m = r / (l + 1) - l, j = r % (l + 1);
-    const long long src = (blk * nfull + roff(l) + (m + l) * (2 * l + 1) + (j + l)) * 32 + lane;
-    half[i] = mkc<C>(to_compute<C>(full[src].re), to_compute<C>(full[src].im));
+__global__ void rot_table_real(const OzPlan P, const Cx<double>* __restrict__ full, C* __restrict__ tab,
+                               int nfull) {
+  const long long pair = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (pair >= P.npairs_pad) return;
+  double q0 = 0, q1 = 0, q2 = 0;
+  if (pair < P.npairs) {
+    const int4 pr = P.pairs[pair];
+    q0 = P.kx[pr.x];
+    q1 = P.ky[pr.y];
+    q2 = P.kz[pr.z];
+  }
+  const Cx<double> w = frame_phase(q0, q1, q2);
+  Cx<double> wp[7];  // w^k, k = 0..mmax (mmax <= 6 on the lane path)
+  wp[0] = mkc<double>(1.0, 0.0);
+  for (int k = 1; k <= P.mmax; ++k)
+    wp[k] = mkc<double>(wp[k - 1].re * w.re - wp[k - 1].im * w.im, wp[k - 1].re * w.im + wp[k - 1].im * w.re);
+  const long long blk = pair >> 5;
+  const int lane = (int)(pair & 31);
+  const Cx<double>* R = full + blk * (long long)nfull * 32 + lane;
+  C* T = tab + blk * (long long)P.nR * 32 + lane;
+  for (int l = 0; l <= P.mmax; ++l)
+    for (int m = -l; m <= l; ++m) {
+      const Cx<double> e = m >= 0 ? conj(wp[m]) : wp[-m];  // w^-m
+      for (int j = 0; j <= l; ++j) {
+        const Cx<double> r = R[(long long)(roff(l) + (m + l) * (2 * l + 1) + (j + l)) * 32];
+        T[(long long)(hoff(l) + (m + l) * (l + 1) + j) * 32] = to_compute<C>(r.re * e.re - r.im * e.im);
+      }
+    }
+  const int nh = hoff(P.mmax + 1);
+  for (int k = 1; k <= P.mmax; ++k) {
+    T[(long long)(nh + 2 * (k - 1)) * 32] = to_compute<C>(wp[k].re);
+    T[(long long)(nh + 2 * (k - 1) + 1) * 32] = to_compute<C>(wp[k].im);
   }
 }
 
@@ -579,16 +618,19 @@ oz_lane_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
   const long long lown = (side ? info.y : info.x) + (long long)blockIdx.y * P.N;
   // the q side does not store at self-paired k-points: the -q store wins
   const bool store = valid && (side == 1 || info.x != info.y);
-  // Half table Rh(l, m, j) = R(l, m, j) for j >= 0; for m1 < 0,
-  // R(l, m, m1) = (-1)^(m+m1) conj Rh(l, -m, -m1).  Both lanes of a pair
-  // read the same entries, so every load serves the two half-warps.
-  const Cx<C>* Rt = static_cast<const Cx<C>*>(P.rtab) + (pair >> 5) * (long long)P.nR * 32 + (pair & 31);
+  // R(l, m, m1) = w^m d(l, m, m1) with w = e^{-i phi} and d real; the table
+  // holds Rh(l, m, j) = d(l, m, j) for j >= 0 (for m1 < 0, d(l, m, m1) =
+  // (-1)^(m+m1) Rh(l, -m, -m1)) and the powers WPOW(k) = w^k.  Both lanes of a
+  // pair read the same entries, so every load serves the two half-warps.
+  const C* Rt = static_cast<const C*>(P.rtab) + (pair >> 5) * (long long)P.nR * 32 + (pair & 31);
 #define RH(l, m, j) Rt[(hoff(l) + ((m) + (l)) * ((l) + 1) + (j)) * 32]
+#define WPOW(k) mkc<C>(Rt[(hoff(MMAX + 1) + 2 * ((k)-1)) * 32], Rt[(hoff(MMAX + 1) + 2 * ((k)-1) + 1) * 32])
 
   // rotation to the q frame (MDFT_Convolution.hpp:427-443), block by block:
-  // D(m, k) = sum_a g_a R(m, a - m, ks k) with ks = +1 on the q side and -1
-  // on the -q side.  For j = |k| > 0 one side needs column +j (direct) and
-  // the other column -j (mirrored), both from the row Rh(m, ., j).
+  // D(m, k) = sum_a g_a R(m, a - m, ks k) = sum_a (g_a w^(a-m)) d(m, a - m, ks k)
+  // with ks = +1 on the q side and -1 on the -q side.  For j = |k| > 0 one
+  // side needs column +j (direct) and the other column -j (mirrored), both
+  // from the row Rh(m, ., j).
 #pragma unroll
   for (int m = 0; m <= MMAX; ++m) {
     const bool flip = side && (m & 1);  // (-1)^m of R(-q) = (-1)^l R(q)
@@ -600,27 +642,32 @@ oz_lane_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
         const Cx<S> u = p[(long long)ipx(m, a - m, mu2) * N + lown];
         g[a] = mkc<C>(to_compute<C>(u.re), to_compute<C>(u.im));
       }
+#pragma unroll
+      for (int t = 1; t <= m; ++t) {
+        const Cx<C> wt = WPOW(t);
+        g[m + t] = cx_mul(g[m + t], wt);
+        g[m - t] = cx_mul(g[m - t], conj(wt));
+      }
       {  // k = 0: column 0 on both sides
         CAcc<C> x;
         cacc_zero(x);
 #pragma unroll
-        for (int b = 0; b <= 2 * m; ++b) cacc_mac(x, g[b], RH(m, b - m, 0));
+        for (int b = 0; b <= 2 * m; ++b) cacc_mac_r(x, g[b], RH(m, b - m, 0));
         Cx<C> v = cacc_get(x);
         if (flip) v = mkc<C>(-v.re, -v.im);
         D[ipx(m, 0, mu2) * 32 + lane] = v;
       }
 #pragma unroll(kOzUnroll<C, MMAX>)
       for (int j = 1; j <= m; ++j) {
-        // direct: sum_b g_b h_b; mirrored: sum_b (-1)^(m+b+j) g_{2m-b} conj(h_b)
+        // direct: sum_b g_b h_b; mirrored: sum_b (-1)^(m+b+j) g_{2m-b} h_b
         CAcc<C> xd, xm;
         cacc_zero(xd);
         cacc_zero(xm);
 #pragma unroll
         for (int b = 0; b <= 2 * m; ++b) {
-          const Cx<C> h = RH(m, b - m, j);
-          cacc_mac(xd, g[b], h);
-          const Cx<C> gm = g[2 * m - b];
-          cacc_macc(xm, ((m + b) & 1) ? mkc<C>(-gm.re, -gm.im) : gm, h);
+          const C h = RH(m, b - m, j);
+          cacc_mac_r(xd, g[b], h);
+          cacc_mac_r(xm, g[2 * m - b], ((m + b) & 1) ? -h : h);
         }
         Cx<C> vd = cacc_get(xd), vm = cacc_get(xm);
         if (j & 1) vm = mkc<C>(-vm.re, -vm.im);
@@ -664,7 +711,8 @@ oz_lane_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
     const bool flip = side && (m & 1);
 #pragma unroll 1
     for (int mu2 = 0; mu2 <= m / mrso; ++mu2) {
-      // rotation back as the OZ outputs appear: out_a += g_k conj R(m, a, ks k)
+      // rotation back as the OZ outputs appear: conj R(m, a', kk) =
+      // w^-a' d(m, a', kk), so acc_a += g_k d(m, a', ks k) and out_a = w^-a' acc_a
       CAcc<C> acc[2 * MMAX + 1];
 #pragma unroll
       for (int a = 0; a <= 2 * m; ++a) cacc_zero(acc[a]);
@@ -700,26 +748,25 @@ oz_lane_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
           }
         }
         const Cx<C> gk = chop(cacc_get(sacc));
-        // conj R(m, a, kk), kk = ks k: conj Rh(m, a, |k|) when kk >= 0, else
-        // (-1)^(a+k) Rh(m, -a, |k|); the row Rh(m, ., |k|) serves both sides
+        // d(m, a', kk), kk = ks k: Rh(m, a', |k|) when kk >= 0, else
+        // (-1)^(a'+k) Rh(m, -a', |k|); the row Rh(m, ., |k|) serves both sides
         const bool direct = side ? (k <= 0) : (k >= 0);
         const bool kodd = (k & 1) != 0;
-        Cx<C> h[2 * MMAX + 1];
+        C h[2 * MMAX + 1];
 #pragma unroll
         for (int b = 0; b <= 2 * m; ++b) h[b] = RH(m, b - m, ak);
 #pragma unroll
         for (int a = 0; a <= 2 * m; ++a) {
-          const Cx<C> hd = h[a], hm = h[2 * m - a];
+          const C hm = h[2 * m - a];
           const bool neg = (((a - m) & 1) != 0) != kodd;
-          Cx<C> r;
-          r.re = direct ? hd.re : (neg ? -hm.re : hm.re);
-          r.im = direct ? -hd.im : (neg ? -hm.im : hm.im);
-          cacc_mac(acc[a], gk, r);
+          cacc_mac_r(acc[a], gk, direct ? h[a] : (neg ? -hm : hm));
         }
       }
 #pragma unroll
       for (int a = 0; a <= 2 * m; ++a) {
         Cx<C> v = cacc_get(acc[a]);
+        if (a > m) v = cx_mul(v, conj(WPOW(a - m)));
+        if (a < m) v = cx_mul(v, WPOW(m - a));
         if (flip) v = mkc<C>(-v.re, -v.im);
         if (side && singular) v = conj(v);
         if (store) p[(long long)ipx(m, a - m, mu2) * N + lown] = mkc<S>(to_storage<S>(v.re), to_storage<S>(v.im));
@@ -729,6 +776,7 @@ oz_lane_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
 #undef OZ_COEF
 #undef OZ_TERM
 #undef RH
+#undef WPOW
 }
 
 // One lane per pair (both sides in one thread): used for FP64 arithmetic,
@@ -939,11 +987,13 @@ void oz_lane_attr(const OzPlan& P) {
 
 template <typename C>
 void oz_build_rtab(const OzPlan& P, DevBuf& rtab) {
-  // the unsplit kernel (FP64) reads the full table, the split kernels the
-  // half table (entries with m1 >= 0)
+  // the unsplit kernel (FP64) reads the full complex table; the split kernels
+  // the real factor d for m1 >= 0 and the powers of the phase w (entries per
+  // pair: sum_l (2l+1)(l+1) + 2 mmax)
   constexpr bool split = split_pairs<C>();
-  const int nfull = nrot(P.mmax), nhalf = hoff(P.mmax + 1);
-  throw_if(P.nR != (split ? nhalf : nfull), "internal: R table size", 4);
+  const int nfull = nrot(P.mmax), nsplit = hoff(P.mmax + 1) + 2 * P.mmax;
+  throw_if(P.nR != (split ? nsplit : nfull), "internal: R table size", 4);
+  throw_if(P.mmax > 6, "internal: R table mmax", 4);
   OzPlan F = P;
   F.nR = nfull;
   DevBuf rt64;
@@ -954,9 +1004,8 @@ void oz_build_rtab(const OzPlan& P, DevBuf& rtab) {
   rot_table_kernel<<<(unsigned)nb, 128>>>(F, target64.as<Cx<double>>());
   launch_check("R(q) table kernel launch");
   if (split) {
-    rtab.alloc(sizeof(Cx<C>) * (size_t)(P.npairs_pad * (long long)nhalf));
-    rot_table_half<C><<<152 * 8, 256>>>(rt64.as<Cx<double>>(), rtab.as<Cx<C>>(), P.npairs_pad / 32,
-                                        P.mmax, nfull, nhalf);
+    rtab.alloc(sizeof(C) * (size_t)(P.npairs_pad * (long long)nsplit));
+    rot_table_real<C><<<(unsigned)nb, 128>>>(P, rt64.as<Cx<double>>(), rtab.as<C>(), nfull);
     launch_check("R(q) table conversion launch");
   }
   cuda_check(cudaDeviceSynchronize(), "R(q) table build");
