@@ -179,13 +179,23 @@ void conv_build(mdft_conv_s* h, const mdft::LucTable& t) {
   h->dq = t.dq;
   h->mnq = mdft::reorder_luc(g, t, need);
   // pair list: reference order kept for the getter, device copy sorted by
-  // the linear index of q (each pair is independent; roles are unchanged)
+  // the linear index of q (each pair is independent; roles are unchanged).
+  // FP32 arithmetic sorts by |q| first: the pairs of a warp then share their
+  // c(|q|) row, which that latency-bound kernel gains more from than it
+  // loses to scattered field accesses (the issue-bound double-float and FP64
+  // kernels lose more than they gain).
   h->pair_list = mdft::gamma_p_map(g.nx, g.ny, g.nz);
   h->npairs = (int)(h->pair_list.size() / 3);
   std::vector<int4> pr(h->npairs);
   for (int i = 0; i < h->npairs; ++i)
     pr[i] = make_int4(h->pair_list[3 * i], h->pair_list[3 * i + 1], h->pair_list[3 * i + 2], 0);
+  constexpr bool by_q = std::is_same<T, float>::value;
+  auto q2 = [&](const int4& a) { return g.kx[a.x] * g.kx[a.x] + g.ky[a.y] * g.ky[a.y] + g.kz[a.z] * g.kz[a.z]; };
   std::sort(pr.begin(), pr.end(), [&](const int4& a, const int4& b) {
+    if (by_q) {
+      const double qa = q2(a), qb = q2(b);
+      if (qa != qb) return qa < qb;
+    }
     const long long la = ((long long)a.x * g.ny + a.y) * g.nz + a.z;
     const long long lb = ((long long)b.x * g.ny + b.y) * g.nz + b.z;
     return la < lb;
