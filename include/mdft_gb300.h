@@ -254,6 +254,45 @@ int mdft_server_wait(mdft_server_t s, long long job_id, void* xi_out, double* ff
  * steps replayed from captured graphs, group steps launched directly. */
 int mdft_server_stats(mdft_server_t s, double* out);
 
+/* ---- Solute external potential and the minimiser --------------------------
+ * The loop around Solver::energy_cproj_mrso (src/mini-mdft.hpp:130-183): the
+ * reference defines its data -- solvent and solute sites
+ * (common/MDFT_Solvent.hpp:410-494, common/MDFT_Solute.hpp:150-200), the
+ * orientation rotation matrices (common/MDFT_Grid.hpp:283-310), qfact
+ * (common/MDFT_Constants.hpp:46-47) -- but computes neither vext nor a
+ * minimiser step; these entry points do, with the formulas of
+ * mini_mdft_gb300/csrc/solver.cu.
+ *
+ * Sites are rows (q [e], sigma [A], epsilon [kJ/mol], x, y, z [A]): solvent
+ * sites in the molecular frame (the reference's Solvent tables), solute sites
+ * in box coordinates.  vext (device, (nx*ny*nz, no) doubles, the layout of
+ * xi) = LJ 12-6 (Lorentz-Berthelot) + qfact q_a q_s / d between every
+ * solvent site of each orientation and every solute site, minimum image,
+ * clamped to [-vmax, vmax] kJ/mol.  Returns when vext is written. */
+int mdft_vext_lj_coulomb(mdft_grid_t grid, const double* solvent_sites, int n_solvent_sites,
+                         const double* solute_sites, int n_solute_sites, double vmax,
+                         double* vext, void* stream);
+
+/* An L-BFGS minimiser of E(xi) = E_id + E_ext + E_exc on one field (batch-1
+ * handles of one grid and precision; xi, vext and the gradient are FP64 in
+ * every precision, the cproj step runs in the handles' precision).  vext
+ * (device, copied; NULL: no external potential), kT [kJ/mol], rho0 and the
+ * get_delta_f prefactor, history: stored curvature pairs (1..32). */
+typedef struct mdft_solver_s* mdft_solver_t;
+int mdft_solver_create(mdft_solver_t* out, mdft_opt_t opt, mdft_conv_t conv, const double* vext,
+                       double kT, double rho0, double prefactor, int history);
+/* E and dE/dxi at xi (device): grad (device, may be NULL), terms (host, 5):
+ * E_total, E_id, E_ext, E_exc, max |dE/dxi|.  Returns when terms are set. */
+int mdft_solver_energy(mdft_solver_t s, const double* xi, double* grad, double* terms, void* stream);
+/* Minimises from xi (device, overwritten with the last accepted iterate)
+ * until max |dE/dxi| <= gtol, |Delta E| <= ftol max(1, |E|), no step along
+ * the search direction lowers E, or max_iter iterations.  trace (host, may be
+ * NULL): (max_iter + 1) rows of the 5 terms, row 0 at the start, row i after
+ * iteration i; iterations (may be NULL): iterations taken. */
+int mdft_solver_minimize(mdft_solver_t s, double* xi, int max_iter, double gtol, double ftol,
+                         double* trace, int* iterations, void* stream);
+int mdft_solver_destroy(mdft_solver_t s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -13,11 +13,13 @@ from .api import (  # noqa: F401
     OrientationProjectionMap,
     OrientationProjectionTransform,
     Server,
+    Solver,
     SpatialGrid,
     get_delta_f,
     get_delta_rho,
     luc_read,
     luc_write,
+    solute_vext,
     wait_timeouts,
 )
 from ._lib import LIB_PATH, lib  # noqa: F401

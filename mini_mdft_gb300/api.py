@@ -434,6 +434,83 @@ class Server:
         return dict(zip(keys, out.tolist()))
 
 
+def solute_vext(spatial_grid, angular_grid, solvent_sites, solute_sites, vmax=100.0, out=None):
+    """External potential of a solute at every grid point and orientation
+    (mdft_vext_lj_coulomb; no counterpart in the reference, which defines the
+    sites but not the potential): LJ 12-6 with Lorentz-Berthelot mixing plus
+    Coulomb (qfact) between every solvent site and every solute site, minimum
+    image, clamped to [-vmax, vmax] kJ/mol.  Sites are rows (q, sigma,
+    epsilon, x, y, z): solvent sites in the molecular frame, solute sites in
+    box coordinates.  Returns (N, ntheta, nphi, npsi) float64 on the GPU."""
+    torch = _torch()
+    sg, ag = spatial_grid, angular_grid
+    g = _GridHandle(sg.m_n_nodes, sg.m_length, ag.m_mmax, ag.m_molrotsymorder)
+    sv = np.ascontiguousarray(solvent_sites, np.float64).reshape(-1, 6)
+    su = np.ascontiguousarray(solute_sites, np.float64).reshape(-1, 6)
+    shape = (g.nx * g.ny * g.nz, g.ntheta, g.nphi, g.npsi)
+    if out is None:
+        out = torch.empty(shape, dtype=torch.float64, device="cuda")
+    _check_field(out, int(np.prod(shape)), (torch.float64,), "vext")
+    check(lib().mdft_vext_lj_coulomb(g.h, _np_d(sv), sv.shape[0], _np_d(su), su.shape[0],
+                                     float(vmax), _dptr(out), _stream()))
+    return out
+
+
+class Solver:
+    """L-BFGS minimiser of the MDFT functional in xi = sqrt(rho/rho0)
+    (mdft_solver_*): E = E_id + E_ext + E_exc, the excess term being the
+    cproj energy of get_delta_f computed by ``opt`` and ``conv`` (single-field
+    handles of one grid and precision).  xi, vext and gradients are float64
+    CUDA tensors (N, ntheta, nphi, npsi) in every precision."""
+
+    TERMS = ("total", "id", "ext", "exc", "gmax")
+
+    def __init__(self, opt, conv, vext=None, kT=None, rho0=None, prefactor=None, history=5):
+        torch = _torch()
+        if kT is None or rho0 is None or prefactor is None:
+            raise MdftError(1, "kT, rho0 and prefactor are required")
+        self._keep = (opt, conv)
+        self.N, self.no = opt.N, opt.no
+        if vext is not None:
+            _check_field(vext, self.N * self.no, (torch.float64,), "vext")
+        h = C.c_void_p()
+        check(lib().mdft_solver_create(C.byref(h), opt.h, conv.h,
+                                       _dptr(vext) if vext is not None else None,
+                                       float(kT), float(rho0), float(prefactor), int(history)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None) and _lib._lib is not None:
+            _lib._lib.mdft_solver_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def energy(self, xi, grad=None):
+        """dict of E_total, E_id, E_ext, E_exc and max |dE/dxi| at xi; the
+        gradient goes to ``grad`` when given."""
+        torch = _torch()
+        _check_field(xi, self.N * self.no, (torch.float64,), "xi")
+        if grad is not None:
+            _check_field(grad, self.N * self.no, (torch.float64,), "grad")
+        t = np.zeros(5, np.float64)
+        check(lib().mdft_solver_energy(self.h, _dptr(xi), _dptr(grad) if grad is not None else None,
+                                       _np_d(t), _stream()))
+        return dict(zip(self.TERMS, t.tolist()))
+
+    def minimize(self, xi, max_iter=50, gtol=1e-5, ftol=0.0):
+        """Minimises in place from xi; returns the (iterations + 1, 5) trace
+        of the terms (row 0 at the start)."""
+        torch = _torch()
+        _check_field(xi, self.N * self.no, (torch.float64,), "xi")
+        trace = np.zeros((int(max_iter) + 1, 5), np.float64)
+        it = C.c_int()
+        check(lib().mdft_solver_minimize(self.h, _dptr(xi), int(max_iter), float(gtol), float(ftol),
+                                         _np_d(trace), C.byref(it), _stream()))
+        return trace[: it.value + 1]
+
+
 def luc_read(path, np_luc, qmax):
     """IO::LucData: (luc_index (5, np_luc) int32, table (np_luc, nq) complex128,
     dq) with the first int(qmax/dq + 0.5) + 2 q rows (mdft_luc_read)."""

@@ -108,6 +108,57 @@ def synthetic_cq(mmax, mrso, nq, dq=0.01, seed=2):
     return idx, np.ascontiguousarray(tab.astype(np.complex128))
 
 
+# Solvent site tables, rows (q [e], sigma [A], epsilon [kJ/mol], x, y, z [A])
+# in the molecular frame (common/MDFT_Solvent.hpp:418-436 spce,
+# :470-494 tip3p); bulk number densities n0 [1/A^3] beside them.
+SPCE_SITES = np.array([[-0.8476, 3.166, 0.65, 0.0, 0.0, 0.0],
+                       [0.4238, 0.0, 0.0, 0.816495, 0.0, 0.5773525],
+                       [0.4238, 0.0, 0.0, -0.816495, 0.0, 0.5773525]])
+SPCE_N0 = 0.0332891
+TIP3P_SITES = np.array([[-0.834, 3.15061, 0.636386, 0.0, 0.0, 0.0],
+                        [0.417, 0.0, 0.0, 0.756950, 0.0, 0.585882],
+                        [0.417, 0.0, 0.0, -0.756950, 0.0, 0.585882]])
+
+
+def kT(temperature=298.0):
+    """kT in kJ/mol (common/MDFT_Thermo.hpp:60)."""
+    return BOLTZ * NAVO * temperature * 1e-3
+
+
+def solvent_constants(n0, mrso=2, temperature=298.0):
+    """(rho0, prefactor) of a solvent of bulk density n0
+    (common/MDFT_Solvent.hpp:366-368, :426-427)."""
+    rho0 = n0 / (8 * math.pi * math.pi / mrso)
+    prefactor = -2 * kT(temperature) * 4 * math.pi * math.pi / mrso / n0
+    return rho0, prefactor
+
+
+def synthetic_solute(n_sites, box, seed=3):
+    """Seeded synthetic solute, rows (q, sigma, epsilon, x, y, z) in box
+    coordinates: positions uniform in the central 10 A cube of the box,
+    sigma ~ U(2.5, 4) A, epsilon ~ U(0.1, 1) kJ/mol, charges ~ N(0, 0.4) e
+    shifted to sum to 0."""
+    rng = np.random.default_rng(seed)
+    pos = np.asarray(box, np.float64)[None, :] / 2 + rng.uniform(-5.0, 5.0, (n_sites, 3))
+    sig = rng.uniform(2.5, 4.0, n_sites)
+    eps = rng.uniform(0.1, 1.0, n_sites)
+    q = rng.normal(0.0, 0.4, n_sites)
+    q = q - q.mean()
+    return np.ascontiguousarray(np.column_stack([q, sig, eps, pos]))
+
+
+def isotropic_cq(mmax, mrso, nq, dq=0.01, amplitude=1e-4, s=1.0):
+    """c(|q|) table with only the (m, n, mu, nu, khi) = 0 entry set, to
+    -amplitude exp(-s q^2): an isotropic, symmetric (c(1,2) = c(2,1)) direct
+    correlation function whose excess energy is convex in delta_rho."""
+    idx = luc_index(mmax, mrso)
+    keep = (idx == 0).all(axis=0)
+    q = np.arange(nq, dtype=np.float64) * dq
+    tab = np.zeros((idx.shape[1], nq), np.complex128)
+    tab[keep, :] = -amplitude * np.exp(-s * q ** 2)
+    return idx, tab
+
+
 def synthetic_delta_rho(N, mmax, mrso, seed=0, dtype=np.float64):
     ntheta, nphi, npsi, _, _ = angular_counts(mmax, mrso)
     rng = np.random.default_rng(seed)

@@ -1,0 +1,163 @@
+"""The solute external potential and the L-BFGS minimiser on the GPU
+(mdft_vext_lj_coulomb, mdft_solver_*), through the C ABI:
+
+* vext equals the oracle's (oracle/solver.py) within 1e-11 of max(1, |v|);
+* the energy terms and gradient equal the oracle's on the same xi, with
+  vexc from the convolution oracle: FP64 and double-float within 1e-12,
+  FP32 within 1e-5 (its convolution is FP32);
+* without the excess term the minimiser reaches the Boltzmann density
+  xi^2 = exp(-vext / kT);
+* the gradient matches central differences of the energy (isotropic c(q),
+  for which it is exact);
+* with a 12-site solute the energies never rise, the gradient falls, and
+  the three forms reach the same minimum."""
+import numpy as np
+import pytest
+
+import oracle as O
+from oracle import solver as OS
+from mini_mdft_gb300 import inputs as I
+
+pytestmark = pytest.mark.gpu
+
+FORMS = ("f64", "f64df", "f32")
+DQ = 0.05
+
+
+def _handles(M, n, box, mmax, mrso, prec, idx, tab):
+    sg, ag = M.SpatialGrid(n, box), M.AngularGrid(mmax, mrso)
+    opt = M.OrientationProjectionTransform(sg, ag, M.OrientationProjectionMap(ag), precision=prec)
+    conv = M.Convolution.from_table(idx, tab, DQ, sg, ag, precision=prec)
+    return sg, ag, opt, conv
+
+
+def test_vext_matches_oracle(gpu_lib):
+    M = gpu_lib
+    n, box, mmax, mrso = (10, 12, 14), (14., 15., 16.), 3, 2
+    sg, ag = M.SpatialGrid(n, box), M.AngularGrid(mmax, mrso)
+    su = I.synthetic_solute(12, box, seed=3)
+    vmax = 100 * I.kT()
+    v = M.solute_vext(sg, ag, I.SPCE_SITES, su, vmax).cpu().numpy().reshape(-1, ag.m_no)
+    vo = OS.vext_lj_coulomb(n, box, ag.m_thetaofntheta, ag.m_nphi, ag.m_npsi, mrso, I.SPCE_SITES, su, vmax)
+    assert np.abs(v - vo).max() <= 1e-11 * max(1.0, np.abs(vo).max())
+    assert (v == vmax).any() and (np.abs(v) < vmax).mean() > 0.5  # cores capped, the rest not
+
+
+@pytest.mark.parametrize("prec", FORMS)
+def test_energy_and_gradient_match_oracle(gpu_lib, prec):
+    import torch
+    M = gpu_lib
+    n, box, mmax, mrso = (8, 8, 8), (10., 10., 10.), 2, 2
+    idx, tab = I.synthetic_cq(mmax, mrso, I.nq_for(n, box, DQ), DQ)
+    sg, ag, opt, conv = _handles(M, n, box, mmax, mrso, prec, idx, tab)
+    g = O.Oracle(n, box, mmax, mrso)
+    g.set_luc(idx, tab, DQ)
+    _, _, w = g.angular()
+    rho0, pref = I.solvent_constants(I.SPCE_N0, mrso)
+    kT = I.kT()
+    su = I.synthetic_solute(4, box, seed=4)
+    vext = OS.vext_lj_coulomb(n, box, ag.m_thetaofntheta, ag.m_nphi, ag.m_npsi, mrso, I.SPCE_SITES, su, 20 * kT)
+    xi = np.random.default_rng(6).uniform(0.8, 1.2, (g.N, g.no))
+    vexc = g.proj2angl(g.conv_execute(g.angl2proj(O.delta_rho(xi, rho0)))).reshape(g.N, g.no)
+    dv = float(np.prod(np.array(box) / np.array(n)))
+    t_o, g_o = OS.energy_terms(xi, vexc, vext, w, kT, rho0, dv, pref)
+    solver = M.Solver(opt, conv, torch.from_numpy(vext).cuda(), kT=kT, rho0=rho0, prefactor=pref)
+    xt = torch.from_numpy(xi).cuda()
+    grad = torch.empty_like(xt)
+    t = solver.energy(xt, grad)
+    tol = 1e-5 if prec == "f32" else 1e-12
+    scale = max(abs(t_o[1]), abs(t_o[2]), abs(t_o[3]))
+    for k, name in enumerate(M.Solver.TERMS[:4]):
+        assert abs(t[name] - t_o[k]) <= tol * scale, name
+    assert np.abs(grad.cpu().numpy() - g_o).max() <= tol * np.abs(g_o).max()
+    assert abs(t["gmax"] - t_o[4]) <= tol * t_o[4]
+
+
+def test_minimizer_reaches_boltzmann_density_without_excess(gpu_lib):
+    import torch
+    M = gpu_lib
+    n, box, mmax, mrso = (8, 8, 8), (12., 12., 12.), 2, 2
+    idx, tab = I.synthetic_cq(mmax, mrso, I.nq_for(n, box, DQ), DQ)
+    tab[:] = 0  # no excess term
+    sg, ag, opt, conv = _handles(M, n, box, mmax, mrso, "f64", idx, tab)
+    rho0, pref = I.solvent_constants(I.SPCE_N0, mrso)
+    kT = I.kT()
+    su = I.synthetic_solute(6, box, seed=5)
+    vext = M.solute_vext(sg, ag, I.SPCE_SITES, su, 5 * kT)
+    xi = torch.ones_like(vext)
+    solver = M.Solver(opt, conv, vext, kT=kT, rho0=rho0, prefactor=pref)
+    # below max |g| ~ 1e-10 the energy change of a step reaches the rounding
+    # of E and the line search ends the run; 1e-9 bounds |ln xi - ln xi_B| by ~1e-6
+    trace = solver.minimize(xi, max_iter=300, gtol=1e-10)
+    assert trace[-1, 4] <= 1e-9
+    assert np.all(np.diff(trace[:, 0]) <= 0)
+    # E depends on xi^2 only (rho = rho0 xi^2): a step may cross to -xi
+    xb = torch.exp(-vext / (2 * kT))
+    assert torch.max(torch.abs(torch.abs(xi) - xb) / xb).item() < 1e-5
+    assert abs(trace[-1, 3]) < 1e-300  # no excess term
+
+
+@pytest.mark.parametrize("prec", ("f64", "f64df"))
+def test_gradient_matches_finite_differences(gpu_lib, prec):
+    import torch
+    M = gpu_lib
+    n, box, mmax, mrso = (12, 12, 12), (14., 14., 14.), 3, 2
+    idx, tab = I.isotropic_cq(mmax, mrso, I.nq_for(n, box, DQ), DQ, amplitude=1e-3)
+    sg, ag, opt, conv = _handles(M, n, box, mmax, mrso, prec, idx, tab)
+    rho0, pref = I.solvent_constants(I.SPCE_N0, mrso)
+    kT = I.kT()
+    vext = M.solute_vext(sg, ag, I.SPCE_SITES, I.synthetic_solute(4, box, seed=8), 20 * kT)
+    solver = M.Solver(opt, conv, vext, kT=kT, rho0=rho0, prefactor=pref)
+    gen = torch.Generator(device="cuda").manual_seed(9)
+    xi = 0.8 + 0.4 * torch.rand(vext.shape, generator=gen, device="cuda", dtype=torch.float64)
+    d = torch.randn(vext.shape, generator=gen, device="cuda", dtype=torch.float64)
+    grad = torch.empty_like(xi)
+    e0 = solver.energy(xi, grad)
+    assert abs(e0["exc"]) > 1e-3 * abs(e0["id"])  # the excess term takes part
+    an = torch.sum(grad * d).item()
+    h = 1e-5
+    fp = solver.energy(xi + h * d)["total"]
+    fm = solver.energy(xi - h * d)["total"]
+    assert abs((fp - fm) / (2 * h) - an) <= 1e-6 * abs(an)
+
+
+def test_minimizer_with_solute_descends_and_forms_agree(gpu_lib):
+    import torch
+    M = gpu_lib
+    n, box, mmax, mrso = (16, 16, 16), (16., 16., 16.), 3, 2
+    idx, tab = I.isotropic_cq(mmax, mrso, I.nq_for(n, box, DQ), DQ, amplitude=1e-3)
+    rho0, pref = I.solvent_constants(I.SPCE_N0, mrso)
+    kT = I.kT()
+    su = I.synthetic_solute(12, box, seed=3)
+    final = {}
+    for prec in FORMS:
+        sg, ag, opt, conv = _handles(M, n, box, mmax, mrso, prec, idx, tab)
+        vext = M.solute_vext(sg, ag, I.SPCE_SITES, su, 100 * kT)
+        solver = M.Solver(opt, conv, vext, kT=kT, rho0=rho0, prefactor=pref, history=7)
+        xi = torch.ones_like(vext)
+        trace = solver.minimize(xi, max_iter=300, gtol=1e-9)
+        assert np.all(np.diff(trace[:, 0]) <= 1e-12 * np.abs(trace[:, 0]).max()), prec
+        assert trace[-1, 4] <= 1e-3 * trace[0, 4], prec
+        assert torch.isfinite(xi).all()
+        final[prec] = trace[-1]
+    assert abs(final["f64df"][0] - final["f64"][0]) <= 1e-9 * abs(final["f64"][0])
+    assert abs(final["f32"][0] - final["f64"][0]) <= 1e-5 * abs(final["f64"][0])
+
+
+def test_solver_argument_errors(gpu_lib):
+    import torch
+    M = gpu_lib
+    n, box, mmax, mrso = (4, 4, 4), (8., 8., 8.), 1, 1
+    idx, tab = I.synthetic_cq(mmax, mrso, I.nq_for(n, box, DQ), DQ)
+    sg, ag, opt, conv = _handles(M, n, box, mmax, mrso, "f64", idx, tab)
+    _, _, opt32, _ = _handles(M, n, box, mmax, mrso, "f32", idx, tab)
+    rho0, pref = I.solvent_constants(I.SPCE_N0, mrso)
+    with pytest.raises(M.MdftError):
+        M.Solver(opt, conv, None, kT=I.kT(), rho0=rho0, prefactor=pref, history=0)
+    with pytest.raises(M.MdftError):
+        M.Solver(opt32, conv, None, kT=I.kT(), rho0=rho0, prefactor=pref)
+    with pytest.raises(M.MdftError):
+        M.solute_vext(sg, ag, I.SPCE_SITES, I.synthetic_solute(2, box), vmax=-1.0)
+    s = M.Solver(opt, conv, None, kT=I.kT(), rho0=rho0, prefactor=pref)
+    with pytest.raises(M.MdftError):
+        s.energy(torch.ones(3, dtype=torch.float64, device="cuda"))
