@@ -49,6 +49,7 @@ def parse_args():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true", help="skip the job-server leg")
+    ap.add_argument("--no-minimizer", action="store_true", help="skip the solute minimiser leg")
     ap.add_argument("--mode", choices=["full", "steps"], default="full",
                     help="steps: only W warm-up + K timed FP64 and FP32 round trips "
                          "(a short, fixed launch sequence for ncu captures)")
@@ -336,6 +337,69 @@ def read_traffic(kernel):
         if m and m.group(1) == kernel:
             return int(m.group(2))
     return None
+
+
+MINIMIZER = dict(n_sites=12, seed=3, vmax_kT=100.0, history=5, iterations=10, amplitude=1e-3)
+
+
+def minimizer_run(prec):
+    """One minimiser run on the headline workload (64^3 / 30 A / mmax 3 /
+    mrso 2): a 12-site synthetic solute (sites uniform in the central 10 A
+    cube, sigma ~ U(2.5, 4) A, epsilon ~ U(0.1, 1) kJ/mol, charges ~ N(0, 0.4) e
+    summing to 0, seed 3) in SPC/E water, vext clamped at 100 kT, and an
+    isotropic c(q) = -1e-3 exp(-q^2) (symmetric, so the gradient is exact).
+    Times the external potential, one energy + gradient evaluation (CUDA
+    events) and MINIMIZER["iterations"] L-BFGS iterations from xi = 1 (host
+    clock around the call: every iteration reads its energies back)."""
+    import torch
+
+    import mini_mdft_gb300 as M
+    from mini_mdft_gb300 import inputs as I
+    n, box, mmax, mrso, dq = (WORKLOAD[k] for k in ("n", "box", "mmax", "mrso", "dq"))
+    idx, tab = I.isotropic_cq(mmax, mrso, I.nq_for(n, box, dq), dq, amplitude=MINIMIZER["amplitude"])
+    sg, ag = M.SpatialGrid(n, box), M.AngularGrid(mmax, mrso)
+    opt = M.OrientationProjectionTransform(sg, ag, M.OrientationProjectionMap(ag), precision=prec)
+    conv = M.Convolution.from_table(idx, tab, dq, sg, ag, precision=prec)
+    rho0, pref = I.solvent_constants(I.SPCE_N0, mrso)
+    kT = I.kT()
+    su = I.synthetic_solute(MINIMIZER["n_sites"], box, seed=MINIMIZER["seed"])
+    vmax = MINIMIZER["vmax_kT"] * kT
+    vext = M.solute_vext(sg, ag, I.SPCE_SITES, su, vmax)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    M.solute_vext(sg, ag, I.SPCE_SITES, su, vmax, out=vext)
+    torch.cuda.synchronize()
+    vext_ms = (time.perf_counter() - t0) * 1e3
+    solver = M.Solver(opt, conv, vext, kT=kT, rho0=rho0, prefactor=pref, history=MINIMIZER["history"])
+    xi = torch.ones_like(vext)
+    grad = torch.empty_like(xi)
+    for _ in range(3):
+        solver.energy(xi, grad)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    reps = 10
+    ev[0].record()
+    for _ in range(reps):
+        solver.energy(xi, grad)
+    ev[1].record()
+    torch.cuda.synchronize()
+    eg_ms = ev[0].elapsed_time(ev[1]) / reps
+    K = MINIMIZER["iterations"]
+    warm = xi.clone()
+    solver.minimize(warm, max_iter=2, gtol=0.0)
+    del warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    trace = solver.minimize(xi, max_iter=K, gtol=0.0)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    it = len(trace) - 1
+    return {"workload": "64^3 grid, box 30 A, mmax 3, mrso 2; 12-site synthetic solute in SPC/E water; "
+                        "isotropic c(q) = -1e-3 exp(-q^2); vext clamped at 100 kT",
+            "form": prec, "history": MINIMIZER["history"], "vext_ms": vext_ms,
+            "energy_gradient_ms": eg_ms, "iterations": it,
+            "ms_per_iteration": el / max(it, 1) * 1e3,
+            "energy_start": float(trace[0, 0]), "energy_end": float(trace[-1, 0]),
+            "gmax_start": float(trace[0, 4]), "gmax_end": float(trace[-1, 4])}
 
 
 SERVING = dict(shapes=[((32, 32, 32), (20.0, 20.0, 20.0), 20), ((64, 64, 64), (30.0, 30.0, 30.0), 4)],
@@ -659,6 +723,8 @@ def run_ours(args):
     }
     if rank == 0 and not args.no_serving:
         out["serving"] = serving_run(head)
+    if rank == 0 and not args.no_minimizer:
+        out["minimizer"] = minimizer_run(head)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         rate, reps, cores, el = cpu_round_trip_rate()
         out["cpu_baseline"] = {"value": rate, "unit": "applies/s", "cores": cores, "kind": "port",

