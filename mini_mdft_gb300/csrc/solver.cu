@@ -37,9 +37,11 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "handles.hpp"
+#include "solver.hpp"
 
 using mdft::DevBuf;
 using mdft::Error;
@@ -440,18 +442,21 @@ __device__ __forceinline__ DF as_df(double a) { return df_from_double_bits(a); }
 __device__ __forceinline__ float as_f(float a) { return a; }
 __device__ __forceinline__ float as_f(double a) { return df_from_double_bits(a).hi; }  // nearest float
 
-// x <- a0 x + c u with c = c0 + c1 S[i1] + c2 S[i2] (slots < 0 left out; a0 = 0
-// does not read x), then S[out] = scale (v . x) when out >= 0.
+// x <- a x + c u with a = (ja >= 0 ? S[ja] : a0) (a = 0 does not read x) and
+// c = c0 + c1 S[i1] + c2 S[i2] (slots < 0 left out), then S[out] = scale (v . x)
+// when out >= 0, with scale = (js1 >= 0 ? S[js1] : sc0) (js2 >= 0 ? S[js2] : 1).
 template <typename TU, typename TV>
 struct PassArgs {
   float* x;
   const TU* u;
   const TV* v;
   long long n;
-  double a0, c0, c1, c2;
+  double a0;
+  int ja;
+  double c0, c1, c2;
   int i1, i2;
-  double scale;
-  int out;
+  double sc0;
+  int js1, js2, out;
   double* S;
   double* part;
   unsigned* counter;
@@ -462,8 +467,9 @@ __global__ void __launch_bounds__(kRedThreads) lbfgs_pass_kernel(const PassArgs<
   double c = A.c0;
   if (A.i1 >= 0) c += A.c1 * A.S[A.i1];
   if (A.i2 >= 0) c += A.c2 * A.S[A.i2];
-  const float cf = (float)c, af = (float)A.a0;
-  const bool rx = A.a0 != 0.0, dot = A.out >= 0;
+  const double a = A.ja >= 0 ? A.S[A.ja] : A.a0;
+  const float cf = (float)c, af = (float)a;
+  const bool rx = a != 0.0, dot = A.out >= 0;
   Acc<DF> acc;
   acc_zero(acc);
   const long long stride = (long long)gridDim.x * blockDim.x;
@@ -493,9 +499,12 @@ __global__ void __launch_bounds__(kRedThreads) lbfgs_pass_kernel(const PassArgs<
   Red<1> r = red_zero<1>();
   r.s[0] = Dd{df_to_double(acc_get(acc)), 0.0};
   double* S = A.S;
-  const int out = A.out;
-  const double scale = A.scale;
-  grid_reduce<1>(r, A.part, A.counter, [S, out, scale](const Red<1>& t) { S[out] = scale * (t.s[0].hi + t.s[0].lo); });
+  const int out = A.out, js1 = A.js1, js2 = A.js2;
+  const double sc0 = A.sc0;
+  grid_reduce<1>(r, A.part, A.counter, [S, out, js1, js2, sc0](const Red<1>& t) {
+    const double scale = (js1 >= 0 ? S[js1] : sc0) * (js2 >= 0 ? S[js2] : 1.0);
+    S[out] = scale * (t.s[0].hi + t.s[0].lo);
+  });
 }
 
 // xn = x + t d (one FP64 FMA per element; d widened exactly from its bits)
@@ -506,11 +515,13 @@ __global__ void __launch_bounds__(256) step_kernel(double* __restrict__ xn, cons
     xn[i] = fma(t, f2d_bits(d[i]), x[i]);
 }
 
-// s = t d, y = gn - g (rounded to FP32); S[o] = s . y, S[o + 1] = y . y
+// s = t d, y = gn - g (rounded to FP32); S[o] = s . y, S[o + 1] = y . y,
+// S[orho] = 1 / (s . y) and S[ogam] = (s . y) / (y . y) when s . y > 1e-12 y . y,
+// else S[orho] = 0 (the pair then drops out of the recursion) and gamma stays
 __global__ void __launch_bounds__(kRedThreads)
 pair_kernel(float* __restrict__ s, float* __restrict__ y, const float* __restrict__ d,
             const double* __restrict__ gn, const double* __restrict__ g, double t, long long n, double* S, int o,
-            double* part, unsigned* counter) {
+            int orho, int ogam, double* part, unsigned* counter) {
   const float tf = (float)t;
   Acc<DF> sy, yy;
   acc_zero(sy);
@@ -541,10 +552,19 @@ pair_kernel(float* __restrict__ s, float* __restrict__ y, const float* __restric
   Red<2> r = red_zero<2>();
   r.s[0] = Dd{df_to_double(acc_get(sy)), 0.0};
   r.s[1] = Dd{df_to_double(acc_get(yy)), 0.0};
-  grid_reduce<2>(r, part, counter, [S, o](const Red<2>& t2) {
-    S[o] = t2.s[0].hi + t2.s[0].lo;
-    S[o + 1] = t2.s[1].hi + t2.s[1].lo;
+  grid_reduce<2>(r, part, counter, [S, o, orho, ogam](const Red<2>& t2) {
+    const double sy = t2.s[0].hi + t2.s[0].lo, yy = t2.s[1].hi + t2.s[1].lo;
+    S[o] = sy;
+    S[o + 1] = yy;
+    const bool ok = yy > 0.0 && sy > 1e-12 * yy;
+    S[orho] = ok ? 1.0 / sy : 0.0;
+    if (ok) S[ogam] = sy / yy;
   });
+}
+
+// a field's scalar block at the start of a run: zero, gamma = 1
+__global__ void lb_init_kernel(double* S, int n, int ogam) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) S[i] = i == ogam ? 1.0 : 0.0;
 }
 
 __global__ void __launch_bounds__(256) to_float_kernel(float* __restrict__ y, const double* __restrict__ x,
@@ -598,6 +618,290 @@ std::vector<double> orientation_rotations(const Grid& g) {
 }  // namespace
 }  // namespace mdft
 
+// ---- host side ---------------------------------------------------------------
+namespace mdft {
+
+namespace {
+void launch_ok(const char* what) {
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) throw Error(MDFT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+}  // namespace
+
+size_t reduction_scratch_bytes() { return sizeof(double) * kRedBlocks * 7 + 256; }
+
+void to_float(float* y, const double* x, long long n, cudaStream_t s) {
+  to_float_kernel<<<stream_blocks(n), 256, 0, s>>>(y, x, n);
+  launch_ok("xi conversion launch");
+}
+
+void vext_compute(const Grid& g, const double* sv_sites, int n_solvent, const double* su_sites, int n_solute,
+                  double vmax, double* vext, cudaStream_t s) {
+  throw_if(!vext || !sv_sites || (n_solute > 0 && !su_sites), "NULL argument");
+  throw_if(n_solvent < 1 || n_solute < 0, "site counts must be >= 1 (solvent) and >= 0 (solute)");
+  throw_if(!(vmax > 0), "vmax must be positive");
+  const int nsv = n_solvent, nsu = n_solute;
+  const long double qf = qfact();
+  auto df2 = [](long double v) {
+    const float h = (float)v;
+    return make_float2(h, (float)(v - (long double)h));
+  };
+  std::vector<int> origin, offset;  // solvent sites at the molecular origin, the others
+  for (int a = 0; a < nsv; ++a) {
+    const double* A = sv_sites + 6 * a;
+    throw_if(A[1] < 0 || A[2] < 0, "sigma and epsilon must be >= 0");
+    (A[3] == 0.0 && A[4] == 0.0 && A[5] == 0.0 ? origin : offset).push_back(a);
+  }
+  for (int t = 0; t < nsu; ++t)
+    throw_if(su_sites[6 * t + 1] < 0 || su_sites[6 * t + 2] < 0, "sigma and epsilon must be >= 0");
+  auto pairs = [&](const std::vector<int>& sites) {
+    std::vector<float2> pc((size_t)3 * std::max<size_t>(sites.size(), 1) * std::max(nsu, 1));
+    for (size_t j = 0; j < sites.size(); ++j)
+      for (int t = 0; t < nsu; ++t) {
+        const double* A = sv_sites + 6 * sites[j];
+        const double* B = su_sites + 6 * t;
+        const long double eps = std::sqrt((long double)A[2] * B[2]), sig = 0.5L * ((long double)A[1] + B[1]);
+        float2* c = pc.data() + 3 * (j * nsu + t);
+        c[0] = df2(4.0L * eps);
+        c[1] = df2(sig * sig);
+        c[2] = df2(qf * A[0] * B[0]);
+      }
+    return pc;
+  };
+  const std::vector<float2> pof = pairs(offset), p0 = pairs(origin);
+  const std::vector<double> rot = orientation_rotations(g);
+  std::vector<float2> off((size_t)3 * g.no * std::max<size_t>(offset.size(), 1));
+  for (int o = 0; o < g.no; ++o)
+    for (size_t j = 0; j < offset.size(); ++j) {
+      const double* R = rot.data() + 9 * (size_t)o;
+      const double* x = sv_sites + 6 * offset[j] + 3;
+      for (int k = 0; k < 3; ++k)
+        off[3 * (o * offset.size() + j) + k] =
+            df2((long double)R[3 * k] * x[0] + (long double)R[3 * k + 1] * x[1] + (long double)R[3 * k + 2] * x[2]);
+    }
+  std::vector<float2> su((size_t)3 * std::max(nsu, 1));
+  for (int t = 0; t < nsu; ++t)
+    for (int k = 0; k < 3; ++k) su[3 * t + k] = df2(su_sites[6 * t + 3 + k]);
+  const int nn[3] = {g.nx, g.ny, g.nz};
+  const double ll[3] = {g.lx, g.ly, g.lz};
+  std::vector<float2> coord[3];
+  for (int k = 0; k < 3; ++k) {
+    coord[k].resize(nn[k]);
+    for (int i = 0; i < nn[k]; ++i) coord[k][i] = df2((long double)i * ll[k] / nn[k]);
+  }
+  DevBuf dcx, dcy, dcz, doff, dsu, dpof, dp0, dv0;
+  dcx.upload(coord[0].data(), sizeof(float2) * coord[0].size());
+  dcy.upload(coord[1].data(), sizeof(float2) * coord[1].size());
+  dcz.upload(coord[2].data(), sizeof(float2) * coord[2].size());
+  doff.upload(off.data(), sizeof(float2) * off.size());
+  dsu.upload(su.data(), sizeof(float2) * su.size());
+  dpof.upload(pof.data(), sizeof(float2) * pof.size());
+  dp0.upload(p0.data(), sizeof(float2) * p0.size());
+  dv0.alloc(sizeof(float2) * (size_t)g.N());
+  VextPlan P{};
+  P.nx = g.nx;
+  P.ny = g.ny;
+  P.nz = g.nz;
+  P.no = g.no;
+  P.nof = (int)offset.size();
+  P.n0 = (int)origin.size();
+  P.nsu = nsu;
+  for (int k = 0; k < 3; ++k) {
+    P.L[k] = df2(ll[k]);
+    P.il[k] = (float)(1.0 / ll[k]);
+  }
+  P.vmax = vmax;
+  P.cx = dcx.as<float2>();
+  P.cy = dcy.as<float2>();
+  P.cz = dcz.as<float2>();
+  P.off = doff.as<float2>();
+  P.su = dsu.as<float2>();
+  P.pof = dpof.as<float2>();
+  P.p0 = dp0.as<float2>();
+  P.v0 = dv0.as<float2>();
+  vext_origin_kernel<<<stream_blocks(g.N()), 256, 0, s>>>(P);
+  launch_ok("vext kernel launch");
+  const long long n = g.N() * (long long)g.no;
+  vext_kernel<<<stream_blocks(n), 256, 0, s>>>(P, vext);
+  launch_ok("vext kernel launch");
+  // the tables are freed on return: finish first
+  cuda_check(cudaStreamSynchronize(s), "vext kernel");
+}
+
+void energy_grad(const EgConst& c, const double* xi, const void* vexc, bool vexc_f32, const double* vext,
+                 const double* w, double* grad, long long n, int no, double* out, void* scratch, cudaStream_t s) {
+  EgArgs A{};
+  A.xi = xi;
+  A.vexc = vexc;
+  A.vext = vext;
+  A.w = w;
+  A.g = grad;
+  A.n = n;
+  A.no = no;
+  A.kT = c.kT;
+  A.rho0 = c.rho0;
+  A.dv = c.dv;
+  A.prefactor = c.prefactor;
+  auto split = [](long double v, float& hi, float& lo) {
+    hi = (float)v;
+    lo = (float)(v - (long double)hi);
+  };
+  split(c.kT, A.kh, A.kl);
+  split((long double)c.rho0 * c.dv, A.ch, A.cl);
+  split(2.0L * c.prefactor * c.rho0, A.xh, A.xl);
+  split(0.693147180559945309417232121458176568L, A.ln2h, A.ln2l);
+  for (int k = 0; k < 10; ++k) split(1.0L / (2 * k + 1), A.ah[k], A.al[k]);
+  A.out = out;
+  A.part = static_cast<double*>(scratch);
+  A.counter = reinterpret_cast<unsigned*>(static_cast<double*>(scratch) + kRedBlocks * 7);
+  const size_t smem = (sizeof(double) + sizeof(float2)) * (size_t)no;
+  throw_if(smem > 48 * 1024, "too many orientations for the energy kernel", MDFT_ERR_UNSUPPORTED);
+  if (vexc_f32)
+    eg_kernel<float><<<red_blocks(n, 152 * 4), kRedThreads, smem, s>>>(A);
+  else
+    eg_kernel<double><<<red_blocks(n, 152 * 4), kRedThreads, smem, s>>>(A);
+  launch_ok("energy kernel launch");
+}
+
+// ---- L-BFGS state machine ------------------------------------------------------
+void Lbfgs::bind(const Bufs& b, long long n, int m) {
+  b_ = b;
+  n_ = n;
+  m_ = m;
+}
+
+template <typename TU, typename TV>
+void Lbfgs::pass(float* x, const TU* u, const TV* v, double a0, int ja, double c1, int i1, double c2, int i2,
+                 double sc0, int js1, int js2, int out, cudaStream_t s) {
+  double* part = static_cast<double*>(b_.scratch);
+  PassArgs<TU, TV> A{x,  u,   v,   n_,  a0,   ja,  0.0, c1,   c2,
+                     i1, i2,  sc0, js1, js2, out, b_.S, part, reinterpret_cast<unsigned*>(part + kRedBlocks * 7)};
+  lbfgs_pass_kernel<TU, TV><<<red_blocks(n_), kRedThreads, 0, s>>>(A);
+  launch_ok("L-BFGS pass launch");
+}
+
+// d = -H g by the two-loop recursion over the nh_ stored pairs; S[gd] = g . d.
+// Every coefficient comes from the device scalars: alpha_i = rho_i (s_i . q),
+// beta_i = rho_i (y_i . r), gamma of the newest accepted pair.
+void Lbfgs::direction(cudaStream_t s) {
+  float* d = b_.d;
+  const double* g = b_.g;
+  auto hs = [&](int i) { return b_.hs + (size_t)i * n_; };
+  auto hy = [&](int i) { return b_.hy + (size_t)i * n_; };
+  // q = -g (c = -1 from c1 with no slot: c = c0 + c1 S[i1]; c0 is 0, so use i1 < 0 and c1 unused)
+  auto neg_g = [&](const auto* v, double sc0, int js1, int js2, int out) {
+    double* part = static_cast<double*>(b_.scratch);
+    using TV = std::remove_const_t<std::remove_pointer_t<decltype(v)>>;
+    PassArgs<double, TV> A{d,  g,   v,   n_,  0.0, -1,  -1.0, 0.0,  0.0,
+                           -1, -1,  sc0, js1, js2, out, b_.S, part, reinterpret_cast<unsigned*>(part + kRedBlocks * 7)};
+    lbfgs_pass_kernel<double, TV><<<red_blocks(n_), kRedThreads, 0, s>>>(A);
+    launch_ok("L-BFGS pass launch");
+  };
+  if (nh_ == 0) {
+    neg_g(g, 1.0, -1, -1, gd());
+    return;
+  }
+  auto idx = [&](int j) { return ((head_ - 1 - j) % m_ + m_) % m_; };  // j = 0: newest
+  neg_g(hs(idx(0)), 0.0, rho(idx(0)), -1, alpha(idx(0)));  // alpha_newest = rho (s . q)
+  for (int j = 0; j < nh_; ++j) {
+    const int i = idx(j);
+    if (j + 1 < nh_) {  // q -= alpha_i y_i; alpha_next = rho_next (s_next . q)
+      const int nx = idx(j + 1);
+      pass(d, hy(i), hs(nx), 1.0, -1, -1.0, alpha(i), 0.0, -1, 0.0, rho(nx), -1, alpha(nx), s);
+    } else {  // last: beta_oldest = rho_oldest gamma (y_oldest . q)
+      pass(d, hy(i), hy(i), 1.0, -1, -1.0, alpha(i), 0.0, -1, 0.0, rho(i), gamma(), beta(0), s);
+    }
+  }
+  for (int j = 0; j < nh_; ++j) {  // oldest first: r = (gamma on the first pass) r + (alpha_i - beta_i) s_i
+    const int i = idx(nh_ - 1 - j);
+    const int ja = j == 0 ? gamma() : -1;
+    if (j + 1 < nh_) {
+      const int nx = idx(nh_ - 2 - j);
+      pass(d, hs(i), hy(nx), 1.0, ja, 1.0, alpha(i), -1.0, beta(j), 0.0, rho(nx), -1, beta(j + 1), s);
+    } else {
+      pass(d, hs(i), g, 1.0, ja, 1.0, alpha(i), -1.0, beta(j), 1.0, -1, -1, gd(), s);
+    }
+  }
+}
+
+void Lbfgs::step(cudaStream_t s) {
+  step_kernel<<<stream_blocks(n_), 256, 0, s>>>(b_.xt, b_.x, b_.d, t_, n_);
+  launch_ok("step kernel launch");
+}
+
+void Lbfgs::start(double gtol, double ftol, int max_iter, cudaStream_t s) {
+  gtol_ = gtol;
+  ftol_ = ftol;
+  max_iter_ = max_iter;
+  nh_ = head_ = ls_ = iter_ = 0;
+  first_ = true;
+  status_ = kRunning;
+  trace_.clear();
+  lb_init_kernel<<<1, 128, 0, s>>>(b_.S, nscalars(m_), gamma());
+  launch_ok("L-BFGS init launch");
+}
+
+bool Lbfgs::on_eval(const double* tail, cudaStream_t s) {
+  const double c1 = 1e-4, max_first_step = 0.1;
+  const int max_ls = 40;
+  const double gdv = tail[0];
+  const double* Et = tail + 3;
+  if (!first_) {
+    if (!(gdv < 0.0)) {  // not a descent direction (rounding): restart from -g
+      nh_ = 0;
+      direction(s);
+      t_ = std::min(1.0, max_first_step / E_[4]);
+      ls_ = 0;
+      step(s);
+      return false;
+    }
+    if (!(std::isfinite(Et[0]) && Et[0] <= E_[0] + c1 * t_ * gdv)) {
+      t_ *= 0.5;
+      if (++ls_ > max_ls) {  // no decrease along the direction: end at x
+        status_ = kStalled;
+        return true;
+      }
+      step(s);
+      return false;
+    }
+    // accepted: curvature pair into the ring slot head_
+    pair_kernel<<<red_blocks(n_), kRedThreads, 0, s>>>(
+        b_.hs + (size_t)head_ * n_, b_.hy + (size_t)head_ * n_, b_.d, b_.gt, b_.g, t_, n_, b_.S, gd() + 1, rho(head_),
+        gamma(), static_cast<double*>(b_.scratch),
+        reinterpret_cast<unsigned*>(static_cast<double*>(b_.scratch) + kRedBlocks * 7));
+    launch_ok("pair kernel launch");
+    head_ = (head_ + 1) % m_;
+    nh_ = std::min(nh_ + 1, m_);
+    ++iter_;
+  }
+  const double Eprev = E_[0];
+  std::copy(Et, Et + 5, E_);
+  trace_.insert(trace_.end(), Et, Et + 5);
+  cuda_check(cudaMemcpyAsync(b_.x, b_.xt, sizeof(double) * (size_t)n_, cudaMemcpyDeviceToDevice, s), "iterate copy");
+  cuda_check(cudaMemcpyAsync(b_.g, b_.gt, sizeof(double) * (size_t)n_, cudaMemcpyDeviceToDevice, s),
+             "gradient copy");
+  if (E_[4] <= gtol_) {
+    status_ = kConverged;
+    return true;
+  }
+  if (!first_ && std::fabs(Eprev - E_[0]) <= ftol_ * std::max(1.0, std::fabs(E_[0]))) {
+    status_ = kFlat;
+    return true;
+  }
+  if (iter_ >= max_iter_) {
+    status_ = kMaxIter;
+    return true;
+  }
+  direction(s);
+  t_ = nh_ == 0 ? std::min(1.0, max_first_step / E_[4]) : 1.0;
+  first_ = false;
+  ls_ = 0;
+  step(s);
+  return false;
+}
+
+}  // namespace mdft
+
 // ---- solver handle -----------------------------------------------------------
 struct mdft_solver_s {
   mdft_opt_s* opt = nullptr;
@@ -605,21 +909,10 @@ struct mdft_solver_s {
   int prec = 0, device = 0, m = 5;
   long long N = 0, n = 0;
   int no = 0, np = 0;
-  double kT = 0, rho0 = 0, prefactor = 0, dv = 0;
+  mdft::EgConst c{};
   bool has_vext = false;
-  mdft::EgArgs eg{};  // constant part of the energy kernel's arguments
-  DevBuf vext, w, p, vexc, xf, ga, gb, xa, d, hs, hy, scal, energy, part, counter;
-  // L-BFGS history (ring of m pairs): rho_i = 1 / (s_i . y_i), gamma of the newest
-  std::vector<double> rho;
-  int nh = 0, head = 0;
-  double gamma = 1.0;
-  float* hs_at(int i) const { return hs.as<float>() + (size_t)i * n; }
-  float* hy_at(int i) const { return hy.as<float>() + (size_t)i * n; }
-  // scalar slots: alpha_i at i < m, then two beta slots, g.d, s.y, y.y
-  int ALPHA(int i) const { return i; }
-  int BETA(int j) const { return m + (j & 1); }
-  int GD() const { return m + 2; }
-  int SY() const { return m + 3; }
+  DevBuf vext, w, p, vexc, xf, x, xt, g, gt, d, hs, hy, S, scratch;
+  mdft::Lbfgs lb;
 };
 
 namespace {
@@ -640,91 +933,18 @@ int solver_guard(F&& f) {
   }
 }
 
-void launch_ok(const char* what) {
-  const cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) throw Error(MDFT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
-}
-
-template <typename TU, typename TV>
-void pass(mdft_solver_s* h, float* x, const TU* u, const TV* v, double a0, double c0, double c1, int i1, double c2,
-          int i2, double scale, int out, cudaStream_t s) {
-  mdft::PassArgs<TU, TV> A{x,     u,   v,           h->n, a0, c0, c1, c2, i1, i2, scale, out, h->scal.as<double>(),
-                           h->part.as<double>(), h->counter.as<unsigned>()};
-  mdft::lbfgs_pass_kernel<TU, TV><<<mdft::red_blocks(h->n), mdft::kRedThreads, 0, s>>>(A);
-  launch_ok("L-BFGS pass launch");
-}
-
-// E(x) and its gradient into g; the energies land in h->energy on the device
-void evaluate(mdft_solver_s* h, const double* x, double* g, cudaStream_t s) {
+// E(x) and its gradient into g; the 5 terms to out (device)
+void evaluate(mdft_solver_s* h, const double* x, double* g, double* out, cudaStream_t s) {
   const void* xin = x;
   if (h->prec == MDFT_F32) {
-    mdft::to_float_kernel<<<mdft::stream_blocks(h->n), 256, 0, s>>>(h->xf.as<float>(), x, h->n);
-    launch_ok("xi conversion launch");
+    mdft::to_float(h->xf.as<float>(), x, h->n, s);
     xin = h->xf.ptr;
   }
-  mdft::detail::angl2proj_fields(h->opt, xin, true, h->rho0, h->p.ptr, 1, s);
+  mdft::detail::angl2proj_fields(h->opt, xin, true, h->c.rho0, h->p.ptr, 1, s);
   mdft::detail::execute_fields(h->conv, h->p.ptr, 1, s);
   mdft::detail::proj2angl_fields(h->opt, h->p.ptr, h->vexc.ptr, 1, s);
-  mdft::EgArgs A = h->eg;
-  A.xi = x;
-  A.vexc = h->vexc.ptr;
-  A.vext = h->has_vext ? h->vext.as<double>() : nullptr;
-  A.g = g;
-  const size_t smem = (sizeof(double) + sizeof(float2)) * (size_t)h->no;
-  if (h->prec == MDFT_F32)
-    mdft::eg_kernel<float><<<mdft::red_blocks(h->n, 152 * 4), mdft::kRedThreads, smem, s>>>(A);
-  else
-    mdft::eg_kernel<double><<<mdft::red_blocks(h->n, 152 * 4), mdft::kRedThreads, smem, s>>>(A);
-  launch_ok("energy kernel launch");
-}
-
-void read_energy(mdft_solver_s* h, double* terms, cudaStream_t s) {
-  cuda_check(cudaMemcpyAsync(terms, h->energy.ptr, 5 * sizeof(double), cudaMemcpyDeviceToHost, s),
-             "energy read-back");
-  cuda_check(cudaStreamSynchronize(s), "solver stream");
-}
-
-double read_scalar(mdft_solver_s* h, int slot, cudaStream_t s) {
-  double v = 0;
-  cuda_check(cudaMemcpyAsync(&v, h->scal.as<double>() + slot, sizeof(double), cudaMemcpyDeviceToHost, s),
-             "scalar read-back");
-  cuda_check(cudaStreamSynchronize(s), "solver stream");
-  return v;
-}
-
-// d = -H g by the two-loop recursion over the h->nh stored pairs; returns g . d
-double direction(mdft_solver_s* h, const double* g, cudaStream_t s) {
-  float* d = h->d.as<float>();
-  const int m = h->m, nh = h->nh;
-  if (nh == 0) {
-    pass(h, d, g, g, 0.0, -1.0, 0, -1, 0, -1, 1.0, h->GD(), s);
-    return read_scalar(h, h->GD(), s);
-  }
-  auto idx = [&](int j) { return ((h->head - 1 - j) % m + m) % m; };  // j = 0: newest
-  // q = -g; alpha_newest = rho (s . q)
-  pass(h, d, g, h->hs_at(idx(0)), 0.0, -1.0, 0, -1, 0, -1, h->rho[idx(0)], h->ALPHA(idx(0)), s);
-  for (int j = 0; j < nh; ++j) {
-    const int i = idx(j);
-    if (j + 1 < nh) {  // q -= alpha_i y_i; alpha_next = rho_next (s_next . q)
-      const int nx = idx(j + 1);
-      pass(h, d, h->hy_at(i), h->hs_at(nx), 1.0, 0.0, -1.0, h->ALPHA(i), 0, -1, h->rho[nx], h->ALPHA(nx), s);
-    } else {  // last: beta_oldest = rho_oldest gamma (y_oldest . q)
-      pass(h, d, h->hy_at(i), h->hy_at(i), 1.0, 0.0, -1.0, h->ALPHA(i), 0, -1, h->rho[i] * h->gamma, h->BETA(0),
-           s);
-    }
-  }
-  for (int j = 0; j < nh; ++j) {  // oldest first: r = (gamma) r + (alpha_i - beta_i) s_i
-    const int i = idx(nh - 1 - j);
-    const double a0 = j == 0 ? h->gamma : 1.0;
-    if (j + 1 < nh) {
-      const int nx = idx(nh - 2 - j);
-      pass(h, d, h->hs_at(i), h->hy_at(nx), a0, 0.0, 1.0, h->ALPHA(i), -1.0, h->BETA(j), h->rho[nx],
-           h->BETA(j + 1), s);
-    } else {
-      pass(h, d, h->hs_at(i), g, a0, 0.0, 1.0, h->ALPHA(i), -1.0, h->BETA(j), 1.0, h->GD(), s);
-    }
-  }
-  return read_scalar(h, h->GD(), s);
+  mdft::energy_grad(h->c, x, h->vexc.ptr, h->prec == MDFT_F32, h->has_vext ? h->vext.as<double>() : nullptr,
+                    h->w.as<double>(), g, h->n, h->no, out, h->scratch.ptr, s);
 }
 
 }  // namespace
@@ -734,98 +954,9 @@ extern "C" {
 int mdft_vext_lj_coulomb(mdft_grid_t grid, const double* solvent_sites, int n_solvent_sites,
                          const double* solute_sites, int n_solute_sites, double vmax, double* vext, void* stream) {
   return solver_guard([&] {
-    throw_if(!grid || !vext, "NULL argument");
-    throw_if(n_solvent_sites < 1 || n_solute_sites < 0, "site counts must be >= 1 (solvent) and >= 0 (solute)");
-    throw_if(!solvent_sites || (n_solute_sites > 0 && !solute_sites), "NULL argument");
-    throw_if(!(vmax > 0), "vmax must be positive");
-    const mdft::Grid& g = grid->g;
-    const int nsv = n_solvent_sites, nsu = n_solute_sites;
-    const long double qf = mdft::qfact();
-    auto df2 = [](long double v) {
-      const float h = (float)v;
-      return make_float2(h, (float)(v - (long double)h));
-    };
-    std::vector<int> origin, offset;  // solvent sites at the molecular origin, the others
-    for (int a = 0; a < nsv; ++a) {
-      const double* A = solvent_sites + 6 * a;
-      throw_if(A[1] < 0 || A[2] < 0, "sigma and epsilon must be >= 0");
-      (A[3] == 0.0 && A[4] == 0.0 && A[5] == 0.0 ? origin : offset).push_back(a);
-    }
-    for (int t = 0; t < nsu; ++t)
-      throw_if(solute_sites[6 * t + 1] < 0 || solute_sites[6 * t + 2] < 0, "sigma and epsilon must be >= 0");
-    auto pairs = [&](const std::vector<int>& sites) {
-      std::vector<float2> pc((size_t)3 * std::max<size_t>(sites.size(), 1) * std::max(nsu, 1));
-      for (size_t j = 0; j < sites.size(); ++j)
-        for (int t = 0; t < nsu; ++t) {
-          const double* A = solvent_sites + 6 * sites[j];
-          const double* B = solute_sites + 6 * t;
-          const long double eps = std::sqrt((long double)A[2] * B[2]), sig = 0.5L * ((long double)A[1] + B[1]);
-          float2* c = pc.data() + 3 * (j * nsu + t);
-          c[0] = df2(4.0L * eps);
-          c[1] = df2(sig * sig);
-          c[2] = df2(qf * A[0] * B[0]);
-        }
-      return pc;
-    };
-    const std::vector<float2> pof = pairs(offset), p0 = pairs(origin);
-    const std::vector<double> rot = mdft::orientation_rotations(g);
-    std::vector<float2> off((size_t)3 * g.no * std::max<size_t>(offset.size(), 1));
-    for (int o = 0; o < g.no; ++o)
-      for (size_t j = 0; j < offset.size(); ++j) {
-        const double* R = rot.data() + 9 * (size_t)o;
-        const double* x = solvent_sites + 6 * offset[j] + 3;
-        for (int k = 0; k < 3; ++k)
-          off[3 * (o * offset.size() + j) + k] =
-              df2((long double)R[3 * k] * x[0] + (long double)R[3 * k + 1] * x[1] + (long double)R[3 * k + 2] * x[2]);
-      }
-    std::vector<float2> su((size_t)3 * std::max(nsu, 1));
-    for (int t = 0; t < nsu; ++t)
-      for (int k = 0; k < 3; ++k) su[3 * t + k] = df2(solute_sites[6 * t + 3 + k]);
-    const int nn[3] = {g.nx, g.ny, g.nz};
-    const double ll[3] = {g.lx, g.ly, g.lz};
-    std::vector<float2> coord[3];
-    for (int k = 0; k < 3; ++k) {
-      coord[k].resize(nn[k]);
-      for (int i = 0; i < nn[k]; ++i) coord[k][i] = df2((long double)i * ll[k] / nn[k]);
-    }
-    DevBuf dcx, dcy, dcz, doff, dsu, dpof, dp0, dv0;
-    dcx.upload(coord[0].data(), sizeof(float2) * coord[0].size());
-    dcy.upload(coord[1].data(), sizeof(float2) * coord[1].size());
-    dcz.upload(coord[2].data(), sizeof(float2) * coord[2].size());
-    doff.upload(off.data(), sizeof(float2) * off.size());
-    dsu.upload(su.data(), sizeof(float2) * su.size());
-    dpof.upload(pof.data(), sizeof(float2) * pof.size());
-    dp0.upload(p0.data(), sizeof(float2) * p0.size());
-    dv0.alloc(sizeof(float2) * (size_t)g.N());
-    mdft::VextPlan P{};
-    P.nx = g.nx;
-    P.ny = g.ny;
-    P.nz = g.nz;
-    P.no = g.no;
-    P.nof = (int)offset.size();
-    P.n0 = (int)origin.size();
-    P.nsu = nsu;
-    for (int k = 0; k < 3; ++k) {
-      P.L[k] = df2(ll[k]);
-      P.il[k] = (float)(1.0 / ll[k]);
-    }
-    P.vmax = vmax;
-    P.cx = dcx.as<float2>();
-    P.cy = dcy.as<float2>();
-    P.cz = dcz.as<float2>();
-    P.off = doff.as<float2>();
-    P.su = dsu.as<float2>();
-    P.pof = dpof.as<float2>();
-    P.p0 = dp0.as<float2>();
-    P.v0 = dv0.as<float2>();
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    mdft::vext_origin_kernel<<<mdft::stream_blocks(g.N()), 256, 0, s>>>(P);
-    launch_ok("vext kernel launch");
-    const long long n = g.N() * (long long)g.no;
-    mdft::vext_kernel<<<mdft::stream_blocks(n), 256, 0, s>>>(P, vext);
-    launch_ok("vext kernel launch");
-    // the tables are freed on return: finish first
-    cuda_check(cudaStreamSynchronize(s), "vext kernel");
+    throw_if(!grid, "NULL argument");
+    mdft::vext_compute(grid->g, solvent_sites, n_solvent_sites, solute_sites, n_solute_sites, vmax, vext,
+                       static_cast<cudaStream_t>(stream));
   });
 }
 
@@ -853,56 +984,33 @@ int mdft_solver_create(mdft_solver_t* out, mdft_opt_t opt, mdft_conv_t conv, con
     h->no = go.no;
     h->np = go.np;
     h->n = h->N * h->no;
-    h->kT = kT;
-    h->rho0 = rho0;
-    h->prefactor = prefactor;
-    h->dv = (go.lx / go.nx) * (go.ly / go.ny) * (go.lz / go.nz);
+    h->c = mdft::EgConst{kT, rho0, (go.lx / go.nx) * (go.ly / go.ny) * (go.lz / go.nz), prefactor};
     const size_t fb = sizeof(double) * (size_t)h->n;
     const size_t eb = h->prec == MDFT_F32 ? 4 : 8;
     h->w.upload(go.w.data(), sizeof(double) * go.no);
     h->p.alloc(2 * eb * (size_t)h->np * h->N);
     h->vexc.alloc(eb * (size_t)h->n);
     if (h->prec == MDFT_F32) h->xf.alloc(sizeof(float) * (size_t)h->n);
-    h->ga.alloc(fb);
-    h->gb.alloc(fb);
-    h->xa.alloc(fb);
+    h->x.alloc(fb);
+    h->xt.alloc(fb);
+    h->g.alloc(fb);
+    h->gt.alloc(fb);
     h->d.alloc(fb / 2);  // FP32 direction and curvature pairs
     h->hs.alloc(fb / 2 * h->m);
     h->hy.alloc(fb / 2 * h->m);
-    h->scal.alloc(sizeof(double) * (h->m + 5));
-    h->energy.alloc(sizeof(double) * 5);
-    h->part.alloc(sizeof(double) * mdft::kRedBlocks * 7);
-    h->counter.alloc(256);
-    cuda_check(cudaMemset(h->counter.ptr, 0, 256), "counter reset");
-    cuda_check(cudaMemset(h->scal.ptr, 0, sizeof(double) * (h->m + 5)), "scalar reset");
+    h->S.alloc(sizeof(double) * mdft::Lbfgs::nscalars(h->m));
+    h->scratch.alloc(mdft::reduction_scratch_bytes());
+    cuda_check(cudaMemset(h->scratch.ptr, 0, mdft::reduction_scratch_bytes()), "scratch reset");
+    cuda_check(cudaMemset(h->S.ptr, 0, sizeof(double) * mdft::Lbfgs::nscalars(h->m)), "scalar reset");
     if (vext) {
       h->vext.alloc(fb);
       cuda_check(cudaMemcpy(h->vext.ptr, vext, fb, cudaMemcpyDeviceToDevice), "vext copy");
       h->has_vext = true;
     }
-    h->rho.assign(h->m, 0.0);
-    {
-      mdft::EgArgs& A = h->eg;
-      A.w = h->w.as<double>();
-      A.n = h->n;
-      A.no = h->no;
-      A.kT = kT;
-      A.rho0 = rho0;
-      A.dv = h->dv;
-      A.prefactor = prefactor;
-      auto split = [](long double v, float& hi, float& lo) {
-        hi = (float)v;
-        lo = (float)(v - (long double)hi);
-      };
-      split(kT, A.kh, A.kl);
-      split((long double)rho0 * h->dv, A.ch, A.cl);
-      split(2.0L * prefactor * rho0, A.xh, A.xl);
-      split(0.693147180559945309417232121458176568L, A.ln2h, A.ln2l);
-      for (int k = 0; k < 10; ++k) split(1.0L / (2 * k + 1), A.ah[k], A.al[k]);
-      A.out = h->energy.as<double>();
-      A.part = h->part.as<double>();
-      A.counter = h->counter.as<unsigned>();
-    }
+    h->lb.bind(mdft::Lbfgs::Bufs{h->x.as<double>(), h->xt.as<double>(), h->g.as<double>(), h->gt.as<double>(),
+                                 h->d.as<float>(), h->hs.as<float>(), h->hy.as<float>(), h->S.as<double>(),
+                                 h->scratch.ptr},
+               h->n, h->m);
     *out = h.release();
   });
 }
@@ -912,8 +1020,10 @@ int mdft_solver_energy(mdft_solver_t h, const double* xi, double* grad, double* 
     throw_if(!h || !xi || !terms, "NULL argument");
     throw_if(mdft::detail::current_device() != h->device, "the solver belongs to another device");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    evaluate(h, xi, grad ? grad : h->ga.as<double>(), s);
-    read_energy(h, terms, s);
+    double* out = h->S.as<double>() + mdft::Lbfgs::energy_at(h->m);
+    evaluate(h, xi, grad ? grad : h->gt.as<double>(), out, s);
+    cuda_check(cudaMemcpyAsync(terms, out, 5 * sizeof(double), cudaMemcpyDeviceToHost, s), "energy read-back");
+    cuda_check(cudaStreamSynchronize(s), "solver stream");
   });
 }
 
@@ -924,70 +1034,24 @@ int mdft_solver_minimize(mdft_solver_t h, double* xi, int max_iter, double gtol,
     throw_if(max_iter < 0, "max_iter must be >= 0");
     throw_if(mdft::detail::current_device() != h->device, "the solver belongs to another device");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    const double c1 = 1e-4, max_first_step = 0.1;
-    const int max_ls = 40;
-    h->nh = 0;
-    h->head = 0;
-    double* x = xi;                  // current iterate
-    double* xn = h->xa.as<double>();  // trial iterate
-    double* g = h->ga.as<double>();
-    double* gn = h->gb.as<double>();
-    double E[5], En[5];
-    evaluate(h, x, g, s);
-    read_energy(h, E, s);
-    if (trace) std::memcpy(trace, E, sizeof E);
-    int it = 0;
-    while (it < max_iter && E[4] > gtol) {
-      double gd = direction(h, g, s);
-      double t = 1.0;
-      if (!(gd < 0.0) || h->nh == 0) {  // first step, or no descent: steepest descent
-        h->nh = 0;
-        if (!(gd < 0.0)) gd = direction(h, g, s);
-        t = std::min(1.0, max_first_step / E[4]);
-      }
-      bool ok = false;
-      for (int ls = 0; ls < max_ls; ++ls) {
-        mdft::step_kernel<<<mdft::stream_blocks(h->n), 256, 0, s>>>(xn, x, h->d.as<float>(), t, h->n);
-        launch_ok("step kernel launch");
-        evaluate(h, xn, gn, s);
-        read_energy(h, En, s);
-        if (std::isfinite(En[0]) && En[0] <= E[0] + c1 * t * gd) {
-          ok = true;
-          break;
-        }
-        t *= 0.5;
-      }
-      if (!ok) break;  // no decrease along the direction: stop at the current iterate
-      // curvature pair of the accepted step into the ring slot `head`
-      mdft::pair_kernel<<<mdft::red_blocks(h->n), mdft::kRedThreads, 0, s>>>(
-          h->hs_at(h->head), h->hy_at(h->head), h->d.as<float>(), gn, g, t, h->n, h->scal.as<double>(), h->SY(),
-          h->part.as<double>(), h->counter.as<unsigned>());
-      launch_ok("pair kernel launch");
-      double sy_yy[2];
-      cuda_check(cudaMemcpyAsync(sy_yy, h->scal.as<double>() + h->SY(), sizeof sy_yy, cudaMemcpyDeviceToHost, s),
-                 "curvature read-back");
+    const size_t fb = sizeof(double) * (size_t)h->n;
+    cuda_check(cudaMemcpyAsync(h->xt.ptr, xi, fb, cudaMemcpyDeviceToDevice, s), "start copy");
+    h->lb.start(gtol, ftol, max_iter, s);
+    const int m = h->m;
+    double* Sd = h->S.as<double>();
+    double tail[8];
+    for (;;) {
+      evaluate(h, h->xt.as<double>(), h->gt.as<double>(), Sd + mdft::Lbfgs::energy_at(m), s);
+      cuda_check(cudaMemcpyAsync(tail, Sd + mdft::Lbfgs::tail_at(m), sizeof tail, cudaMemcpyDeviceToHost, s),
+                 "tail read-back");
       cuda_check(cudaStreamSynchronize(s), "solver stream");
-      if (sy_yy[0] > 1e-12 * sy_yy[1] && sy_yy[1] > 0) {
-        h->rho[h->head] = 1.0 / sy_yy[0];
-        h->gamma = sy_yy[0] / sy_yy[1];
-        h->head = (h->head + 1) % h->m;
-        h->nh = std::min(h->nh + 1, h->m);
-      } else {
-        h->nh = 0;  // the slot was overwritten: restart the history
-      }
-      std::swap(x, xn);
-      std::swap(g, gn);
-      const double Eprev = E[0];
-      std::memcpy(E, En, sizeof E);
-      ++it;
-      if (trace) std::memcpy(trace + 5 * (size_t)it, E, sizeof E);
-      if (std::fabs(Eprev - E[0]) <= ftol * std::max(1.0, std::fabs(E[0]))) break;
+      if (h->lb.on_eval(tail, s)) break;
     }
-    if (x != xi)
-      cuda_check(cudaMemcpyAsync(xi, x, sizeof(double) * (size_t)h->n, cudaMemcpyDeviceToDevice, s),
-                 "final iterate copy");
+    cuda_check(cudaMemcpyAsync(xi, h->x.ptr, fb, cudaMemcpyDeviceToDevice, s), "final iterate copy");
     cuda_check(cudaStreamSynchronize(s), "solver stream");
-    if (iterations) *iterations = it;
+    const std::vector<double>& tr = h->lb.trace();
+    if (trace) std::memcpy(trace, tr.data(), sizeof(double) * std::min(tr.size(), (size_t)5 * (max_iter + 1)));
+    if (iterations) *iterations = h->lb.iterations();
   });
 }
 
