@@ -249,6 +249,26 @@ int mdft_server_submit(mdft_server_t s, int solvent_id, int nx, int ny, int nz, 
  * latency from submit (seconds, may be NULL).  Each job is waited for once. */
 int mdft_server_wait(mdft_server_t s, long long job_id, void* xi_out, double* ff_out,
                      double* latency_s);
+/* Solute jobs (no counterpart in the reference): each job carries a solute
+ * and is minimised with the full functional of mdft_solver_minimize (L-BFGS
+ * on E_id + E_ext + E_exc, every precision's xi in double), its minimiser
+ * state resident on the device; same-shape jobs share one batched energy
+ * evaluation per step.  The solvent's molecular model first: sites as for
+ * mdft_vext_lj_coulomb (molecular frame), kT [kJ/mol], vmax [kJ/mol]. */
+int mdft_server_set_solvent_model(mdft_server_t s, int solvent_id, const double* sites, int n_sites, double kT,
+                                  double vmax);
+/* Queues a solute job (sites in box coordinates, copied; xi0: host doubles,
+ * (nx*ny*nz, no), NULL for xi = 1) that runs until max |dE/dxi| <= gtol, no
+ * step lowers E, or max_iter iterations. */
+int mdft_server_submit_solute(mdft_server_t s, int solvent_id, int nx, int ny, int nz, double lx, double ly,
+                              double lz, const double* solute_sites, int n_sites, const double* xi0, int max_iter,
+                              double gtol, long long* job_id);
+/* Blocks until the solute job is done: final xi (host doubles, may be NULL),
+ * trace ((max_iter + 1) rows of E_total, E_id, E_ext, E_exc, max |dE/dxi|,
+ * may be NULL), iterations, status (0 gtol reached, 1 E flat, 2 max_iter,
+ * 3 no decrease along the direction) and latency (each may be NULL). */
+int mdft_server_wait_solute(mdft_server_t s, long long job_id, double* xi_out, double* trace_out, int* iterations,
+                            int* status, double* latency_s);
 /* out[0..7]: jobs done, jobs done per second since the first submit, p50 and
  * p99 latency (s), job groups held, peak device bytes of the groups, group
  * steps replayed from captured graphs, group steps launched directly. */

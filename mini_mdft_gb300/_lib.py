@@ -64,6 +64,10 @@ SIGNATURES = {
                                  C.POINTER(C.c_longlong)]),
     "mdft_server_wait": (i32, [vp, C.c_longlong, vp, dp, dp]),
     "mdft_server_stats": (i32, [vp, dp]),
+    "mdft_server_set_solvent_model": (i32, [vp, i32, dp, i32, f64, f64]),
+    "mdft_server_submit_solute": (i32, [vp, i32, i32, i32, i32, f64, f64, f64, dp, i32, dp, i32, f64,
+                                        C.POINTER(C.c_longlong)]),
+    "mdft_server_wait_solute": (i32, [vp, C.c_longlong, dp, dp, ip, ip, dp]),
     "mdft_vext_lj_coulomb": (i32, [vp, dp, i32, dp, i32, f64, vp, vp]),
     "mdft_solver_create": (i32, [C.POINTER(vp), vp, vp, vp, f64, f64, f64, i32]),
     "mdft_solver_energy": (i32, [vp, vp, vp, dp, vp]),

@@ -413,7 +413,7 @@ class Server:
 
     def wait(self, job):
         """(final xi, energies of every step, latency in s) of a job."""
-        shape, n_steps = self._jobs.pop(job, (None, 0))
+        shape, n_steps = self._jobs.pop(job, (None, 0))[:2]
         lat = C.c_double()
         if shape is None:  # not submitted here, or already waited for: the server says which
             check(lib().mdft_server_wait(self.h, C.c_longlong(job), None, None, C.byref(lat)))
@@ -423,6 +423,43 @@ class Server:
         check(lib().mdft_server_wait(self.h, C.c_longlong(job), xi.ctypes.data_as(C.c_void_p),
                                      ff.ctypes.data_as(C.POINTER(C.c_double)), C.byref(lat)))
         return xi, ff, lat.value
+
+    def set_solvent_model(self, solvent, sites, kT, vmax):
+        """The solvent's molecular model for solute jobs: sites (q, sigma,
+        epsilon, x, y, z) in the molecular frame, kT and vmax in kJ/mol."""
+        sv = np.ascontiguousarray(sites, np.float64).reshape(-1, 6)
+        check(lib().mdft_server_set_solvent_model(self.h, int(solvent), _np_d(sv), sv.shape[0], float(kT),
+                                                  float(vmax)))
+
+    def submit_solute(self, solvent, n_nodes, length, solute_sites, max_iter=100, gtol=1e-5, xi0=None):
+        """Queues a solute job: minimise the full functional from xi0 (None:
+        xi = 1) with the solute's external potential; returns its id."""
+        nx, ny, nz = (int(v) for v in n_nodes)
+        ntheta, nphi, npsi = self._solvents[solvent]
+        su = np.ascontiguousarray(solute_sites, np.float64).reshape(-1, 6)
+        x = None
+        if xi0 is not None:
+            x = np.ascontiguousarray(xi0, np.float64)
+            if x.size != nx * ny * nz * ntheta * nphi * npsi:
+                raise ValueError("xi0 has the wrong size")
+        jid = C.c_longlong()
+        check(lib().mdft_server_submit_solute(self.h, int(solvent), nx, ny, nz, *(float(v) for v in length),
+                                              _np_d(su), su.shape[0], _np_d(x) if x is not None else None,
+                                              int(max_iter), float(gtol), C.byref(jid)))
+        self._jobs[jid.value] = ((nx * ny * nz, ntheta, nphi, npsi), int(max_iter), "solute")
+        return jid.value
+
+    def wait_solute(self, job):
+        """(final xi, trace (iterations + 1, 5): E_total, E_id, E_ext, E_exc,
+        max |dE/dxi|, status, latency in s) of a solute job; status 0: gtol
+        reached, 1: E flat, 2: max_iter, 3: no decrease along the direction."""
+        shape, max_iter, _ = self._jobs.pop(job)
+        xi = np.empty(shape, np.float64)
+        trace = np.zeros((max_iter + 1, 5), np.float64)
+        it, st, lat = C.c_int(), C.c_int(), C.c_double()
+        check(lib().mdft_server_wait_solute(self.h, C.c_longlong(job), _np_d(xi), _np_d(trace), C.byref(it),
+                                            C.byref(st), C.byref(lat)))
+        return xi, trace[: it.value + 1], st.value, lat.value
 
     def stats(self):
         """dict: done, solves_per_s, p50_s, p99_s, groups, peak_bytes,

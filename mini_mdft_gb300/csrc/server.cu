@@ -36,6 +36,7 @@
 #include <vector>
 
 #include "handles.hpp"
+#include "solver.hpp"
 
 using mdft::Error;
 using mdft::throw_if;
@@ -80,6 +81,9 @@ struct Solvent {
   double dq, rho0, prefactor;
   std::vector<int> luc_index;
   std::vector<double> luc;
+  // molecular model for solute jobs: sites (q, sigma, epsilon, x, y, z), kT, vmax
+  std::vector<double> sites;
+  double kT = 0, vmax = 0;
 };
 
 // Page-locked host buffers for the job fields, kept for reuse: copies to and
@@ -130,6 +134,13 @@ struct Job {
   std::vector<double> ff;         // energy of every step
   int n_steps = 0;
   double step = 0;
+  // solute jobs (kind 1): L-BFGS minimisation of the full functional
+  int kind = 0;
+  std::vector<double> solute;      // (q, sigma, epsilon, x, y, z) rows
+  int max_iter = 0;
+  double gtol = 0;
+  std::vector<double> trace5;      // 5 terms per accepted iterate
+  int iterations = 0, status = -1;
   int state = 0;  // 0 queued, 1 running, 2 done, -1 failed
   int code = 0;
   std::string error;
@@ -137,7 +148,7 @@ struct Job {
   int slot = -1, steps_done = 0;
 };
 
-using Key = std::tuple<int, int, int, int, double, double, double>;
+using Key = std::tuple<int, int, int, int, int, double, double, double>;  // kind, solvent, grid
 
 struct DevPtr {
   void* p = nullptr;
@@ -151,8 +162,11 @@ struct DevPtr {
   }
 };
 
+constexpr int kHistory = 5;  // L-BFGS pairs of a solute job
+
 struct Group {
   Key key;
+  int kind = 0;
   int B = 1, k = 0, prec = MDFT_F64, cap = 0;
   long long N = 0;
   int no = 0, np = 0;
@@ -163,12 +177,20 @@ struct Group {
   mdft_conv_t conv = nullptr;
   DevPtr xi, vexc, df, p, w, ff_cur, trace, step_ctr, alpha, scratch;
   size_t scratch_per_slot = 0;
+  // solute groups: per slot the minimiser's fields (xt contiguous: the batched
+  // evaluation reads the k trial points as one array) and scalar blocks
+  DevPtr xt, x, g, gt, vext, d, hs, hy, S, red;
+  double* tails = nullptr;  // page-locked: 8 doubles per slot read back each step
+  std::vector<mdft::Lbfgs> lb;
+  mdft::EgConst eg{};
+  Solvent model;
   cudaStream_t stream = nullptr;
   std::vector<std::shared_ptr<Job>> slots;  // active jobs, slot i = field i
   std::map<int, cudaGraphExec_t> graphs;    // per active count; null: run directly
   std::map<int, int> seen;                  // steps run directly at each active count
   Clock::time_point last_used;
   ~Group() {
+    if (tails) cudaFreeHost(tails);
     for (auto& g : graphs)
       if (g.second) cudaGraphExecDestroy(g.second);
     if (stream) cudaStreamDestroy(stream);
@@ -208,6 +230,7 @@ struct mdft_server_s {
   Group* group_for(const Job& j);
   void step(Group& g);
   void enqueue_step(Group& g, int k);
+  void bind_slot(Group& g, int slot);
   void finish(Group& g, int slot);
   void fail_group(Group& g, const std::string& msg, int code);
   void fail_job(const std::shared_ptr<Job>& j, const std::string& msg, int code);
@@ -235,7 +258,7 @@ void mdft_server_s::fail_group(Group& g, const std::string& msg, int code) {
 }
 
 Group* mdft_server_s::group_for(const Job& j) {
-  const Key key{j.solvent, j.n[0], j.n[1], j.n[2], j.len[0], j.len[1], j.len[2]};
+  const Key key{j.kind, j.solvent, j.n[0], j.n[1], j.n[2], j.len[0], j.len[1], j.len[2]};
   auto it = groups.find(key);
   if (it != groups.end()) return it->second.get();
   Solvent sv;
@@ -246,6 +269,7 @@ Group* mdft_server_s::group_for(const Job& j) {
   // footprint: plans (measured) + arena (computed); admit only within budget
   auto g = std::make_unique<Group>();
   g->key = key;
+  g->kind = j.kind;
   g->B = max_batch;
   g->prec = prec;
   g->cap = trace_cap;
@@ -262,8 +286,14 @@ Group* mdft_server_s::group_for(const Job& j) {
   const size_t fb = field_bytes(*g);
   const size_t nbp = mdft::delta_f_partials((size_t)g->N, g->no);
   g->scratch_per_slot = (sizeof(double2) * nbp + 256 + 255) / 256 * 256;
-  const size_t arena = 3 * fb * g->B + (size_t)g->np * g->N * 2 * g->elem * g->B +
-                       g->scratch_per_slot * g->B + (size_t)g->B * (g->cap + 3) * 8 + 8 * g->no;
+  const size_t f64b = (size_t)g->N * g->no * 8;  // one FP64 field
+  const size_t arena =
+      g->kind == 0 ? 3 * fb * g->B + (size_t)g->np * g->N * 2 * g->elem * g->B + g->scratch_per_slot * g->B +
+                         (size_t)g->B * (g->cap + 3) * 8 + 8 * g->no
+                   : (5 * f64b + f64b / 2 * (1 + 2 * kHistory) + fb * (g->elem == 4 ? 2 : 1) +
+                      (size_t)g->np * g->N * 2 * g->elem) *
+                             g->B +
+                         mdft::reduction_scratch_bytes() + 8 * g->no;
   // a rough bound on the plans before building them: the R(q) table and
   // pair data dominate (about 1 KB per grid point at mmax <= 6)
   const size_t plan_guess = (size_t)g->N * 1024;
@@ -295,15 +325,31 @@ Group* mdft_server_s::group_for(const Job& j) {
   ckr(mdft_conv_create_batched(&g->conv, g->grid, sv.luc_index.data(), sv.luc.data(), sv.np_luc, sv.nq, sv.dq,
                                prec, g->B),
       "job plan (convolution)");
-  g->xi.alloc(fb * g->B, "server arena");
   g->vexc.alloc(fb * g->B, "server arena");
-  g->df.alloc(fb * g->B, "server arena");
   g->p.alloc((size_t)g->np * g->N * 2 * g->elem * g->B, "server arena");
-  g->scratch.alloc(g->scratch_per_slot * g->B, "server arena");
-  g->trace.alloc((size_t)g->B * g->cap * 8, "server arena");
-  g->ff_cur.alloc((size_t)g->B * 8, "server arena");
-  g->alpha.alloc((size_t)g->B * 8, "server arena");
-  g->step_ctr.alloc((size_t)g->B * 4, "server arena");
+  if (g->kind == 0) {
+    g->xi.alloc(fb * g->B, "server arena");
+    g->df.alloc(fb * g->B, "server arena");
+    g->scratch.alloc(g->scratch_per_slot * g->B, "server arena");
+    g->trace.alloc((size_t)g->B * g->cap * 8, "server arena");
+    g->ff_cur.alloc((size_t)g->B * 8, "server arena");
+    g->alpha.alloc((size_t)g->B * 8, "server arena");
+    g->step_ctr.alloc((size_t)g->B * 4, "server arena");
+  } else {
+    if (g->elem == 4) g->xi.alloc(fb * g->B, "server arena");  // FP32 copy of the trial points
+    for (DevPtr* f : {&g->xt, &g->x, &g->g, &g->gt, &g->vext}) f->alloc(f64b * g->B, "server arena");
+    g->d.alloc(f64b / 2 * g->B, "server arena");
+    g->hs.alloc(f64b / 2 * kHistory * g->B, "server arena");
+    g->hy.alloc(f64b / 2 * kHistory * g->B, "server arena");
+    g->S.alloc(sizeof(double) * mdft::Lbfgs::nscalars(kHistory) * g->B, "server arena");
+    g->red.alloc(mdft::reduction_scratch_bytes(), "server arena");
+    ck(cudaMemset(g->red.p, 0, mdft::reduction_scratch_bytes()), "scratch reset");
+    ck(cudaHostAlloc((void**)&g->tails, sizeof(double) * 8 * g->B, cudaHostAllocDefault), "page-locked tails");
+    g->lb.resize(g->B);
+    g->model = sv;
+    g->eg = mdft::EgConst{sv.kT, sv.rho0, (j.len[0] / j.n[0]) * (j.len[1] / j.n[1]) * (j.len[2] / j.n[2]),
+                          sv.prefactor};
+  }
   g->w.alloc((size_t)g->no * 8, "server arena");
   std::vector<double> th(info[5]), wth(info[5]), w(g->no);
   ckr(mdft_grid_angular(g->grid, th.data(), wth.data(), w.data()), "angular weights");
@@ -335,12 +381,25 @@ void mdft_server_s::admit() {
     }
     const int slot = g->k;
     try {
-      const size_t fb = field_bytes(*g);
-      ck(cudaMemcpyAsync(g->xi.as<unsigned char>() + fb * slot, j->xi, fb, cudaMemcpyHostToDevice, g->stream),
-         "job field upload");
-      ck(cudaMemcpyAsync(g->alpha.as<double>() + slot, &j->step, 8, cudaMemcpyHostToDevice, g->stream),
-         "job step upload");
-      ck(cudaMemsetAsync(g->step_ctr.as<int>() + slot, 0, 4, g->stream), "job counter reset");
+      if (g->kind == 0) {
+        const size_t fb = field_bytes(*g);
+        ck(cudaMemcpyAsync(g->xi.as<unsigned char>() + fb * slot, j->xi, fb, cudaMemcpyHostToDevice, g->stream),
+           "job field upload");
+        ck(cudaMemcpyAsync(g->alpha.as<double>() + slot, &j->step, 8, cudaMemcpyHostToDevice, g->stream),
+           "job step upload");
+        ck(cudaMemsetAsync(g->step_ctr.as<int>() + slot, 0, 4, g->stream), "job counter reset");
+      } else {
+        // start point, the job's external potential, a fresh minimiser
+        const long long n = g->N * g->no;
+        ck(cudaMemcpyAsync(g->xt.as<double>() + (size_t)n * slot, j->xi, sizeof(double) * n, cudaMemcpyHostToDevice,
+                           g->stream),
+           "job field upload");
+        mdft::vext_compute(g->grid->g, g->model.sites.data(), (int)g->model.sites.size() / 6,
+                           j->solute.data(), (int)j->solute.size() / 6, g->model.vmax,
+                           g->vext.as<double>() + (size_t)n * slot, g->stream);
+        bind_slot(*g, slot);
+        g->lb[slot].start(j->gtol, 0.0, j->max_iter, g->stream);
+      }
       ck(cudaStreamSynchronize(g->stream), "job admission");
     } catch (const Error& e) {
       fail_job(j, e.what(), e.code);
@@ -359,7 +418,48 @@ void mdft_server_s::admit() {
   pending.swap(keep);
 }
 
+void mdft_server_s::bind_slot(Group& g, int slot) {
+  const size_t n = (size_t)g.N * g.no;
+  const int ns = mdft::Lbfgs::nscalars(kHistory);
+  g.lb[slot].bind(mdft::Lbfgs::Bufs{g.x.as<double>() + n * slot, g.xt.as<double>() + n * slot,
+                                    g.g.as<double>() + n * slot, g.gt.as<double>() + n * slot,
+                                    g.d.as<float>() + n * slot, g.hs.as<float>() + n * kHistory * slot,
+                                    g.hy.as<float>() + n * kHistory * slot, g.S.as<double>() + (size_t)ns * slot,
+                                    g.red.p},
+                  (long long)n, kHistory);
+}
+
+// Solute groups: the energy and gradient of every active job at its trial
+// point (one batched cproj evaluation), and each job's scalar tail read back;
+// the minimisers then choose the next trial points on the host.
+void enqueue_solve_step(Group& g, int k) {
+  cudaStream_t s = g.stream;
+  const size_t n = (size_t)g.N * g.no;
+  const void* xin = g.xt.p;
+  if (g.elem == 4) {
+    mdft::to_float(g.xi.as<float>(), g.xt.as<double>(), (long long)n * k, s);
+    xin = g.xi.p;
+  }
+  mdft::detail::angl2proj_fields(g.opt, xin, true, g.rho0, g.p.p, k, s);
+  mdft::detail::execute_fields(g.conv, g.p.p, k, s);
+  mdft::detail::proj2angl_fields(g.opt, g.p.p, g.vexc.p, k, s);
+  const int ns = mdft::Lbfgs::nscalars(kHistory);
+  for (int j = 0; j < k; ++j) {
+    double* S = g.S.as<double>() + (size_t)ns * j;
+    mdft::energy_grad(g.eg, g.xt.as<double>() + n * j, g.vexc.as<unsigned char>() + n * g.elem * j, g.elem == 4,
+                      g.vext.as<double>() + n * j, g.w.as<double>(), g.gt.as<double>() + n * j, (long long)n, g.no,
+                      S + mdft::Lbfgs::energy_at(kHistory), g.red.p, s);
+    ck(cudaMemcpyAsync(g.tails + 8 * j, S + mdft::Lbfgs::tail_at(kHistory), 8 * sizeof(double),
+                       cudaMemcpyDeviceToHost, s),
+       "minimiser tail read-back");
+  }
+}
+
 void mdft_server_s::enqueue_step(Group& g, int k) {
+  if (g.kind == 1) {
+    enqueue_solve_step(g, k);
+    return;
+  }
   cudaStream_t s = g.stream;
   mdft::detail::angl2proj_fields(g.opt, g.xi.p, true, g.rho0, g.p.p, k, s);
   mdft::detail::execute_fields(g.conv, g.p.p, k, s);
@@ -434,6 +534,45 @@ void mdft_server_s::step(Group& g) {
 
 void mdft_server_s::finish(Group& g, int slot) {
   std::shared_ptr<Job> j = g.slots[slot];
+  if (g.kind == 1) {
+    const size_t n = (size_t)g.N * g.no;
+    ck(cudaMemcpyAsync(j->xi, g.x.as<double>() + n * slot, sizeof(double) * n, cudaMemcpyDeviceToHost, g.stream),
+       "job field download");
+    std::vector<double> tr = g.lb[slot].trace();
+    const int iters = g.lb[slot].iterations(), status = (int)g.lb[slot].status();
+    const int last = g.k - 1;
+    if (slot != last) {  // the last active job moves into the freed slot
+      const int ns = mdft::Lbfgs::nscalars(kHistory);
+      auto mv = [&](DevPtr& f, size_t per) {
+        ck(cudaMemcpyAsync(f.as<unsigned char>() + per * slot, f.as<unsigned char>() + per * last, per,
+                           cudaMemcpyDeviceToDevice, g.stream),
+           "slot move");
+      };
+      for (DevPtr* f : {&g.xt, &g.x, &g.g, &g.gt, &g.vext}) mv(*f, 8 * n);
+      mv(g.d, 4 * n);
+      mv(g.hs, 4 * n * kHistory);
+      mv(g.hy, 4 * n * kHistory);
+      mv(g.S, 8 * (size_t)ns);
+      g.lb[slot] = g.lb[last];
+      bind_slot(g, slot);
+      g.slots[slot] = g.slots[last];
+      g.slots[slot]->slot = slot;
+    }
+    ck(cudaStreamSynchronize(g.stream), "job completion");
+    g.slots.pop_back();
+    g.k -= 1;
+    g.last_used = Clock::now();
+    std::lock_guard<std::mutex> lk(mu);
+    j->trace5.swap(tr);
+    j->iterations = iters;
+    j->status = status;
+    j->state = 2;
+    j->t_done = Clock::now();
+    latencies.push_back(std::chrono::duration<double>(j->t_done - j->t_submit).count());
+    t_last_done = j->t_done;
+    cv_done.notify_all();
+    return;
+  }
   const size_t fb = field_bytes(g);
   std::vector<double> ff(j->n_steps);
   // the final field goes back into the job's page-locked buffer
@@ -512,8 +651,16 @@ void mdft_server_s::run() {
       try {
         ck(cudaStreamSynchronize(g->stream), "server step");
         for (auto& j : g->slots) j->steps_done += 1;
-        for (int s = g->k - 1; s >= 0; --s)
-          if (g->slots[s]->steps_done >= g->slots[s]->n_steps) finish(*g, s);
+        if (g->kind == 1) {
+          // every minimiser takes its evaluation and queues its next trial
+          // point (highest slot first, so that a finished job's slot is
+          // refilled by a job that has already queued its own)
+          for (int s = g->k - 1; s >= 0; --s)
+            if (g->lb[s].on_eval(g->tails + 8 * s, g->stream)) finish(*g, s);
+        } else {
+          for (int s = g->k - 1; s >= 0; --s)
+            if (g->slots[s]->steps_done >= g->slots[s]->n_steps) finish(*g, s);
+        }
       } catch (const Error& e) {
         fail_group(*g, e.what(), e.code);
       }
@@ -669,8 +816,109 @@ int mdft_server_wait(mdft_server_t s, long long job_id, void* xi_out, double* ff
       }
     } rel{s, j};
     if (j->state == -1) throw Error(j->code, j->error);
+    throw_if(j->kind != 0, "a solute job: collect it with mdft_server_wait_solute");
     if (xi_out) std::memcpy(xi_out, j->xi, j->xi_bytes);
     if (ff_out) std::memcpy(ff_out, j->ff.data(), sizeof(double) * j->ff.size());
+    if (latency_s) *latency_s = std::chrono::duration<double>(j->t_done - j->t_submit).count();
+  });
+}
+
+int mdft_server_set_solvent_model(mdft_server_t s, int solvent_id, const double* sites, int n_sites, double kT,
+                                  double vmax) {
+  return sguard([&] {
+    throw_if(!s || !sites, "NULL argument");
+    throw_if(n_sites < 1, "a solvent model needs at least one site");
+    throw_if(!(kT > 0) || !(vmax > 0), "kT and vmax must be positive");
+    std::lock_guard<std::mutex> lk(s->mu);
+    throw_if(solvent_id < 0 || solvent_id >= (int)s->solvents.size(), "unknown solvent");
+    Solvent& sv = s->solvents[solvent_id];
+    sv.sites.assign(sites, sites + 6 * (size_t)n_sites);
+    sv.kT = kT;
+    sv.vmax = vmax;
+  });
+}
+
+int mdft_server_submit_solute(mdft_server_t s, int solvent_id, int nx, int ny, int nz, double lx, double ly,
+                              double lz, const double* solute_sites, int n_sites, const double* xi0, int max_iter,
+                              double gtol, long long* job_id) {
+  return sguard([&] {
+    throw_if(!s || !job_id || (n_sites > 0 && !solute_sites), "NULL argument");
+    throw_if(nx < 1 || ny < 1 || nz < 1 || !(lx > 0) || !(ly > 0) || !(lz > 0), "invalid grid");
+    throw_if(n_sites < 0, "n_sites must be >= 0");
+    throw_if(max_iter < 0 || max_iter > 100000, "max_iter must be 0..100000");
+    throw_if(!(gtol >= 0), "gtol must be >= 0");
+    auto j = std::make_shared<Job>();
+    int no = 0;
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      throw_if(solvent_id < 0 || solvent_id >= (int)s->solvents.size(), "unknown solvent");
+      const Solvent& sv = s->solvents[solvent_id];
+      throw_if(sv.sites.empty(), "the solvent has no molecular model (mdft_server_set_solvent_model)");
+      const int nt = sv.mmax + 1, nphi = 2 * sv.mmax + 1, npsi = 2 * (sv.mmax / sv.mrso) + 1;
+      no = nt * nphi * npsi;
+    }
+    const size_t n = (size_t)nx * ny * nz * no, bytes = n * sizeof(double);
+    j->kind = 1;
+    j->solvent = solvent_id;
+    j->n[0] = nx;
+    j->n[1] = ny;
+    j->n[2] = nz;
+    j->len[0] = lx;
+    j->len[1] = ly;
+    j->len[2] = lz;
+    j->solute.assign(solute_sites, solute_sites + 6 * (size_t)n_sites);
+    j->max_iter = max_iter;
+    j->gtol = gtol;
+    j->xi = s->pinned.get(bytes);
+    j->xi_bytes = bytes;
+    if (xi0) {
+      std::memcpy(j->xi, xi0, bytes);
+    } else {
+      double* x = static_cast<double*>(j->xi);
+      std::fill(x, x + n, 1.0);  // the bulk density
+    }
+    j->t_submit = Clock::now();
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      j->id = s->next_id++;
+      if (!s->any_submit) {
+        s->any_submit = true;
+        s->t_first_submit = j->t_submit;
+      }
+      s->jobs[j->id] = j;
+      s->incoming.push_back(j);
+      *job_id = j->id;
+    }
+    s->cv_work.notify_all();
+  });
+}
+
+int mdft_server_wait_solute(mdft_server_t s, long long job_id, double* xi_out, double* trace_out, int* iterations,
+                            int* status, double* latency_s) {
+  return sguard([&] {
+    throw_if(!s, "NULL argument");
+    std::shared_ptr<Job> j;
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->jobs.find(job_id);
+    throw_if(it == s->jobs.end(), "unknown job (or its result was already taken)");
+    j = it->second;
+    s->cv_done.wait(lk, [&] { return j->state == 2 || j->state == -1; });
+    s->jobs.erase(it);
+    lk.unlock();
+    struct Release {
+      mdft_server_s* s;
+      std::shared_ptr<Job> j;
+      ~Release() {
+        s->pinned.put(j->xi, j->xi_bytes);
+        j->xi = nullptr;
+      }
+    } rel{s, j};
+    if (j->state == -1) throw Error(j->code, j->error);
+    throw_if(j->kind != 1, "not a solute job: collect it with mdft_server_wait");
+    if (xi_out) std::memcpy(xi_out, j->xi, j->xi_bytes);
+    if (trace_out) std::memcpy(trace_out, j->trace5.data(), sizeof(double) * j->trace5.size());
+    if (iterations) *iterations = j->iterations;
+    if (status) *status = j->status;
     if (latency_s) *latency_s = std::chrono::duration<double>(j->t_done - j->t_submit).count();
   });
 }

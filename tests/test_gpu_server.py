@@ -115,3 +115,86 @@ def test_server_budget_too_small(gpu_lib):
     with pytest.raises(M.MdftError, match="unknown job"):
         srv.wait(jid)
     srv.close()
+
+
+# solute jobs: (grid, box, mmax, mrso, solute sites, solute seed)
+SOLUTE_JOBS = [((12, 10, 8), (12., 10., 9.), 2, 2, 5, 11), ((12, 10, 8), (12., 10., 9.), 2, 2, 8, 12),
+               ((8, 8, 8), (10., 10., 10.), 2, 2, 7, 13), ((10, 12, 8), (11., 12., 10.), 1, 1, 4, 14),
+               ((10, 12, 8), (11., 12., 10.), 1, 1, 9, 15)]
+SOLUTE_DQ = 0.05
+
+
+def _solute_alone(M, n, box, mmax, mrso, table, su, max_iter, gtol, prec):
+    """The job alone: the single-field minimiser (mdft_solver_minimize)."""
+    import torch
+    idx, tab = table
+    rho0, pref = I.solvent_constants(I.SPCE_N0, mrso)
+    kT = I.kT()
+    sg, ag = M.SpatialGrid(n, box), M.AngularGrid(mmax, mrso)
+    opt = M.OrientationProjectionTransform(sg, ag, precision=prec)
+    conv = M.Convolution.from_table(idx, tab, SOLUTE_DQ, sg, ag, precision=prec)
+    vext = M.solute_vext(sg, ag, I.SPCE_SITES, su, 100 * kT)
+    solver = M.Solver(opt, conv, vext, kT=kT, rho0=rho0, prefactor=pref, history=5)
+    xi = torch.ones_like(vext)
+    trace = solver.minimize(xi, max_iter=max_iter, gtol=gtol)
+    return xi.cpu().numpy().reshape(-1), trace
+
+
+@pytest.mark.parametrize("prec", ["f64df", "f32"])
+def test_solute_jobs_match_the_single_minimiser(gpu_lib, prec):
+    """Solute jobs of three shapes and two angular grids, submitted from three
+    threads to a server with two slots per group (so finished jobs' slots are
+    refilled and compacted mid-run): every job's trace and final field equal
+    the same job run alone through the single-field minimiser."""
+    M = gpu_lib
+    kT = I.kT()
+    max_iter, gtol = 12, 1e-9
+    tables, alone = {}, []
+    for n, box, mmax, mrso, ns, seed in SOLUTE_JOBS:
+        if (mmax, mrso) not in tables:
+            nq = max(I.nq_for(n2, b2, SOLUTE_DQ) for n2, b2, m2, r2, _, _ in SOLUTE_JOBS if (m2, r2) == (mmax, mrso))
+            tables[(mmax, mrso)] = I.isotropic_cq(mmax, mrso, nq + 2, SOLUTE_DQ, amplitude=1e-3)
+        su = I.synthetic_solute(ns, box, seed=seed)
+        alone.append(_solute_alone(M, n, box, mmax, mrso, tables[(mmax, mrso)], su, max_iter, gtol, prec))
+    srv = M.Server(precision=prec, max_batch=2)
+    solvent = {}
+    for (mmax, mrso), (idx, tab) in tables.items():
+        rho0, pref = I.solvent_constants(I.SPCE_N0, mrso)
+        sid = srv.add_solvent(mmax, mrso, idx, tab, SOLUTE_DQ, rho0, pref)
+        srv.set_solvent_model(sid, I.SPCE_SITES, kT, 100 * kT)
+        solvent[(mmax, mrso)] = sid
+    ids = [None] * len(SOLUTE_JOBS)
+
+    def submit(part):
+        for i in part:
+            n, box, mmax, mrso, ns, seed = SOLUTE_JOBS[i]
+            ids[i] = srv.submit_solute(solvent[(mmax, mrso)], n, box, I.synthetic_solute(ns, box, seed=seed),
+                                       max_iter=max_iter, gtol=gtol)
+
+    threads = [threading.Thread(target=submit, args=(part,)) for part in ([0, 3], [1, 4], [2])]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    for i, jid in enumerate(ids):
+        xi, trace, status, lat = srv.wait_solute(jid)
+        xa, ta = alone[i]
+        assert trace.shape == ta.shape, i
+        assert np.array_equal(trace, ta), (i, np.abs(trace - ta).max())
+        assert np.array_equal(xi.reshape(-1), xa), i
+        assert lat > 0
+        assert np.all(np.diff(trace[:, 0]) <= 0)
+    st = srv.stats()
+    assert st["done"] == len(SOLUTE_JOBS)
+    srv.close()
+
+
+def test_solute_job_needs_a_solvent_model(gpu_lib):
+    M = gpu_lib
+    idx, tab = I.isotropic_cq(1, 1, 40, SOLUTE_DQ)
+    srv = M.Server(precision="f64", max_batch=2)
+    rho0, pref = I.solvent_constants(I.SPCE_N0, 1)
+    sid = srv.add_solvent(1, 1, idx, tab, SOLUTE_DQ, rho0, pref)
+    with pytest.raises(M.MdftError):
+        srv.submit_solute(sid, (4, 4, 4), (8., 8., 8.), I.synthetic_solute(2, (8., 8., 8.)))
+    srv.close()
