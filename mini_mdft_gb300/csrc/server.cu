@@ -179,7 +179,7 @@ struct Group {
   size_t scratch_per_slot = 0;
   // solute groups: per slot the minimiser's fields (xt contiguous: the batched
   // evaluation reads the k trial points as one array) and scalar blocks
-  DevPtr xt, x, g, gt, vext, d, hs, hy, S, red;
+  DevPtr xt, x, g, gt, vext, d, hs, hy, hinv, S, red;
   double* tails = nullptr;  // page-locked: 8 doubles per slot read back each step
   std::vector<mdft::Lbfgs> lb;
   mdft::EgConst eg{};
@@ -290,7 +290,7 @@ Group* mdft_server_s::group_for(const Job& j) {
   const size_t arena =
       g->kind == 0 ? 3 * fb * g->B + (size_t)g->np * g->N * 2 * g->elem * g->B + g->scratch_per_slot * g->B +
                          (size_t)g->B * (g->cap + 3) * 8 + 8 * g->no
-                   : (5 * f64b + f64b / 2 * (1 + 2 * kHistory) + fb * (g->elem == 4 ? 2 : 1) +
+                   : (5 * f64b + f64b / 2 * (2 + 2 * kHistory) + fb * (g->elem == 4 ? 2 : 1) +
                       (size_t)g->np * g->N * 2 * g->elem) *
                              g->B +
                          mdft::reduction_scratch_bytes() + 8 * g->no;
@@ -339,6 +339,7 @@ Group* mdft_server_s::group_for(const Job& j) {
     if (g->elem == 4) g->xi.alloc(fb * g->B, "server arena");  // FP32 copy of the trial points
     for (DevPtr* f : {&g->xt, &g->x, &g->g, &g->gt, &g->vext}) f->alloc(f64b * g->B, "server arena");
     g->d.alloc(f64b / 2 * g->B, "server arena");
+    g->hinv.alloc(f64b / 2 * g->B, "server arena");
     g->hs.alloc(f64b / 2 * kHistory * g->B, "server arena");
     g->hy.alloc(f64b / 2 * kHistory * g->B, "server arena");
     g->S.alloc(sizeof(double) * mdft::Lbfgs::nscalars(kHistory) * g->B, "server arena");
@@ -424,8 +425,8 @@ void mdft_server_s::bind_slot(Group& g, int slot) {
   g.lb[slot].bind(mdft::Lbfgs::Bufs{g.x.as<double>() + n * slot, g.xt.as<double>() + n * slot,
                                     g.g.as<double>() + n * slot, g.gt.as<double>() + n * slot,
                                     g.d.as<float>() + n * slot, g.hs.as<float>() + n * kHistory * slot,
-                                    g.hy.as<float>() + n * kHistory * slot, g.S.as<double>() + (size_t)ns * slot,
-                                    g.red.p},
+                                    g.hy.as<float>() + n * kHistory * slot, g.hinv.as<float>() + n * slot,
+                                    g.S.as<double>() + (size_t)ns * slot, g.red.p},
                   (long long)n, kHistory);
 }
 
@@ -448,7 +449,7 @@ void enqueue_solve_step(Group& g, int k) {
     double* S = g.S.as<double>() + (size_t)ns * j;
     mdft::energy_grad(g.eg, g.xt.as<double>() + n * j, g.vexc.as<unsigned char>() + n * g.elem * j, g.elem == 4,
                       g.vext.as<double>() + n * j, g.w.as<double>(), g.gt.as<double>() + n * j, (long long)n, g.no,
-                      S + mdft::Lbfgs::energy_at(kHistory), g.red.p, s);
+                      S + mdft::Lbfgs::energy_at(kHistory), g.red.p, g.hinv.as<float>() + n * j, s);
     ck(cudaMemcpyAsync(g.tails + 8 * j, S + mdft::Lbfgs::tail_at(kHistory), 8 * sizeof(double),
                        cudaMemcpyDeviceToHost, s),
        "minimiser tail read-back");
@@ -550,6 +551,7 @@ void mdft_server_s::finish(Group& g, int slot) {
       };
       for (DevPtr* f : {&g.xt, &g.x, &g.g, &g.gt, &g.vext}) mv(*f, 8 * n);
       mv(g.d, 4 * n);
+      mv(g.hinv, 4 * n);
       mv(g.hs, 4 * n * kHistory);
       mv(g.hy, 4 * n * kHistory);
       mv(g.S, 8 * (size_t)ns);

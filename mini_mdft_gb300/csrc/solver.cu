@@ -292,6 +292,10 @@ struct EgArgs {
   double* out;  // [E_total, E_id, E_ext, E_exc, max |g|]
   double* part;
   unsigned* counter;
+  // 1 / D with D = 2 rho0 dv w kT max(ln xi^2 + 2 + vext/kT, 1): the local
+  // terms' curvature d^2/dxi^2 (E_id + E_ext), floored at half its value at
+  // their minimum -- the minimiser's diagonal preconditioner (may be null)
+  float* hinv;
 };
 namespace {
 
@@ -351,13 +355,15 @@ __device__ __forceinline__ LnSq df_ln_sq(double x, const EgArgs& A) {
 // its FP64 instructions predicated.
 struct Terms64 {
   double id, ext, exc, g;
+  float hinv;
 };
 __device__ __noinline__ Terms64 terms_f64(double x, double wo, double v, double ve, const EgArgs A) {
   const double x2 = x * x;
   const double l = x2 > 0.0 ? log(x2) : 0.0;
   const double c_ext = A.rho0 * A.dv, c_exc = A.prefactor * A.rho0;
   return Terms64{wo * (x2 * l - x2 + 1.0), wo * x2 * ve, wo * v * fma(x, x, -1.0),
-                 2.0 * x * wo * (c_ext * (A.kT * l + ve) + 2.0 * c_exc * v)};
+                 2.0 * x * wo * (c_ext * (A.kT * l + ve) + 2.0 * c_exc * v),
+                 (float)(1.0 / (2.0 * wo * c_ext * A.kT * fmax(l + 2.0 + ve / A.kT, 1.0)))};
 }
 
 template <typename TV>
@@ -400,12 +406,14 @@ __global__ void __launch_bounds__(kRedThreads) eg_kernel(const EgArgs A) {
       acc_mac(a_exc, wd, vd * q.t);
       const DF inner = cext * (kT * q.L + ved) + cexc2 * vd;
       gi = df_to_double(twice(df_from_double_bits(x) * wd) * inner);
+      if (A.hinv) A.hinv[i] = 1.f / (2.f * wd.hi * cext.hi * kT.hi * fmaxf(q.L.hi + 2.f + ved.hi / kT.hi, 1.f));
     } else {
       const Terms64 tt = terms_f64(x, ws[o], v, ve, A);
       d_id += tt.id;
       d_ext += tt.ext;
       d_exc += tt.exc;
       gi = tt.g;
+      if (A.hinv) A.hinv[i] = tt.hinv;
     }
     A.g[i] = gi;
     const unsigned long long gb = bits_of(gi) & 0x7fffffffffffffffull;
@@ -460,6 +468,8 @@ struct PassArgs {
   double* S;
   double* part;
   unsigned* counter;
+  const float* h;  // when set: x <- (jh >= 0 ? S[jh] : 1) h * (a x + c u), element by element
+  int jh;
 };
 
 template <typename TU, typename TV>
@@ -468,7 +478,7 @@ __global__ void __launch_bounds__(kRedThreads) lbfgs_pass_kernel(const PassArgs<
   if (A.i1 >= 0) c += A.c1 * A.S[A.i1];
   if (A.i2 >= 0) c += A.c2 * A.S[A.i2];
   const double a = A.ja >= 0 ? A.S[A.ja] : A.a0;
-  const float cf = (float)c, af = (float)a;
+  const float cf = (float)c, af = (float)a, hf = A.jh >= 0 ? (float)A.S[A.jh] : 1.f;
   const bool rx = a != 0.0, dot = A.out >= 0;
   Acc<DF> acc;
   acc_zero(acc);
@@ -483,15 +493,18 @@ __global__ void __launch_bounds__(kRedThreads) lbfgs_pass_kernel(const PassArgs<
       uo[j] = as_f(A.u[i + j * stride]);
       if (dot) vo[j] = A.v[i + j * stride];
     }
+    float ho[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) ho[j] = A.h ? hf * A.h[i + j * stride] : 1.f;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      const float xv = fmaf(cf, uo[j], af * xo[j]);
+      const float xv = ho[j] * fmaf(cf, uo[j], af * xo[j]);
       A.x[i + j * stride] = xv;
       if (dot) acc_mac(acc, as_df(vo[j]), as_df(xv));
     }
   }
   for (; i < A.n; i += stride) {
-    const float xv = fmaf(cf, as_f(A.u[i]), rx ? af * A.x[i] : 0.f);
+    const float xv = (A.h ? hf * A.h[i] : 1.f) * fmaf(cf, as_f(A.u[i]), rx ? af * A.x[i] : 0.f);
     A.x[i] = xv;
     if (dot) acc_mac(acc, as_df(A.v[i]), as_df(xv));
   }
@@ -515,13 +528,14 @@ __global__ void __launch_bounds__(256) step_kernel(double* __restrict__ xn, cons
     xn[i] = fma(t, f2d_bits(d[i]), x[i]);
 }
 
-// s = t d, y = gn - g (rounded to FP32); S[o] = s . y, S[o + 1] = y . y,
-// S[orho] = 1 / (s . y) and S[ogam] = (s . y) / (y . y) when s . y > 1e-12 y . y,
-// else S[orho] = 0 (the pair then drops out of the recursion) and gamma stays
+// s = t d, y = gn - g (rounded to FP32); S[o] = s . y, S[o + 1] = y . H0 y with
+// the diagonal H0 = h (y . y without one), S[orho] = 1 / (s . y) and
+// S[ogam] = (s . y) / (y . H0 y) when s . y > 1e-12 y . H0 y, else S[orho] = 0
+// (the pair then drops out of the recursion) and gamma stays
 __global__ void __launch_bounds__(kRedThreads)
 pair_kernel(float* __restrict__ s, float* __restrict__ y, const float* __restrict__ d,
-            const double* __restrict__ gn, const double* __restrict__ g, double t, long long n, double* S, int o,
-            int orho, int ogam, double* part, unsigned* counter) {
+            const double* __restrict__ gn, const double* __restrict__ g, const float* __restrict__ h, double t,
+            long long n, double* S, int o, int orho, int ogam, double* part, unsigned* counter) {
   const float tf = (float)t;
   Acc<DF> sy, yy;
   acc_zero(sy);
@@ -534,7 +548,7 @@ pair_kernel(float* __restrict__ s, float* __restrict__ y, const float* __restric
     s[k] = sv;
     y[k] = yv;
     acc_mac(sy, as_df(sv), as_df(yv));
-    acc_mac(yy, as_df(yv), as_df(yv));
+    acc_mac(yy, as_df(h ? h[k] * yv : yv), as_df(yv));
   };
   for (; i + 3 * stride < n; i += 4 * stride) {  // four elements' loads in flight
     float dv[4];
@@ -729,8 +743,10 @@ void vext_compute(const Grid& g, const double* sv_sites, int n_solvent, const do
 }
 
 void energy_grad(const EgConst& c, const double* xi, const void* vexc, bool vexc_f32, const double* vext,
-                 const double* w, double* grad, long long n, int no, double* out, void* scratch, cudaStream_t s) {
+                 const double* w, double* grad, long long n, int no, double* out, void* scratch, float* hinv,
+                 cudaStream_t s) {
   EgArgs A{};
+  A.hinv = hinv;
   A.xi = xi;
   A.vexc = vexc;
   A.vext = vext;
@@ -772,54 +788,57 @@ void Lbfgs::bind(const Bufs& b, long long n, int m) {
 
 template <typename TU, typename TV>
 void Lbfgs::pass(float* x, const TU* u, const TV* v, double a0, int ja, double c1, int i1, double c2, int i2,
-                 double sc0, int js1, int js2, int out, cudaStream_t s) {
+                 double sc0, int js1, int js2, int out, cudaStream_t s, const float* h, int jh) {
   double* part = static_cast<double*>(b_.scratch);
-  PassArgs<TU, TV> A{x,  u,   v,   n_,  a0,   ja,  0.0, c1,   c2,
-                     i1, i2,  sc0, js1, js2, out, b_.S, part, reinterpret_cast<unsigned*>(part + kRedBlocks * 7)};
+  PassArgs<TU, TV> A{x,  u,   v,   n_,  a0,  ja,   0.0,  c1,   c2,  i1,  i2,
+                     sc0, js1, js2, out, b_.S, part, reinterpret_cast<unsigned*>(part + kRedBlocks * 7), h, jh};
   lbfgs_pass_kernel<TU, TV><<<red_blocks(n_), kRedThreads, 0, s>>>(A);
   launch_ok("L-BFGS pass launch");
 }
 
-// d = -H g by the two-loop recursion over the nh_ stored pairs; S[gd] = g . d.
-// Every coefficient comes from the device scalars: alpha_i = rho_i (s_i . q),
-// beta_i = rho_i (y_i . r), gamma of the newest accepted pair.
+// d = -H g by the two-loop recursion over the nh_ stored pairs, with the
+// initial inverse Hessian gamma P, P = 1/D the diagonal of the inverse local
+// curvature (written by the last evaluation, at x) and gamma = (s . y) /
+// (y . P y) of the newest pair (P alone before the first pair); S[gd] = g . d.  Every coefficient
+// comes from the device scalars: alpha_i = rho_i (s_i . q), beta_i =
+// rho_i (y_i . r).
 void Lbfgs::direction(cudaStream_t s) {
   float* d = b_.d;
   const double* g = b_.g;
+  const float* h0 = b_.hinv;
   auto hs = [&](int i) { return b_.hs + (size_t)i * n_; };
   auto hy = [&](int i) { return b_.hy + (size_t)i * n_; };
-  // q = -g (c = -1 from c1 with no slot: c = c0 + c1 S[i1]; c0 is 0, so use i1 < 0 and c1 unused)
-  auto neg_g = [&](const auto* v, double sc0, int js1, int js2, int out) {
+  // x <- [h0 *] (-g), dot with v
+  auto neg_g = [&](const auto* v, double sc0, int js1, int out, const float* h) {
     double* part = static_cast<double*>(b_.scratch);
     using TV = std::remove_const_t<std::remove_pointer_t<decltype(v)>>;
-    PassArgs<double, TV> A{d,  g,   v,   n_,  0.0, -1,  -1.0, 0.0,  0.0,
-                           -1, -1,  sc0, js1, js2, out, b_.S, part, reinterpret_cast<unsigned*>(part + kRedBlocks * 7)};
+    PassArgs<double, TV> A{d,   g,   v,  n_,  0.0,  -1,   -1.0, 0.0, 0.0, -1, -1,
+                           sc0, js1, -1, out, b_.S, part, reinterpret_cast<unsigned*>(part + kRedBlocks * 7), h, -1};
     lbfgs_pass_kernel<double, TV><<<red_blocks(n_), kRedThreads, 0, s>>>(A);
     launch_ok("L-BFGS pass launch");
   };
   if (nh_ == 0) {
-    neg_g(g, 1.0, -1, -1, gd());
+    neg_g(g, 1.0, -1, gd(), h0);
     return;
   }
   auto idx = [&](int j) { return ((head_ - 1 - j) % m_ + m_) % m_; };  // j = 0: newest
-  neg_g(hs(idx(0)), 0.0, rho(idx(0)), -1, alpha(idx(0)));  // alpha_newest = rho (s . q)
+  neg_g(hs(idx(0)), 0.0, rho(idx(0)), alpha(idx(0)), nullptr);  // q = -g; alpha_newest = rho (s . q)
   for (int j = 0; j < nh_; ++j) {
     const int i = idx(j);
     if (j + 1 < nh_) {  // q -= alpha_i y_i; alpha_next = rho_next (s_next . q)
       const int nx = idx(j + 1);
       pass(d, hy(i), hs(nx), 1.0, -1, -1.0, alpha(i), 0.0, -1, 0.0, rho(nx), -1, alpha(nx), s);
-    } else {  // last: beta_oldest = rho_oldest gamma (y_oldest . q)
-      pass(d, hy(i), hy(i), 1.0, -1, -1.0, alpha(i), 0.0, -1, 0.0, rho(i), gamma(), beta(0), s);
+    } else {  // last: r = gamma h0 (q - alpha y); beta_oldest = rho_oldest (y_oldest . r)
+      pass(d, hy(i), hy(i), 1.0, -1, -1.0, alpha(i), 0.0, -1, 0.0, rho(i), -1, beta(0), s, h0, gamma());
     }
   }
-  for (int j = 0; j < nh_; ++j) {  // oldest first: r = (gamma on the first pass) r + (alpha_i - beta_i) s_i
+  for (int j = 0; j < nh_; ++j) {  // oldest first: r += (alpha_i - beta_i) s_i
     const int i = idx(nh_ - 1 - j);
-    const int ja = j == 0 ? gamma() : -1;
     if (j + 1 < nh_) {
       const int nx = idx(nh_ - 2 - j);
-      pass(d, hs(i), hy(nx), 1.0, ja, 1.0, alpha(i), -1.0, beta(j), 0.0, rho(nx), -1, beta(j + 1), s);
+      pass(d, hs(i), hy(nx), 1.0, -1, 1.0, alpha(i), -1.0, beta(j), 0.0, rho(nx), -1, beta(j + 1), s);
     } else {
-      pass(d, hs(i), g, 1.0, ja, 1.0, alpha(i), -1.0, beta(j), 1.0, -1, -1, gd(), s);
+      pass(d, hs(i), g, 1.0, -1, 1.0, alpha(i), -1.0, beta(j), 1.0, -1, -1, gd(), s);
     }
   }
 }
@@ -842,15 +861,15 @@ void Lbfgs::start(double gtol, double ftol, int max_iter, cudaStream_t s) {
 }
 
 bool Lbfgs::on_eval(const double* tail, cudaStream_t s) {
-  const double c1 = 1e-4, max_first_step = 0.1;
+  const double c1 = 1e-4;
   const int max_ls = 40;
   const double gdv = tail[0];
   const double* Et = tail + 3;
   if (!first_) {
-    if (!(gdv < 0.0)) {  // not a descent direction (rounding): restart from -g
+    if (!(gdv < 0.0)) {  // not a descent direction (rounding): restart from -H0 g
       nh_ = 0;
       direction(s);
-      t_ = std::min(1.0, max_first_step / E_[4]);
+      t_ = 1.0;
       ls_ = 0;
       step(s);
       return false;
@@ -866,8 +885,8 @@ bool Lbfgs::on_eval(const double* tail, cudaStream_t s) {
     }
     // accepted: curvature pair into the ring slot head_
     pair_kernel<<<red_blocks(n_), kRedThreads, 0, s>>>(
-        b_.hs + (size_t)head_ * n_, b_.hy + (size_t)head_ * n_, b_.d, b_.gt, b_.g, t_, n_, b_.S, gd() + 1, rho(head_),
-        gamma(), static_cast<double*>(b_.scratch),
+        b_.hs + (size_t)head_ * n_, b_.hy + (size_t)head_ * n_, b_.d, b_.gt, b_.g, b_.hinv, t_, n_, b_.S, gd() + 1,
+        rho(head_), gamma(), static_cast<double*>(b_.scratch),
         reinterpret_cast<unsigned*>(static_cast<double*>(b_.scratch) + kRedBlocks * 7));
     launch_ok("pair kernel launch");
     head_ = (head_ + 1) % m_;
@@ -893,7 +912,7 @@ bool Lbfgs::on_eval(const double* tail, cudaStream_t s) {
     return true;
   }
   direction(s);
-  t_ = nh_ == 0 ? std::min(1.0, max_first_step / E_[4]) : 1.0;
+  t_ = 1.0;  // the diagonal preconditioner scales even the first step
   first_ = false;
   ls_ = 0;
   step(s);
@@ -911,7 +930,7 @@ struct mdft_solver_s {
   int no = 0, np = 0;
   mdft::EgConst c{};
   bool has_vext = false;
-  DevBuf vext, w, p, vexc, xf, x, xt, g, gt, d, hs, hy, S, scratch;
+  DevBuf vext, w, p, vexc, xf, x, xt, g, gt, d, hs, hy, hinv, S, scratch;
   mdft::Lbfgs lb;
 };
 
@@ -944,7 +963,7 @@ void evaluate(mdft_solver_s* h, const double* x, double* g, double* out, cudaStr
   mdft::detail::execute_fields(h->conv, h->p.ptr, 1, s);
   mdft::detail::proj2angl_fields(h->opt, h->p.ptr, h->vexc.ptr, 1, s);
   mdft::energy_grad(h->c, x, h->vexc.ptr, h->prec == MDFT_F32, h->has_vext ? h->vext.as<double>() : nullptr,
-                    h->w.as<double>(), g, h->n, h->no, out, h->scratch.ptr, s);
+                    h->w.as<double>(), g, h->n, h->no, out, h->scratch.ptr, h->hinv.as<float>(), s);
 }
 
 }  // namespace
@@ -995,7 +1014,8 @@ int mdft_solver_create(mdft_solver_t* out, mdft_opt_t opt, mdft_conv_t conv, con
     h->xt.alloc(fb);
     h->g.alloc(fb);
     h->gt.alloc(fb);
-    h->d.alloc(fb / 2);  // FP32 direction and curvature pairs
+    h->d.alloc(fb / 2);  // FP32 direction, curvature pairs and diagonal preconditioner
+    h->hinv.alloc(fb / 2);
     h->hs.alloc(fb / 2 * h->m);
     h->hy.alloc(fb / 2 * h->m);
     h->S.alloc(sizeof(double) * mdft::Lbfgs::nscalars(h->m));
@@ -1008,8 +1028,8 @@ int mdft_solver_create(mdft_solver_t* out, mdft_opt_t opt, mdft_conv_t conv, con
       h->has_vext = true;
     }
     h->lb.bind(mdft::Lbfgs::Bufs{h->x.as<double>(), h->xt.as<double>(), h->g.as<double>(), h->gt.as<double>(),
-                                 h->d.as<float>(), h->hs.as<float>(), h->hy.as<float>(), h->S.as<double>(),
-                                 h->scratch.ptr},
+                                 h->d.as<float>(), h->hs.as<float>(), h->hy.as<float>(), h->hinv.as<float>(),
+                                 h->S.as<double>(), h->scratch.ptr},
                h->n, h->m);
     *out = h.release();
   });

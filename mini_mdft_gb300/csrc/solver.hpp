@@ -20,17 +20,20 @@ void vext_compute(const Grid& g, const double* solvent_sites, int n_solvent, con
                   int n_solute, double vmax, double* vext, cudaStream_t s);
 
 // E and dE/dxi at xi: gradient to grad, [E_total, E_id, E_ext, E_exc,
-// max |g|] to out (device).  vexc is double, or float when vexc_f32; vext
+// max |g|] to out (device), and (hinv not null) the inverse of the local
+// terms' curvature, floored, as the minimiser's diagonal preconditioner.  vexc is double, or float when vexc_f32; vext
 // may be null.  part / counter: reduction scratch (reduction_scratch_bytes,
 // the counter zero, left zero).
 void energy_grad(const EgConst& c, const double* xi, const void* vexc, bool vexc_f32, const double* vext,
-                 const double* w, double* grad, long long n, int no, double* out, void* scratch, cudaStream_t s);
+                 const double* w, double* grad, long long n, int no, double* out, void* scratch, float* hinv,
+                 cudaStream_t s);
 size_t reduction_scratch_bytes();
 
 // xi (double) -> float copy of n values
 void to_float(float* y, const double* x, long long n, cudaStream_t s);
 
-// L-BFGS (two-loop recursion, Armijo backtracking) of one field.  The host
+// L-BFGS (two-loop recursion with a diagonal initial inverse Hessian, the
+// inverse local curvature; Armijo backtracking) of one field.  The host
 // keeps only the line-search bookkeeping; every scalar of the recursion
 // (alpha_i, rho_i, gamma, beta, g.d, s.y, y.y) lives in the field's device
 // scalar block S, and a curvature pair with s.y <= 1e-12 y.y enters with
@@ -49,6 +52,7 @@ class Lbfgs {
     float* d;    // search direction
     float* hs;   // m stored steps s_i (n floats each)
     float* hy;   // m gradient changes y_i
+    float* hinv; // diagonal preconditioner 1/D (written by the evaluation)
     double* S;   // nscalars(m) device scalars
     void* scratch;
   };
@@ -74,7 +78,7 @@ class Lbfgs {
   void step(cudaStream_t s);
   template <typename TU, typename TV>
   void pass(float* x, const TU* u, const TV* v, double a0, int ja, double c1, int i1, double c2, int i2, double sc0,
-            int js1, int js2, int out, cudaStream_t s);
+            int js1, int js2, int out, cudaStream_t s, const float* h = nullptr, int jh = -1);
   int alpha(int i) const { return i; }
   int rho(int i) const { return m_ + i; }
   int gamma() const { return 2 * m_; }
