@@ -50,6 +50,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true", help="skip the job-server leg")
     ap.add_argument("--no-minimizer", action="store_true", help="skip the solute minimiser leg")
+    ap.add_argument("--no-large-solve", action="store_true", help="skip the 128^3 / mmax 5 solve")
     ap.add_argument("--mode", choices=["full", "steps"], default="full",
                     help="steps: only W warm-up + K timed FP64 and FP32 round trips "
                          "(a short, fixed launch sequence for ncu captures)")
@@ -409,6 +410,73 @@ def minimizer_run(prec):
             "gmax_start": float(trace[0, 4]), "gmax_end": float(trace[-1, 4])}
 
 
+LARGE_SOLVE = dict(n=(128, 128, 128), box=(50.0, 50.0, 50.0), mmax=5, mrso=2, n_sites=60, seed=5, iterations=20,
+                   dq=0.05, history=5)
+
+
+def large_solve_run():
+    """The large single solve: 128^3 / 50 A, mmax 5, mrso 2 (330
+    orientations, 5.5 GB per FP64 orientation field), a 60-site synthetic
+    solute in SPC/E water, isotropic c(q) = -a exp(-q^2) with a = 15 dv/(2N)
+    (the water-like stiffness of the minimiser workloads), 20 L-BFGS
+    iterations from xi = 1, in the double-float (FP64 fields) and the mixed
+    (FP32 convolution) forms; per form the external potential, one energy +
+    gradient (CUDA events), the 20 iterations (host clock: each reads its
+    energies back) and the final energies."""
+    import torch
+
+    import mini_mdft_gb300 as M
+    from mini_mdft_gb300 import inputs as I
+    cfg = LARGE_SOLVE
+    n, box, mmax, mrso, dq = cfg["n"], cfg["box"], cfg["mmax"], cfg["mrso"], cfg["dq"]
+    N = n[0] * n[1] * n[2]
+    dv = box[0] * box[1] * box[2] / N
+    amp = 15 * dv / (2 * N)
+    idx, tab = I.isotropic_cq(mmax, mrso, I.nq_for(n, box, dq) + 2, dq, amplitude=amp)
+    rho0, pref = I.solvent_constants(I.SPCE_N0, mrso)
+    kT = I.kT()
+    su = I.synthetic_solute(cfg["n_sites"], box, seed=cfg["seed"])
+    out = {"workload": "128^3 grid, box 50 A, mmax 5, mrso 2 (330 orientations); 60-site synthetic solute in "
+                       "SPC/E water; isotropic c(q) = -%.3g exp(-q^2); %d L-BFGS iterations from xi = 1"
+                       % (amp, cfg["iterations"]), "forms": {}}
+    for prec in ("f64df", "f32"):
+        sg, ag = M.SpatialGrid(n, box), M.AngularGrid(mmax, mrso)
+        opt = M.OrientationProjectionTransform(sg, ag, M.OrientationProjectionMap(ag), precision=prec)
+        conv = M.Convolution.from_table(idx, tab, dq, sg, ag, precision=prec)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        vext = M.solute_vext(sg, ag, I.SPCE_SITES, su, 100 * kT)
+        torch.cuda.synchronize()
+        vext_s = time.perf_counter() - t0
+        solver = M.Solver(opt, conv, vext, kT=kT, rho0=rho0, prefactor=pref, history=cfg["history"])
+        xi = torch.ones_like(vext)
+        grad = torch.empty_like(xi)
+        solver.energy(xi, grad)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ev[0].record()
+        for _ in range(3):
+            solver.energy(xi, grad)
+        ev[1].record()
+        torch.cuda.synchronize()
+        eg_ms = ev[0].elapsed_time(ev[1]) / 3
+        del grad
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        trace = solver.minimize(xi, max_iter=cfg["iterations"], gtol=0.0)
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        it = len(trace) - 1
+        out["forms"][prec] = {"vext_ms": vext_s * 1e3, "energy_gradient_ms": eg_ms, "iterations": it,
+                              "ms_per_iteration": el / max(it, 1) * 1e3,
+                              "energy_start": float(trace[0, 0]), "energy_end": float(trace[-1, 0]),
+                              "gmax_start": float(trace[0, 4]), "gmax_end": float(trace[-1, 4])}
+        del solver, vext, xi, opt, conv
+        torch.cuda.empty_cache()
+    f = out["forms"]
+    out["mixed_energy_rel_diff"] = abs(f["f32"]["energy_end"] - f["f64df"]["energy_end"]) / abs(f["f64df"]["energy_end"])
+    return out
+
+
 SERVING = dict(shapes=[((32, 32, 32), (20.0, 20.0, 20.0), 20), ((64, 64, 64), (30.0, 30.0, 30.0), 4)],
                mmax=3, mrso=2, steps=(5, 15), step=2e-3, max_batch=8)
 
@@ -460,18 +528,22 @@ def serving_run(prec):
                     M.Convolution.from_table(idx, tab, dq, sg, ag, precision=prec),
                     torch.from_numpy(ag.m_w), host, dev, p, torch.empty_like(dev), torch.empty_like(dev),
                     torch.empty_like(host).pin_memory())
+    def one_at_a_time(job_list):
+        for n, box, k in job_list:
+            opt, conv, w, host, xi, p, vexc, df, out = plans[n]
+            xi.copy_(host, non_blocking=True)
+            for _ in range(k):
+                opt.angl2proj_from_xi(xi, rho0, p)
+                conv.execute(p)
+                opt.proj2angl(p, vexc)
+                M.get_delta_f(xi, vexc, w, df, rho0, pref)
+                xi -= SERVING["step"] * df
+            out.copy_(xi)
+
+    one_at_a_time([(n, box, 2) for n, box, _ in SERVING["shapes"]])  # warm-up, as for the server
     torch.cuda.synchronize()
     t1 = time.perf_counter()
-    for n, box, k in jobs:
-        opt, conv, w, host, xi, p, vexc, df, out = plans[n]
-        xi.copy_(host, non_blocking=True)
-        for _ in range(k):
-            opt.angl2proj_from_xi(xi, rho0, p)
-            conv.execute(p)
-            opt.proj2angl(p, vexc)
-            M.get_delta_f(xi, vexc, w, df, rho0, pref)
-            xi -= SERVING["step"] * df
-        out.copy_(xi)
+    one_at_a_time(jobs)
     torch.cuda.synchronize()
     seq = time.perf_counter() - t1
     lats.sort()
@@ -571,6 +643,10 @@ def serving_solute_run(prec):
             sg, ag = M.SpatialGrid(n, box), M.AngularGrid(mmax, mrso)
             plans[(si, mmax)] = (sg, ag, M.OrientationProjectionTransform(sg, ag, precision=prec),
                                  M.Convolution.from_table(idx, tab, dq, sg, ag, precision=prec))
+    for (si, mmax), (sg, ag, opt, conv) in plans.items():  # warm-up, as for the server
+        vext = M.solute_vext(sg, ag, I.SPCE_SITES, solutes[0][:2], vmax)
+        M.Solver(opt, conv, vext, kT=kT, rho0=rho0, prefactor=pref, history=5).minimize(torch.ones_like(vext),
+                                                                                           max_iter=3, gtol=0.0)
     seq = 0.0
     for k, (si, mmax, _, _) in enumerate(jobs):
         sg, ag, opt, conv = plans[(si, mmax)]
@@ -850,6 +926,8 @@ def run_ours(args):
         out["minimizer"] = minimizer_run(head)
     if rank == 0 and not args.no_serving:
         out["serving_solute"] = serving_solute_run(head)
+    if rank == 0 and not args.no_large_solve:
+        out["large_solve"] = large_solve_run()
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         rate, reps, cores, el = cpu_round_trip_rate()
         out["cpu_baseline"] = {"value": rate, "unit": "applies/s", "cores": cores, "kind": "port",

@@ -188,6 +188,7 @@ struct Group {
   std::vector<std::shared_ptr<Job>> slots;  // active jobs, slot i = field i
   std::map<int, cudaGraphExec_t> graphs;    // per active count; null: run directly
   std::map<int, int> seen;                  // steps run directly at each active count
+  bool inflight = false;                    // a step is queued on the stream
   Clock::time_point last_used;
   ~Group() {
     if (tails) cudaFreeHost(tails);
@@ -231,6 +232,7 @@ struct mdft_server_s {
   void step(Group& g);
   void enqueue_step(Group& g, int k);
   void bind_slot(Group& g, int slot);
+  void complete_step(Group& g);
   void finish(Group& g, int slot);
   void fail_group(Group& g, const std::string& msg, int code);
   void fail_job(const std::shared_ptr<Job>& j, const std::string& msg, int code);
@@ -376,7 +378,7 @@ void mdft_server_s::admit() {
       fail_job(j, e.what(), e.code);
       continue;
     }
-    if (!g || g->k >= g->B) {
+    if (!g || g->k >= g->B || g->inflight) {
       keep.push_back(j);
       continue;
     }
@@ -621,7 +623,7 @@ void mdft_server_s::run() {
       std::unique_lock<std::mutex> lk(mu);
       auto busy = [&] {
         for (auto& kv : groups)
-          if (kv.second->k > 0) return true;
+          if (kv.second->k > 0 || kv.second->inflight) return true;
         return false;
       };
       cv_work.wait(lk, [&] { return stop || !incoming.empty() || busy() || !pending.empty(); });
@@ -632,41 +634,61 @@ void mdft_server_s::run() {
       }
     }
     admit();
-    std::vector<Group*> live;
-    for (auto& kv : groups)
-      if (kv.second->k > 0) live.push_back(kv.second.get());
-    if (live.empty()) {
+    // Each group advances on its own: a group whose step has finished takes
+    // its results and launches its next step at once, without waiting for
+    // the other groups' steps (small grids step several times per step of a
+    // large one, and the groups' work overlaps on the device).
+    bool progress = false, live = false;
+    for (auto& kv : groups) {
+      Group* g = kv.second.get();
+      if (g->inflight) {
+        const cudaError_t q = cudaStreamQuery(g->stream);
+        if (q == cudaErrorNotReady) {
+          live = true;
+          continue;
+        }
+        g->inflight = false;
+        progress = true;
+        try {
+          ck(q, "server step");
+          complete_step(*g);
+        } catch (const Error& e) {
+          fail_group(*g, e.what(), e.code);
+        }
+      }
+      if (g->k > 0) {
+        live = true;
+        try {
+          step(*g);
+          g->inflight = true;
+          progress = true;
+        } catch (const Error& e) {
+          fail_group(*g, e.what(), e.code);
+        }
+      }
+    }
+    if (!live) {
       // queued jobs that cannot be placed yet and nothing running: wait for news
       std::unique_lock<std::mutex> lk(mu);
       cv_work.wait_for(lk, std::chrono::milliseconds(2), [&] { return stop || !incoming.empty(); });
-      continue;
+    } else if (!progress) {
+      std::this_thread::sleep_for(std::chrono::microseconds(20));
     }
-    for (Group* g : live) {
-      try {
-        step(*g);
-      } catch (const Error& e) {
-        fail_group(*g, e.what(), e.code);
-      }
-    }
-    for (Group* g : live) {
-      if (g->k == 0) continue;
-      try {
-        ck(cudaStreamSynchronize(g->stream), "server step");
-        for (auto& j : g->slots) j->steps_done += 1;
-        if (g->kind == 1) {
-          // every minimiser takes its evaluation and queues its next trial
-          // point (highest slot first, so that a finished job's slot is
-          // refilled by a job that has already queued its own)
-          for (int s = g->k - 1; s >= 0; --s)
-            if (g->lb[s].on_eval(g->tails + 8 * s, g->stream)) finish(*g, s);
-        } else {
-          for (int s = g->k - 1; s >= 0; --s)
-            if (g->slots[s]->steps_done >= g->slots[s]->n_steps) finish(*g, s);
-        }
-      } catch (const Error& e) {
-        fail_group(*g, e.what(), e.code);
-      }
-    }
+  }
+}
+
+// The group's step has finished: every job records it, solute jobs' minimisers
+// queue their next trial points, finished jobs leave.
+void mdft_server_s::complete_step(Group& g) {
+  for (auto& j : g.slots) j->steps_done += 1;
+  if (g.kind == 1) {
+    // highest slot first, so that a finished job's slot is refilled by a job
+    // that has already queued its own next point
+    for (int s = g.k - 1; s >= 0; --s)
+      if (g.lb[s].on_eval(g.tails + 8 * s, g.stream)) finish(g, s);
+  } else {
+    for (int s = g.k - 1; s >= 0; --s)
+      if (g.slots[s]->steps_done >= g.slots[s]->n_steps) finish(g, s);
   }
 }
 
