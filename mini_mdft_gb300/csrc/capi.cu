@@ -746,11 +746,11 @@ int mdft_get_delta_f(const void* xi, const void* vexc, const double* w, void* de
     if (precision != MDFT_F32)  // MDFT_F64 and MDFT_F64_DF fields are double
       mdft::launch_delta_f<double>(static_cast<const double*>(xi), static_cast<const double*>(vexc), w,
                                    static_cast<double*>(delta_f), ff_dev, nxyz, no, rho0, prefactor,
-                                   scratch.p, s);
+                                   scratch.p, s, precision == MDFT_F64);
     else
       mdft::launch_delta_f<float>(static_cast<const float*>(xi), static_cast<const float*>(vexc), w,
                                   static_cast<float*>(delta_f), ff_dev, nxyz, no, rho0, prefactor,
-                                  scratch.p, s);
+                                  scratch.p, s, false);
   });
 }
 

@@ -553,9 +553,11 @@ size_t delta_f_partials(size_t nxyz, int no);
 // `code` (for extern "C" entry points defined outside capi.cu).
 int record_error(int code, const std::string& msg);
 
+// fp64: FP64 arithmetic (the MDFT_F64 form); otherwise double-float on the
+// FP32 pipes (double fields) or float (float fields)
 template <typename T>
 void launch_delta_f(const T* xi, const T* vexc, const double* w, T* df,
                     double* ff, size_t nxyz, int no, double rho0,
-                    double prefactor, void* work, cudaStream_t s);
+                    double prefactor, void* work, cudaStream_t s, bool fp64);
 
 }  // namespace mdft

@@ -1,12 +1,12 @@
 // energy.cu -- get_delta_rho and get_delta_f (common/MDFT_Solvent.hpp:578-660).
 //
-// get_delta_f streams xi and vexc once: each CTA stages a tile of grid points
-// (the (nxyz, no) rows are contiguous, so the tile is one contiguous run),
-// writes delta_f = 2 rho0 xi vexc on the way, sums each point's orientations
-// in index order, and reduces the per-point energies of the tile with
-// compensated (two-sum) arithmetic.  The tile sums go to a small partials
-// array; the last CTA to finish adds them in a fixed order, so ff is
-// deterministic and independent of scheduling.
+// get_delta_f streams xi and vexc once: each CTA takes tiles of grid points
+// in turn (the (nxyz, no) rows are contiguous, so a tile is one contiguous
+// run), writes delta_f = 2 rho0 xi vexc on the way, and sums each tile's
+// energy terms in double-float (compensated) arithmetic.  The tile sums go to a
+// small partials array; the last CTA to finish adds them in a fixed order,
+// so ff is deterministic and independent of scheduling.
+#include <algorithm>
 #include <mutex>
 #include <string>
 
@@ -51,56 +51,136 @@ __device__ __forceinline__ DD warp_dd_sum(DD v) {
   return v;
 }
 
-template <typename T>
+// df = 2 rho0 xi vexc in the field type: double-float arithmetic and one FP64
+// add to store (FP64 fields), plain float (FP32 fields, as the reference's
+// float instantiation computes it)
+__device__ __forceinline__ double df_value(double x, double v, DF two_rho0) {
+  return df_to_double((two_rho0 * df_from_double_bits(x)) * df_from_double_bits(v));
+}
+__device__ __forceinline__ float df_value(float x, float v, DF two_rho0) { return two_rho0.hi * x * v; }
+__device__ __forceinline__ DF as_pair(double x) { return df_from_double_bits(x); }
+__device__ __forceinline__ DF as_pair(float x) { return DF(x, 0.f); }
+
+// Tiles of kEnergyPoints grid points (contiguous runs of the (nxyz, no)
+// fields).  Every element's energy term vexc w (xi^2 - 1) is formed in
+// double-float on the FP32 pipes (the FP64 pipe of this GPU is 1/64 as
+// wide; in FP64 this kernel is bound by it at ~5 FP64 operations per
+// element) and accumulated in a Dot2 sum per thread -- or, for the FP64
+// form (F64), in FP64 as the reference does; the threads' sums are combined
+// as double-double values in a fixed order (warps, then the CTA's warps,
+// then the CTAs' partials in the last CTA), so ff is deterministic.
+template <typename T, bool F64>
 __global__ void __launch_bounds__(kEnergyThreads)
 delta_f_kernel(const T* __restrict__ xi, const T* __restrict__ vexc, const double* __restrict__ w,
                T* __restrict__ df, double* __restrict__ ff, size_t nxyz, int no, double rho0,
                double prefactor, double2* __restrict__ partials, unsigned* __restrict__ counter) {
   extern __shared__ __align__(16) unsigned char sm[];
-  double* ws = reinterpret_cast<double*>(sm);            // (no)
-  double* term = ws + no;                                // (kEnergyPoints * no)
-  __shared__ double ppt[kEnergyPoints];
+  float2* ws = reinterpret_cast<float2*>(sm);  // w as double-float pairs (no)
+  // per-warp sums of a tile, double-buffered by tile parity (one barrier per
+  // tile): double-float pairs, or doubles for the FP64 form
+  __shared__ float2 wsf[2][kEnergyThreads / 32];
+  __shared__ double wsd[2][kEnergyThreads / 32];
   __shared__ bool last;
-  const int tid = threadIdx.x, bd = blockDim.x;
-  const size_t pt0 = (size_t)blockIdx.x * kEnergyPoints;
-  const int cnt = (int)min((size_t)kEnergyPoints, nxyz - pt0);
-  for (int i = tid; i < no; i += bd) ws[i] = w[i];
-  __syncthreads();
-  const size_t g0 = pt0 * (size_t)no;
-  const T two_rho0 = (T)(2.0 * rho0);
-  for (int i = tid; i < cnt * no; i += bd) {
-    const T x = xi[g0 + i], v = vexc[g0 + i];
-    df[g0 + i] = two_rho0 * x * v;
-    term[i] = (double)v * ws[i % no] * ((double)x * (double)x - 1.0);
+  const int tid = threadIdx.x, bd = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = bd / 32;
+  int buf = 0;
+  for (int i = tid; i < no; i += bd) {
+    const DF wd = df_from_double_bits(w[i]);
+    ws[i] = make_float2(wd.hi, wd.lo);
   }
   __syncthreads();
-  if (tid < kEnergyPoints) {
-    double s = 0.0;
-    if (tid < cnt)
-      for (int io = 0; io < no; ++io) s += term[tid * no + io];
-    ppt[tid] = tid < cnt ? rho0 * s * prefactor : 0.0;
-  }
-  __syncthreads();
-  if (tid < 32) {
-    DD v = warp_dd_sum(DD{ppt[tid], 0.0});
-    if (tid == 0) {
-      partials[blockIdx.x] = make_double2(v.hi, v.lo);
-      __threadfence();
-      const unsigned done = atomicAdd(counter, 1u);
-      last = (done == gridDim.x - 1);
+  const float tr_h = (float)(2.0 * rho0);
+  const DF two_rho0(tr_h, (float)(2.0 * rho0 - (double)tr_h)), one(1.f, 0.f);
+  const double sc = rho0 * prefactor;
+  const size_t ntiles = (nxyz + kEnergyPoints - 1) / kEnergyPoints;
+  const int ostep = bd % no;
+  // the CTA takes tiles blockIdx.x, blockIdx.x + gridDim.x, ...; each tile's
+  // sum goes to its own partial
+  for (size_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const size_t pt0 = tile * kEnergyPoints;
+    const int cnt = (int)min((size_t)kEnergyPoints, nxyz - pt0);
+    const size_t g0 = pt0 * (size_t)no;
+    const int n = cnt * no;
+    Acc<DF> acc;
+    acc_zero(acc);
+    double acc64 = 0.0;
+    int o = tid % no;
+    auto one_elem = [&](int i, T x, T v) {
+      if constexpr (F64) {
+        df[g0 + i] = (T)(2.0 * rho0) * x * v;
+        acc64 = fma((double)v * w[o], fma((double)x, (double)x, -1.0), acc64);
+      } else {
+        df[g0 + i] = df_value(x, v, two_rho0);
+        const DF xd = as_pair(x);
+        const float2 w2 = ws[o];
+        acc_mac(acc, as_pair(v) * DF(w2.x, w2.y), xd * xd - one);
+      }
+      o += ostep;
+      if (o >= no) o -= no;
+    };
+    int i = tid;
+    for (; i + 3 * bd < n; i += 4 * bd) {  // four elements' loads in flight
+      T x[4], v[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        x[j] = xi[g0 + i + j * bd];
+        v[j] = vexc[g0 + i + j * bd];
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) one_elem(i + j * bd, x[j], v[j]);
     }
+    for (; i < n; i += bd) one_elem(i, xi[g0 + i], vexc[g0 + i]);
+    // the tile's sum: warps by shuffles, then warp 0 over the warps --
+    // double-float additions on the FP32 pipe (plain FP64 adds for the FP64
+    // form); the tile's share of ff = rho0 prefactor sum becomes a
+    // double-double partial
+    if constexpr (F64) {
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) acc64 += __shfl_down_sync(0xffffffffu, acc64, off);
+      if (lane == 0) wsd[buf][wid] = acc64;
+    } else {
+      DF a = acc_get(acc);
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1)
+        a = a + DF(__shfl_down_sync(0xffffffffu, a.hi, off), __shfl_down_sync(0xffffffffu, a.lo, off));
+      if (lane == 0) wsf[buf][wid] = make_float2(a.hi, a.lo);
+    }
+    __syncthreads();
+    if (wid == 0) {
+      if constexpr (F64) {
+        double t = lane < nw ? wsd[buf][lane] : 0.0;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) t += __shfl_down_sync(0xffffffffu, t, off);
+        if (lane == 0) partials[tile] = make_double2(t * sc, 0.0);
+      } else {
+        const float2 q = lane < nw ? wsf[buf][lane] : make_float2(0.f, 0.f);
+        DF t(q.x, q.y);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1)
+          t = t + DF(__shfl_down_sync(0xffffffffu, t.hi, off), __shfl_down_sync(0xffffffffu, t.lo, off));
+        if (lane == 0) {
+          const DD u = two_sum((double)t.hi * sc, (double)t.lo * sc);
+          partials[tile] = make_double2(u.hi, u.lo);
+        }
+      }
+    }
+    buf ^= 1;
+  }
+  if (tid == 0) {
+    __threadfence();
+    const unsigned done = atomicAdd(counter, 1u);
+    last = (done == gridDim.x - 1);
   }
   __syncthreads();
   if (!last || tid >= 32) return;
   __threadfence();
-  DD acc{0.0, 0.0};
-  for (unsigned b = tid; b < gridDim.x; b += 32) {
+  DD acc2{0.0, 0.0};
+  for (size_t b = tid; b < ntiles; b += 32) {
     const double2 q = __ldcg(&partials[b]);
-    acc = dd_add(acc, DD{q.x, q.y});
+    acc2 = dd_add(acc2, DD{q.x, q.y});
   }
-  acc = warp_dd_sum(acc);
+  acc2 = warp_dd_sum(acc2);
   if (tid == 0) {
-    *ff = acc.hi + acc.lo;
+    *ff = acc2.hi + acc2.lo;
     *counter = 0u;  // leave the counter ready for the next call
   }
 }
@@ -123,12 +203,11 @@ void launch_delta_rho(const T* xi, T* dr, size_t n, double rho0, cudaStream_t s)
 
 template <typename T>
 void launch_delta_f(const T* xi, const T* vexc, const double* w, T* df, double* ff, size_t nxyz,
-                    int no, double rho0, double prefactor, void* work, cudaStream_t s) {
+                    int no, double rho0, double prefactor, void* work, cudaStream_t s, bool fp64) {
   const size_t nb = delta_f_partials(nxyz, no);
   throw_if(nb > 0x7fffffffULL, "grid too large", 4);
-  const size_t smem = sizeof(double) * ((size_t)no + (size_t)kEnergyPoints * no);
-  throw_if(smem > 200 * 1024, "too many orientations for the energy kernel", 4);
-  if (smem > 48 * 1024) allow_max_smem(delta_f_kernel<T>, smem, "delta_f smem attribute");
+  const size_t smem = sizeof(float2) * (size_t)no;
+  throw_if(smem > 48 * 1024, "too many orientations for the energy kernel", 4);
   double2* partials = static_cast<double2*>(work);
   unsigned* counter = reinterpret_cast<unsigned*>(partials + nb);
   if (nb == 0) {
@@ -136,17 +215,23 @@ void launch_delta_f(const T* xi, const T* vexc, const double* w, T* df, double* 
     return;
   }
   clear_stale_error();
-  delta_f_kernel<T><<<(unsigned)nb, kEnergyThreads, smem, s>>>(xi, vexc, w, df, ff, nxyz, no, rho0,
-                                                               prefactor, partials, counter);
+  // at most 8 CTAs per SM, each looping over tiles (one partial per tile)
+  const unsigned grid = (unsigned)std::min<size_t>(nb, 152 * 8);
+  if (fp64 && sizeof(T) == 8)
+    delta_f_kernel<T, true><<<grid, kEnergyThreads, smem, s>>>(xi, vexc, w, df, ff, nxyz, no, rho0, prefactor,
+                                                               partials, counter);
+  else
+    delta_f_kernel<T, false><<<grid, kEnergyThreads, smem, s>>>(xi, vexc, w, df, ff, nxyz, no, rho0, prefactor,
+                                                                partials, counter);
   launch_check("delta_f kernel launch");
 }
 
 template void launch_delta_rho<double>(const double*, double*, size_t, double, cudaStream_t);
 template void launch_delta_rho<float>(const float*, float*, size_t, double, cudaStream_t);
 template void launch_delta_f<double>(const double*, const double*, const double*, double*, double*,
-                                     size_t, int, double, double, void*, cudaStream_t);
+                                     size_t, int, double, double, void*, cudaStream_t, bool);
 template void launch_delta_f<float>(const float*, const float*, const double*, float*, double*,
-                                    size_t, int, double, double, void*, cudaStream_t);
+                                    size_t, int, double, double, void*, cudaStream_t, bool);
 
 
 // ---------------------------------------------------------------------------
@@ -223,10 +308,11 @@ extern "C" int mdft_get_delta_f_noalloc(const void* xi, const void* vexc, const 
     cuda_check(cudaMemsetAsync(counter, 0, sizeof(unsigned), s), "cudaMemsetAsync(fixed scratch counter)");
     if (precision != 1)  // MDFT_F64 and MDFT_F64_DF fields are double
       launch_delta_f<double>(static_cast<const double*>(xi), static_cast<const double*>(vexc), w,
-                             static_cast<double*>(delta_f), ff_dev, nxyz, no, rho0, prefactor, scratch, s);
+                             static_cast<double*>(delta_f), ff_dev, nxyz, no, rho0, prefactor, scratch, s,
+                             precision == 0);
     else
       launch_delta_f<float>(static_cast<const float*>(xi), static_cast<const float*>(vexc), w,
-                            static_cast<float*>(delta_f), ff_dev, nxyz, no, rho0, prefactor, scratch, s);
+                            static_cast<float*>(delta_f), ff_dev, nxyz, no, rho0, prefactor, scratch, s, false);
     return 0;
   } catch (const Error& e) {
     return record_error(e.code, e.what());

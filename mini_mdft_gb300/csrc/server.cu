@@ -477,13 +477,13 @@ void mdft_server_s::enqueue_step(Group& g, int k) {
           reinterpret_cast<const double*>(g.xi.as<unsigned char>() + fb * j),
           reinterpret_cast<const double*>(g.vexc.as<unsigned char>() + fb * j), g.w.as<double>(),
           reinterpret_cast<double*>(g.df.as<unsigned char>() + fb * j), g.ff_cur.as<double>() + j, (size_t)g.N,
-          g.no, g.rho0, g.prefactor, sc, s);
+          g.no, g.rho0, g.prefactor, sc, s, g.prec == MDFT_F64);
     else
       mdft::launch_delta_f<float>(
           reinterpret_cast<const float*>(g.xi.as<unsigned char>() + fb * j),
           reinterpret_cast<const float*>(g.vexc.as<unsigned char>() + fb * j), g.w.as<double>(),
           reinterpret_cast<float*>(g.df.as<unsigned char>() + fb * j), g.ff_cur.as<double>() + j, (size_t)g.N,
-          g.no, g.rho0, g.prefactor, sc, s);
+          g.no, g.rho0, g.prefactor, sc, s, false);
   }
   trace_kernel<<<(k + 127) / 128, 128, 0, s>>>(g.ff_cur.as<double>(), g.trace.as<double>(), g.step_ctr.as<int>(), k,
                                                 g.cap);
