@@ -51,9 +51,10 @@ def parse_args():
     ap.add_argument("--no-serving", action="store_true", help="skip the job-server leg")
     ap.add_argument("--no-minimizer", action="store_true", help="skip the solute minimiser leg")
     ap.add_argument("--no-large-solve", action="store_true", help="skip the 128^3 / mmax 5 solve")
-    ap.add_argument("--mode", choices=["full", "steps"], default="full",
-                    help="steps: only W warm-up + K timed FP64 and FP32 round trips "
-                         "(a short, fixed launch sequence for ncu captures)")
+    ap.add_argument("--mode", choices=["full", "steps", "energy"], default="full",
+                    help="steps: only W warm-up + K timed FP64 and FP32 round trips; energy: "
+                         "get_delta_f and a short solute minimisation (short, fixed launch "
+                         "sequences for ncu captures)")
     return ap.parse_args()
 
 
@@ -346,6 +347,45 @@ def read_traffic(kernel):
 # (1/S(0) - 1 with the structure factor S(0) ~ 0.06)
 CQ_AMPLITUDE = 3e-6
 MINIMIZER = dict(n_sites=12, seed=3, vmax_kT=100.0, history=5, iterations=10, amplitude=CQ_AMPLITUDE)
+
+
+def energy_launches():
+    """A fixed launch sequence of the energy, gradient and minimiser kernels
+    for ncu captures, on the headline workload (64^3 / 30 A / mmax 3):
+    get_delta_f twice on FP64 fields (FP64 form) and twice on FP32 fields,
+    then with the 12-site solute of the minimiser leg (double-float form)
+    the external potential, two energy evaluations and 4 L-BFGS
+    iterations."""
+    import torch
+
+    import mini_mdft_gb300 as M
+    from mini_mdft_gb300 import inputs as I
+    n, box, mmax, mrso, dq = (WORKLOAD[k] for k in ("n", "box", "mmax", "mrso", "dq"))
+    N = n[0] * n[1] * n[2]
+    sg, ag = M.SpatialGrid(n, box), M.AngularGrid(mmax, mrso)
+    rho0, pref = I.solvent_constants(I.SPCE_N0, mrso)
+    kT = I.kT()
+    w = torch.from_numpy(ag.m_w).cuda()
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    for dt in (torch.float64, torch.float32):
+        xi = torch.rand((N, ag.m_ntheta, ag.m_nphi, ag.m_npsi), generator=gen, device="cuda", dtype=dt) * 0.2 + 0.9
+        vexc = torch.rand(xi.shape, generator=gen, device="cuda", dtype=dt)
+        df = torch.empty_like(xi)
+        ff = torch.zeros(1, dtype=torch.float64, device="cuda")
+        for _ in range(2):
+            M.get_delta_f(xi, vexc, w, df, rho0, pref, ff_out=ff)
+    idx, tab = I.isotropic_cq(mmax, mrso, I.nq_for(n, box, 0.05), 0.05, amplitude=CQ_AMPLITUDE)
+    opt = M.OrientationProjectionTransform(sg, ag, M.OrientationProjectionMap(ag), precision="f64df")
+    conv = M.Convolution.from_table(idx, tab, 0.05, sg, ag, precision="f64df")
+    vext = M.solute_vext(sg, ag, I.SPCE_SITES, I.synthetic_solute(12, box, seed=3), 100 * kT)
+    solver = M.Solver(opt, conv, vext, kT=kT, rho0=rho0, prefactor=pref, history=5)
+    x = torch.ones_like(vext)
+    g = torch.empty_like(x)
+    for _ in range(2):
+        solver.energy(x, g)
+    trace = solver.minimize(x, max_iter=4, gtol=0.0)
+    torch.cuda.synchronize()
+    return {"mode": "energy", "iterations": len(trace) - 1, "energy_end": float(trace[-1, 0])}
 
 
 def minimizer_run(prec):
@@ -785,6 +825,10 @@ def run_ours(args):
     s = sizes()
     K, W = args.steps, args.warmup
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    if args.mode == "energy":
+        if rank == 0:
+            print(json.dumps(energy_launches()), flush=True)
+        return
     forms = ("f64", "f64df", "f32")
     P = {f: make_problem(f) for f in forms}
     if args.mode == "steps":
