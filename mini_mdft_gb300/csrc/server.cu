@@ -633,38 +633,40 @@ void mdft_server_s::run() {
         incoming.pop_front();
       }
     }
-    admit();
     // Each group advances on its own: a group whose step has finished takes
-    // its results and launches its next step at once, without waiting for
-    // the other groups' steps (small grids step several times per step of a
-    // large one, and the groups' work overlaps on the device).
+    // its results, refills its free slots from the queue, and launches its
+    // next step at once, without waiting for the other groups' steps (small
+    // grids step several times per step of a large one, and the groups'
+    // work overlaps on the device).
     bool progress = false, live = false;
     for (auto& kv : groups) {
       Group* g = kv.second.get();
-      if (g->inflight) {
-        const cudaError_t q = cudaStreamQuery(g->stream);
-        if (q == cudaErrorNotReady) {
-          live = true;
-          continue;
-        }
-        g->inflight = false;
-        progress = true;
-        try {
-          ck(q, "server step");
-          complete_step(*g);
-        } catch (const Error& e) {
-          fail_group(*g, e.what(), e.code);
-        }
-      }
-      if (g->k > 0) {
+      if (!g->inflight) continue;
+      const cudaError_t q = cudaStreamQuery(g->stream);
+      if (q == cudaErrorNotReady) {
         live = true;
-        try {
-          step(*g);
-          g->inflight = true;
-          progress = true;
-        } catch (const Error& e) {
-          fail_group(*g, e.what(), e.code);
-        }
+        continue;
+      }
+      g->inflight = false;
+      progress = true;
+      try {
+        ck(q, "server step");
+        complete_step(*g);
+      } catch (const Error& e) {
+        fail_group(*g, e.what(), e.code);
+      }
+    }
+    admit();  // every group not in flight takes queued jobs into its free slots
+    for (auto& kv : groups) {
+      Group* g = kv.second.get();
+      if (g->inflight || g->k == 0) continue;
+      live = true;
+      try {
+        step(*g);
+        g->inflight = true;
+        progress = true;
+      } catch (const Error& e) {
+        fail_group(*g, e.what(), e.code);
       }
     }
     if (!live) {
