@@ -4,7 +4,7 @@ oracle on the same seeded inputs.
 Tolerances (max-norm relative error, max|gpu - oracle| / max|oracle|):
   FP64 plain form: 1e-12 (projections, convolved fields, energy, gradient);
   FP32 mixed form: 1e-4 for the fields, 1e-6 for the excess energy (the
-  spec bound for the mixed form is on the energy).
+  mixed form's accuracy target is stated on the excess free energy).
 """
 import numpy as np
 import pytest

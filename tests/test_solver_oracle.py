@@ -127,3 +127,30 @@ def test_excess_gradient_is_exact_for_a_symmetric_cq():
         fd = (fp - fm) / (2 * h)
         errs.append(abs(fd - (gr * d).sum()) / abs(fd))
     assert errs[1] < 1e-6 and errs[1] < errs[0] / 50  # second-order convergence
+
+
+def test_synthetic_solute_follows_its_recipe():
+    box = (30.0, 30.0, 30.0)
+    su = I.synthetic_solute(12, box, seed=3)
+    assert su.shape == (12, 6)
+    assert abs(su[:, 0].sum()) < 1e-14  # neutral
+    assert np.all((su[:, 1] >= 2.5) & (su[:, 1] <= 4.0))
+    assert np.all((su[:, 2] >= 0.1) & (su[:, 2] <= 1.0))
+    assert np.all(np.abs(su[:, 3:6] - 15.0) <= 5.0)  # central 10 A cube
+    assert np.array_equal(su, I.synthetic_solute(12, box, seed=3))
+    assert not np.array_equal(su, I.synthetic_solute(12, box, seed=4))
+
+
+def test_isotropic_cq_has_only_the_zero_entry():
+    idx, tab = I.isotropic_cq(3, 2, 50, 0.05, amplitude=2e-3, s=1.5)
+    zero = (idx == 0).all(axis=0)
+    assert zero.sum() == 1
+    q = np.arange(50) * 0.05
+    assert np.allclose(tab[zero][0], -2e-3 * np.exp(-1.5 * q * q), rtol=0, atol=1e-18)
+    assert not np.any(tab[~zero])
+
+
+def test_solvent_constants_match_the_tip3p_helper():
+    assert I.solvent_constants(I.TIP3P_N0, 2) == pytest.approx(I.tip3p_constants(2), rel=1e-15)
+    rho0, pref = I.solvent_constants(I.SPCE_N0, 2)
+    assert pref == pytest.approx(-I.kT() / rho0, rel=1e-14)  # -2 kT 4 pi^2 / (mrso n0) = -kT / rho0
