@@ -1,11 +1,12 @@
 // energy.cu -- get_delta_rho and get_delta_f (common/MDFT_Solvent.hpp:578-660).
 //
-// get_delta_f streams xi and vexc once: each CTA takes tiles of grid points
-// in turn (the (nxyz, no) rows are contiguous, so a tile is one contiguous
-// run), writes delta_f = 2 rho0 xi vexc on the way, and sums each tile's
-// energy terms in double-float (compensated) arithmetic.  The tile sums go to a
-// small partials array; the last CTA to finish adds them in a fixed order,
-// so ff is deterministic and independent of scheduling.
+// get_delta_f streams xi and vexc once: each CTA takes one contiguous run of
+// grid points (the (nxyz, no) rows are contiguous), writes
+// delta_f = 2 rho0 xi vexc on the way, and sums its energy terms in
+// double-float (compensated) arithmetic.  The grid is one wave of CTAs of
+// equal runs; each CTA leaves one partial sum and the last CTA to finish adds
+// them in a fixed order, so ff is deterministic and independent of
+// scheduling.
 #include <algorithm>
 #include <mutex>
 #include <string>
@@ -17,7 +18,7 @@ namespace mdft {
 namespace {
 
 constexpr int kEnergyThreads = 256;
-constexpr int kEnergyPoints = 32;  // grid points per CTA
+constexpr int kEnergyPoints = 32;  // grid points per partial slot of the scratch (sizing unit)
 
 template <typename T>
 __global__ void delta_rho_kernel(const T* __restrict__ xi, T* __restrict__ dr, size_t n, T rho0) {
@@ -61,127 +62,154 @@ __device__ __forceinline__ float df_value(float x, float v, DF two_rho0) { retur
 __device__ __forceinline__ DF as_pair(double x) { return df_from_double_bits(x); }
 __device__ __forceinline__ DF as_pair(float x) { return DF(x, 0.f); }
 
-// Tiles of kEnergyPoints grid points (contiguous runs of the (nxyz, no)
-// fields).  Every element's energy term vexc w (xi^2 - 1) is formed in
-// double-float on the FP32 pipes (the FP64 pipe of this GPU is 1/64 as
-// wide; in FP64 this kernel is bound by it at ~5 FP64 operations per
-// element) and accumulated in a Dot2 sum per thread -- or, for the FP64
-// form (F64), in FP64 as the reference does; the threads' sums are combined
-// as double-double values in a fixed order (warps, then the CTA's warps,
-// then the CTAs' partials in the last CTA), so ff is deterministic.
+// One contiguous run of `chunk` grid points per CTA (the last CTA's run may
+// be shorter).  Every element's energy term vexc w (xi^2 - 1) is formed in
+// double-float on the FP32 pipes (the FP64 pipe of this GPU is 1/64 as wide;
+// in FP64 this kernel is bound by it at ~5 FP64 operations per element) and
+// accumulated in a Dot2 sum per thread -- or, for the FP64 form (F64), in
+// FP64 as the reference does.  The threads' sums are combined in a fixed
+// order (warps by shuffles, then warp 0 over the CTA's warps) into one
+// partial per CTA; the last CTA to finish adds the partials with all its
+// threads in the same fixed order.  The combining runs in double-float on
+// the FP32 pipes (plain FP64 adds for the FP64 form): a double-double sum of
+// ~1000 partials by one warp spends hundreds of microseconds on the FP64
+// pipe while every other SM idles.
 template <typename T, bool F64>
 __global__ void __launch_bounds__(kEnergyThreads)
 delta_f_kernel(const T* __restrict__ xi, const T* __restrict__ vexc, const double* __restrict__ w,
-               T* __restrict__ df, double* __restrict__ ff, size_t nxyz, int no, double rho0,
-               double prefactor, double2* __restrict__ partials, unsigned* __restrict__ counter) {
+               T* __restrict__ df, double* __restrict__ ff, size_t nxyz, int no, size_t chunk, double rho0,
+               double prefactor, void* __restrict__ partials, unsigned* __restrict__ counter) {
   extern __shared__ __align__(16) unsigned char sm[];
   float2* ws = reinterpret_cast<float2*>(sm);  // w as double-float pairs (no)
-  // per-warp sums of a tile, double-buffered by tile parity (one barrier per
-  // tile): double-float pairs, or doubles for the FP64 form
-  __shared__ float2 wsf[2][kEnergyThreads / 32];
-  __shared__ double wsd[2][kEnergyThreads / 32];
+  __shared__ float2 wsf[kEnergyThreads / 32];  // per-warp sums (double-float)
+  __shared__ double wsd[kEnergyThreads / 32];  // per-warp sums (FP64 form)
   __shared__ bool last;
+  float2* pf = static_cast<float2*>(partials);
+  double* pd = static_cast<double*>(partials);
   const int tid = threadIdx.x, bd = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = bd / 32;
-  int buf = 0;
-  for (int i = tid; i < no; i += bd) {
-    const DF wd = df_from_double_bits(w[i]);
-    ws[i] = make_float2(wd.hi, wd.lo);
+  if constexpr (!F64) {
+    for (int i = tid; i < no; i += bd) {
+      const DF wd = df_from_double_bits(w[i]);
+      ws[i] = make_float2(wd.hi, wd.lo);
+    }
+    __syncthreads();
   }
-  __syncthreads();
   const float tr_h = (float)(2.0 * rho0);
   const DF two_rho0(tr_h, (float)(2.0 * rho0 - (double)tr_h)), one(1.f, 0.f);
   const double sc = rho0 * prefactor;
-  const size_t ntiles = (nxyz + kEnergyPoints - 1) / kEnergyPoints;
+  const size_t pt0 = (size_t)blockIdx.x * chunk;
+  const int n = pt0 < nxyz ? (int)((min(chunk, nxyz - pt0)) * (size_t)no) : 0;
+  const T* __restrict__ xs = xi + pt0 * (size_t)no;
+  const T* __restrict__ vs = vexc + pt0 * (size_t)no;
+  T* __restrict__ ds = df + pt0 * (size_t)no;
+  Acc<DF> acc;
+  acc_zero(acc);
+  double acc64 = 0.0;
+  // the run starts on a grid point, so element i has orientation i mod no
+  int o = tid % no;
   const int ostep = bd % no;
-  // the CTA takes tiles blockIdx.x, blockIdx.x + gridDim.x, ...; each tile's
-  // sum goes to its own partial
-  for (size_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const size_t pt0 = tile * kEnergyPoints;
-    const int cnt = (int)min((size_t)kEnergyPoints, nxyz - pt0);
-    const size_t g0 = pt0 * (size_t)no;
-    const int n = cnt * no;
-    Acc<DF> acc;
-    acc_zero(acc);
-    double acc64 = 0.0;
-    int o = tid % no;
-    auto one_elem = [&](int i, T x, T v) {
-      if constexpr (F64) {
-        df[g0 + i] = (T)(2.0 * rho0) * x * v;
-        acc64 = fma((double)v * w[o], fma((double)x, (double)x, -1.0), acc64);
-      } else {
-        df[g0 + i] = df_value(x, v, two_rho0);
-        const DF xd = as_pair(x);
-        const float2 w2 = ws[o];
-        acc_mac(acc, as_pair(v) * DF(w2.x, w2.y), xd * xd - one);
-      }
-      o += ostep;
-      if (o >= no) o -= no;
-    };
-    int i = tid;
-    for (; i + 3 * bd < n; i += 4 * bd) {  // four elements' loads in flight
-      T x[4], v[4];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        x[j] = xi[g0 + i + j * bd];
-        v[j] = vexc[g0 + i + j * bd];
-      }
-#pragma unroll
-      for (int j = 0; j < 4; ++j) one_elem(i + j * bd, x[j], v[j]);
-    }
-    for (; i < n; i += bd) one_elem(i, xi[g0 + i], vexc[g0 + i]);
-    // the tile's sum: warps by shuffles, then warp 0 over the warps --
-    // double-float additions on the FP32 pipe (plain FP64 adds for the FP64
-    // form); the tile's share of ff = rho0 prefactor sum becomes a
-    // double-double partial
+  auto one_elem = [&](int i, T x, T v) {
     if constexpr (F64) {
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) acc64 += __shfl_down_sync(0xffffffffu, acc64, off);
-      if (lane == 0) wsd[buf][wid] = acc64;
+      ds[i] = (T)(2.0 * rho0) * x * v;
+      acc64 = fma((double)v * w[o], fma((double)x, (double)x, -1.0), acc64);
     } else {
-      DF a = acc_get(acc);
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1)
-        a = a + DF(__shfl_down_sync(0xffffffffu, a.hi, off), __shfl_down_sync(0xffffffffu, a.lo, off));
-      if (lane == 0) wsf[buf][wid] = make_float2(a.hi, a.lo);
+      ds[i] = df_value(x, v, two_rho0);
+      const DF xd = as_pair(x);
+      const float2 w2 = ws[o];
+      acc_mac(acc, as_pair(v) * DF(w2.x, w2.y), xd * xd - one);
     }
-    __syncthreads();
-    if (wid == 0) {
-      if constexpr (F64) {
-        double t = lane < nw ? wsd[buf][lane] : 0.0;
+    o += ostep;
+    if (o >= no) o -= no;
+  };
+  int i = tid;
+  for (; i + 3 * bd < n; i += 4 * bd) {  // four elements' loads in flight
+    T x[4], v[4];
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) t += __shfl_down_sync(0xffffffffu, t, off);
-        if (lane == 0) partials[tile] = make_double2(t * sc, 0.0);
-      } else {
-        const float2 q = lane < nw ? wsf[buf][lane] : make_float2(0.f, 0.f);
-        DF t(q.x, q.y);
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1)
-          t = t + DF(__shfl_down_sync(0xffffffffu, t.hi, off), __shfl_down_sync(0xffffffffu, t.lo, off));
-        if (lane == 0) {
-          const DD u = two_sum((double)t.hi * sc, (double)t.lo * sc);
-          partials[tile] = make_double2(u.hi, u.lo);
-        }
-      }
+    for (int j = 0; j < 4; ++j) {
+      x[j] = xs[i + j * bd];
+      v[j] = vs[i + j * bd];
     }
-    buf ^= 1;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) one_elem(i + j * bd, x[j], v[j]);
   }
-  if (tid == 0) {
-    __threadfence();
-    const unsigned done = atomicAdd(counter, 1u);
-    last = (done == gridDim.x - 1);
+  for (; i < n; i += bd) one_elem(i, xs[i], vs[i]);
+
+  // the CTA's sum: warps by shuffles, then warp 0 over the warps; the
+  // partial is the unscaled sum (double-float pair, or a double)
+  if constexpr (F64) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) acc64 += __shfl_down_sync(0xffffffffu, acc64, off);
+    if (lane == 0) wsd[wid] = acc64;
+  } else {
+    DF a = acc_get(acc);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+      a = a + DF(__shfl_down_sync(0xffffffffu, a.hi, off), __shfl_down_sync(0xffffffffu, a.lo, off));
+    if (lane == 0) wsf[wid] = make_float2(a.hi, a.lo);
   }
   __syncthreads();
-  if (!last || tid >= 32) return;
-  __threadfence();
-  DD acc2{0.0, 0.0};
-  for (size_t b = tid; b < ntiles; b += 32) {
-    const double2 q = __ldcg(&partials[b]);
-    acc2 = dd_add(acc2, DD{q.x, q.y});
+  if (wid == 0) {
+    if constexpr (F64) {
+      double t = lane < nw ? wsd[lane] : 0.0;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) t += __shfl_down_sync(0xffffffffu, t, off);
+      if (lane == 0) pd[blockIdx.x] = t;
+    } else {
+      const float2 q = lane < nw ? wsf[lane] : make_float2(0.f, 0.f);
+      DF t(q.x, q.y);
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1)
+        t = t + DF(__shfl_down_sync(0xffffffffu, t.hi, off), __shfl_down_sync(0xffffffffu, t.lo, off));
+      if (lane == 0) pf[blockIdx.x] = make_float2(t.hi, t.lo);
+    }
+    if (tid == 0) {
+      __threadfence();
+      last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+    }
   }
-  acc2 = warp_dd_sum(acc2);
-  if (tid == 0) {
-    *ff = acc2.hi + acc2.lo;
-    *counter = 0u;  // leave the counter ready for the next call
+  __syncthreads();  // also ends warp 0's reads of wsf / wsd
+  if (!last) return;
+  __threadfence();
+  // the last CTA: thread t adds partials t, t + bd, ...; then the warps by
+  // shuffles and warp 0 over the warps, as above
+  if constexpr (F64) {
+    double t = 0.0;
+    for (unsigned b = tid; b < gridDim.x; b += bd) t += __ldcg(&pd[b]);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) t += __shfl_down_sync(0xffffffffu, t, off);
+    if (lane == 0) wsd[wid] = t;
+    __syncthreads();
+    if (wid == 0) {
+      t = lane < nw ? wsd[lane] : 0.0;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) t += __shfl_down_sync(0xffffffffu, t, off);
+      if (lane == 0) {
+        *ff = t * sc;
+        *counter = 0u;  // leave the counter ready for the next call
+      }
+    }
+  } else {
+    DF t(0.f, 0.f);
+    for (unsigned b = tid; b < gridDim.x; b += bd) {
+      const float2 q = __ldcg(&pf[b]);
+      t = t + DF(q.x, q.y);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+      t = t + DF(__shfl_down_sync(0xffffffffu, t.hi, off), __shfl_down_sync(0xffffffffu, t.lo, off));
+    if (lane == 0) wsf[wid] = make_float2(t.hi, t.lo);
+    __syncthreads();
+    if (wid == 0) {
+      const float2 q = lane < nw ? wsf[lane] : make_float2(0.f, 0.f);
+      t = DF(q.x, q.y);
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1)
+        t = t + DF(__shfl_down_sync(0xffffffffu, t.hi, off), __shfl_down_sync(0xffffffffu, t.lo, off));
+      if (lane == 0) {
+        *ff = fma(sc, f2d_bits(t.hi), sc * f2d_bits(t.lo));
+        *counter = 0u;  // leave the counter ready for the next call
+      }
+    }
   }
 }
 
@@ -201,6 +229,23 @@ void launch_delta_rho(const T* xi, T* dr, size_t n, double rho0, cudaStream_t s)
   launch_check("delta_rho kernel launch");
 }
 
+// One wave: as many CTAs as the device holds at once (SMs x resident CTAs of
+// this kernel), each with an equal run of grid points, and no more CTAs than
+// the scratch has partial slots (one per kEnergyPoints points).  The grid
+// depends only on the device and the problem, so ff does too.
+template <typename T, bool F64>
+unsigned delta_f_grid(size_t nxyz, size_t nb, size_t smem, size_t* chunk) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
+  cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, delta_f_kernel<T, F64>, kEnergyThreads, smem),
+             "cudaOccupancyMaxActiveBlocksPerMultiprocessor(delta_f)");
+  const size_t wave = (size_t)std::max(1, sms) * (size_t)std::max(1, per_sm);
+  const size_t want = std::min(nb, wave);
+  *chunk = (nxyz + want - 1) / want;
+  return (unsigned)((nxyz + *chunk - 1) / *chunk);  // CTAs with a non-empty run
+}
+
 template <typename T>
 void launch_delta_f(const T* xi, const T* vexc, const double* w, T* df, double* ff, size_t nxyz,
                     int no, double rho0, double prefactor, void* work, cudaStream_t s, bool fp64) {
@@ -208,21 +253,24 @@ void launch_delta_f(const T* xi, const T* vexc, const double* w, T* df, double* 
   throw_if(nb > 0x7fffffffULL, "grid too large", 4);
   const size_t smem = sizeof(float2) * (size_t)no;
   throw_if(smem > 48 * 1024, "too many orientations for the energy kernel", 4);
-  double2* partials = static_cast<double2*>(work);
-  unsigned* counter = reinterpret_cast<unsigned*>(partials + nb);
+  unsigned* counter = reinterpret_cast<unsigned*>(static_cast<double2*>(work) + nb);
   if (nb == 0) {
     cuda_check(cudaMemsetAsync(ff, 0, sizeof(double), s), "cudaMemsetAsync(ff)");
     return;
   }
+  const bool f64 = fp64 && sizeof(T) == 8;
+  size_t chunk = 0;
+  const unsigned grid = f64 ? delta_f_grid<T, true>(nxyz, nb, smem, &chunk)
+                            : delta_f_grid<T, false>(nxyz, nb, smem, &chunk);
+  // a CTA's run indexes its elements with int
+  throw_if(chunk * (size_t)no > (size_t)0x7fffffff - 4 * kEnergyThreads, "grid too large", 4);
   clear_stale_error();
-  // at most 8 CTAs per SM, each looping over tiles (one partial per tile)
-  const unsigned grid = (unsigned)std::min<size_t>(nb, 152 * 8);
-  if (fp64 && sizeof(T) == 8)
-    delta_f_kernel<T, true><<<grid, kEnergyThreads, smem, s>>>(xi, vexc, w, df, ff, nxyz, no, rho0, prefactor,
-                                                               partials, counter);
+  if (f64)
+    delta_f_kernel<T, true><<<grid, kEnergyThreads, smem, s>>>(xi, vexc, w, df, ff, nxyz, no, chunk, rho0,
+                                                               prefactor, work, counter);
   else
-    delta_f_kernel<T, false><<<grid, kEnergyThreads, smem, s>>>(xi, vexc, w, df, ff, nxyz, no, rho0, prefactor,
-                                                                partials, counter);
+    delta_f_kernel<T, false><<<grid, kEnergyThreads, smem, s>>>(xi, vexc, w, df, ff, nxyz, no, chunk, rho0,
+                                                                prefactor, work, counter);
   launch_check("delta_f kernel launch");
 }
 

@@ -164,6 +164,86 @@ __device__ void grid_reduce(Red<K> r, double* __restrict__ part, unsigned* __res
   }
 }
 
+// Sums of per-thread double-float values combined on the FP32 pipes: warps
+// by shuffles, warp 0 over the CTA's warps, one partial (K pairs) per CTA,
+// and in the last CTA to finish every thread over the partials, then the
+// warps again, in a fixed order.  The L-BFGS dot products are double-float
+// Dot2 sums per thread, so double-float combining keeps their precision;
+// combining them as double-doubles (grid_reduce) spends tens of
+// microseconds per launch on the narrow FP64 pipe.  part: >= K float pairs
+// per CTA (the (gridDim.x, 2K + 1) doubles of grid_reduce hold them);
+// counter: zero on entry, left zero.  fin gets the K sums as doubles.
+template <int K>
+__device__ __forceinline__ void df_warp_sum(DF (&v)[K]) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+      v[k] = v[k] + DF(__shfl_down_sync(0xffffffffu, v[k].hi, off), __shfl_down_sync(0xffffffffu, v[k].lo, off));
+}
+template <int K, typename Fin>
+__device__ void grid_reduce_df(DF (&v)[K], double* __restrict__ part, unsigned* __restrict__ counter, Fin fin) {
+  __shared__ float2 sh[K][kRedThreads / 32];
+  __shared__ bool last;
+  float2* pf = reinterpret_cast<float2*>(part);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x / 32;
+  df_warp_sum<K>(v);
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) sh[k][wid] = make_float2(v[k].hi, v[k].lo);
+  }
+  __syncthreads();
+  if (wid == 0) {
+    DF t[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const float2 q = lane < nw ? sh[k][lane] : make_float2(0.f, 0.f);
+      t[k] = DF(q.x, q.y);
+    }
+    df_warp_sum<K>(t);
+    if (lane == 0) {
+#pragma unroll
+      for (int k = 0; k < K; ++k) pf[(size_t)blockIdx.x * K + k] = make_float2(t[k].hi, t[k].lo);
+      __threadfence();
+      last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+  }
+  __syncthreads();  // also ends warp 0's reads of sh
+  if (!last) return;
+  __threadfence();
+  DF t[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) t[k] = DF(0.f, 0.f);
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const float2 q = __ldcg(&pf[(size_t)b * K + k]);
+      t[k] = t[k] + DF(q.x, q.y);
+    }
+  }
+  df_warp_sum<K>(t);
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) sh[k][wid] = make_float2(t[k].hi, t[k].lo);
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const float2 q = lane < nw ? sh[k][lane] : make_float2(0.f, 0.f);
+      t[k] = DF(q.x, q.y);
+    }
+    df_warp_sum<K>(t);
+    if (lane == 0) {
+      double r[K];
+#pragma unroll
+      for (int k = 0; k < K; ++k) r[k] = df_to_double(t[k]);
+      fin(r);
+      *counter = 0u;
+    }
+  }
+}
+
 // grid of a streaming reduction: at most `cap` CTAs (8 per SM for the
 // memory-bound passes, so that enough loads are in flight; 4 for the energy
 // kernel, whose registers allow 4)
@@ -443,8 +523,9 @@ __global__ void __launch_bounds__(kRedThreads) eg_kernel(const EgArgs A) {
 // two-loop recursion only forms a preconditioned direction, whose rounding
 // the line search absorbs, while the iterate and the gradient stay FP64.
 // Every dot product is a double-float Dot2 sum on the FP32 pipe (products
-// exact by FMA, compensated additions), so no pass touches the narrow FP64
-// pipe; the threads' sums are combined as double-double values.
+// exact by FMA, compensated additions), and the threads' sums are combined
+// in double-float too (grid_reduce_df), so no pass leans on the narrow FP64
+// pipe.
 __device__ __forceinline__ DF as_df(float a) { return DF(a, 0.f); }
 __device__ __forceinline__ DF as_df(double a) { return df_from_double_bits(a); }
 __device__ __forceinline__ float as_f(float a) { return a; }
@@ -509,14 +590,13 @@ __global__ void __launch_bounds__(kRedThreads) lbfgs_pass_kernel(const PassArgs<
     if (dot) acc_mac(acc, as_df(A.v[i]), as_df(xv));
   }
   if (!dot) return;
-  Red<1> r = red_zero<1>();
-  r.s[0] = Dd{df_to_double(acc_get(acc)), 0.0};
+  DF r[1] = {acc_get(acc)};
   double* S = A.S;
   const int out = A.out, js1 = A.js1, js2 = A.js2;
   const double sc0 = A.sc0;
-  grid_reduce<1>(r, A.part, A.counter, [S, out, js1, js2, sc0](const Red<1>& t) {
+  grid_reduce_df<1>(r, A.part, A.counter, [S, out, js1, js2, sc0](const double* t) {
     const double scale = (js1 >= 0 ? S[js1] : sc0) * (js2 >= 0 ? S[js2] : 1.0);
-    S[out] = scale * (t.s[0].hi + t.s[0].lo);
+    S[out] = scale * t[0];
   });
 }
 
@@ -563,11 +643,9 @@ pair_kernel(float* __restrict__ s, float* __restrict__ y, const float* __restric
     for (int j = 0; j < 4; ++j) one(i + j * stride, dv[j], gnv[j], gv[j]);
   }
   for (; i < n; i += stride) one(i, d[i], gn[i], g[i]);
-  Red<2> r = red_zero<2>();
-  r.s[0] = Dd{df_to_double(acc_get(sy)), 0.0};
-  r.s[1] = Dd{df_to_double(acc_get(yy)), 0.0};
-  grid_reduce<2>(r, part, counter, [S, o, orho, ogam](const Red<2>& t2) {
-    const double sy = t2.s[0].hi + t2.s[0].lo, yy = t2.s[1].hi + t2.s[1].lo;
+  DF r[2] = {acc_get(sy), acc_get(yy)};
+  grid_reduce_df<2>(r, part, counter, [S, o, orho, ogam](const double* t2) {
+    const double sy = t2[0], yy = t2[1];
     S[o] = sy;
     S[o + 1] = yy;
     const bool ok = yy > 0.0 && sy > 1e-12 * yy;
