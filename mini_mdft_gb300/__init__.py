@@ -23,4 +23,5 @@ from .api import (  # noqa: F401
     wait_timeouts,
 )
 from ._lib import LIB_PATH, lib  # noqa: F401
+from .solvent import Solvents, check_mole_fractions, mole_fractions  # noqa: F401
 
