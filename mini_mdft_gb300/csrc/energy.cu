@@ -294,7 +294,8 @@ template void launch_delta_f<float>(const float*, const float*, const double*, f
 // its per-CTA partial sums kept in one fixed array in the library's own
 // device memory instead of a stream-ordered temporary.
 //
-// The array holds kNoAllocMaxPartials partials (one per 32 grid points), so
+// The array holds kNoAllocMaxPartials partial slots (one per 32 grid points,
+// the scratch sizing of every get_delta_f call; a call fills one per CTA), so
 // grids of up to 2,097,152 points (128^3) are accepted and larger ones are
 // rejected with an error; it costs 1 MiB of device memory on every GPU that
 // loads the library, held until the process exits.  All calls share it and
