@@ -29,29 +29,6 @@ __global__ void delta_rho_kernel(const T* __restrict__ xi, T* __restrict__ dr, s
   }
 }
 
-struct DD {
-  double hi, lo;
-};
-__device__ __forceinline__ DD two_sum(double a, double b) {
-  const double s = a + b;
-  const double bb = s - a;
-  const double e = (a - (s - bb)) + (b - bb);
-  return DD{s, e};
-}
-__device__ __forceinline__ DD dd_add(DD a, DD b) {
-  DD s = two_sum(a.hi, b.hi);
-  const double e = s.lo + (a.lo + b.lo);
-  const double hi = s.hi + e;
-  return DD{hi, e - (hi - s.hi)};
-}
-__device__ __forceinline__ DD dd_shfl_down(DD v, int off) {
-  return DD{__shfl_down_sync(0xffffffffu, v.hi, off), __shfl_down_sync(0xffffffffu, v.lo, off)};
-}
-__device__ __forceinline__ DD warp_dd_sum(DD v) {
-  for (int off = 16; off > 0; off >>= 1) v = dd_add(v, dd_shfl_down(v, off));
-  return v;
-}
-
 // df = 2 rho0 xi vexc in the field type: double-float arithmetic and one FP64
 // add to store (FP64 fields), plain float (FP32 fields, as the reference's
 // float instantiation computes it)
