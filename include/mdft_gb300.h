@@ -184,9 +184,10 @@ int mdft_get_delta_rho(const void* xi, void* delta_rho, size_t n, double rho0,
  * ff = sum_r rho0 prefactor sum_o vexc w (xi^2 - 1) over xi, vexc, delta_f
  * of shape (nxyz, no) and w (no) (all device pointers, w always double).
  * ff_dev is a device double; it is overwritten (the reference sets ff = 0
- * first).  The sum over points is deterministic (fixed reduction tree with
- * compensated partial sums).  Uses a stream-ordered temporary of
- * 16 bytes per 128 points. */
+ * first).  The sum over points is deterministic on a given GPU (a fixed
+ * reduction tree with compensated partial sums; its shape follows the
+ * device's SM count and the kernel's occupancy).  Uses a stream-ordered
+ * temporary of 16 bytes per 32 points, plus 16. */
 int mdft_get_delta_f(const void* xi, const void* vexc, const double* w,
                      void* delta_f, double* ff_dev, size_t nxyz, int no,
                      double rho0, double prefactor, int precision,
