@@ -21,7 +21,8 @@ reference's Kokkos/kokkos-fft build is unavailable; see oracle/build.py) on
 all host cores.
 
 Multi-GPU (torchrun): the path does not shard; each rank runs an independent
-replica of the workload and ``value`` is the sum over ranks.
+replica of the workload, and ``value`` is the round trips of all ranks
+divided by the slowest rank's time (barrier, then a MAX all-reduce).
 """
 import argparse
 import json
@@ -65,27 +66,60 @@ def dist_env():
     return ws, rank, local
 
 
-def sizes():
+def sizes(wl=None):
     from mini_mdft_gb300 import inputs as I
-    nt, nphi, npsi, no, np_ = I.angular_counts(WORKLOAD["mmax"], WORKLOAD["mrso"])
-    n = WORKLOAD["n"]
+    wl = wl or WORKLOAD
+    nt, nphi, npsi, no, np_ = I.angular_counts(wl["mmax"], wl["mrso"])
+    n = wl["n"]
     N = n[0] * n[1] * n[2]
     return dict(N=N, ntheta=nt, nphi=nphi, npsi=npsi, no=no, np=np_,
-                np_new=I.np_new_count(WORKLOAD["mmax"], WORKLOAD["mrso"]))
+                np_new=I.np_new_count(wl["mmax"], wl["mrso"]))
 
 
 def algorithmic_bytes(s, real_bytes):
-    """Per-stage algorithmic bytes: each stage reads its input once and
-    writes its output once (c(q) table and maps excluded: L2-resident)."""
+    """Per-launch algorithmic bytes: each kernel reads its input once and
+    writes its output once (c(q) table, R(q) table and maps excluded)."""
     N, no, np_ = s["N"], s["no"], s["np"]
     cb = 2 * real_bytes
-    return {
+    fft = N * np_ * cb * 2           # one axis pass: read + write p
+    out = {
         "angl2proj": N * (real_bytes * no + cb * np_),
-        "fft_axis": N * np_ * cb * 2,         # one axis pass: read + write p
+        "fft_axis": fft,
         "oz": N * np_ * cb * 2,
         "proj2angl": N * (cb * np_ + real_bytes * no),
         "round_trip": N * (2 * real_bytes * no + 8 * cb * np_),
     }
+    for k in STAGES:
+        if k.startswith("fft_"):
+            out[k] = fft
+    return out
+
+
+# CUDA kernel run by each launch of the round trip (names as ncu lists them)
+KERNEL_OF_STAGE = {
+    "angl2proj": "angl2proj_fast_kernel", "proj2angl": "proj2angl_fast_kernel",
+    "fft_fwd_z": "fft_fixed_kernel", "fft_inv_z": "fft_fixed_kernel",
+    "fft_fwd_y": "fft_tma_kernel", "fft_fwd_x": "fft_tma_kernel",
+    "fft_inv_x": "fft_tma_kernel", "fft_inv_y": "fft_tma_kernel",
+    "oz": {"f64": "oz_lane1_kernel", "f64df": "oz_lane_kernel", "f32": "oz_lane_kernel"},
+}
+
+
+def kernel_name(stage, form):
+    k = KERNEL_OF_STAGE[stage]
+    return k[form] if isinstance(k, dict) else k
+
+
+def per_kernel_table(st, form, s, hbm_peak):
+    """One entry per launch of the round trip: algorithmic bytes, CUDA-event
+    time, achieved GB/s and fraction of the measured HBM bandwidth."""
+    ab = algorithmic_bytes(s, 4 if form == "f32" else 8)
+    rows = []
+    for k in STAGES:
+        t = st[k]
+        rows.append({"launch": k, "kernel": kernel_name(k, form), "algorithmic_bytes": ab[k],
+                     "ms": t * 1e3, "achieved_gbs": ab[k] / t / 1e9, "frac": ab[k] / t / 1e9 / hbm_peak})
+    return rows
 
 
 class ClockSampler:
@@ -148,15 +182,16 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(rows), "samples_under_load": len(loaded)}
 
 
-def make_problem(prec):
+def make_problem(prec, wl=None):
     """Handles and resident buffers of one form: "f64" (FP64 arithmetic),
-    "f64df" (FP64 fields, double-float arithmetic) or "f32" (mixed form)."""
-    import numpy as np
+    "f64df" (FP64 fields, double-float arithmetic) or "f32" (mixed form), on
+    the workload `wl` (default: the 64^3 / 30 A / mmax 3 headline)."""
     import torch
 
     import mini_mdft_gb300 as M
     from mini_mdft_gb300 import inputs as I
-    n, box, mmax, mrso, dq = (WORKLOAD[k] for k in ("n", "box", "mmax", "mrso", "dq"))
+    wl = wl or WORKLOAD
+    n, box, mmax, mrso, dq = (wl[k] for k in ("n", "box", "mmax", "mrso", "dq"))
     nq = I.nq_for(n, box, dq)
     idx, tab = I.synthetic_cq(mmax, mrso, nq, dq)
     sg, ag = M.SpatialGrid(n, box), M.AngularGrid(mmax, mrso)
@@ -169,7 +204,7 @@ def make_problem(prec):
     p = torch.zeros((ag.m_np,) + tuple(n), dtype=cd, device="cuda")
     vexc = torch.zeros_like(dr)
     return dict(opt=opt, conv=conv, dr=dr, p=p, vexc=vexc, dr_host=dr_host, ag=ag, rd=rd, cd=cd,
-                prec=prec)
+                prec=prec, wl=wl, idx=idx, tab=tab)
 
 
 def step(P):
@@ -193,26 +228,33 @@ def timed_steps(P, K, flush):
     return sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / 1e3
 
 
+STAGES = ["angl2proj", "fft_fwd_z", "fft_fwd_y", "fft_fwd_x", "oz", "fft_inv_x", "fft_inv_y", "fft_inv_z",
+          "proj2angl"]
+
+
 def stage_times(P, reps, flush):
-    """Average device time of each stage of the round trip as step() runs it
-    (CUDA events on the launching stream; the convolution's inner stages
-    through Convolution.execute_timed, so the double-float form is timed on
-    its packed kernels).  L2 is flushed before each round trip."""
+    """Average device time of each kernel of the round trip as step() runs it
+    (CUDA events on the launching stream; the convolution's passes through
+    Convolution.execute_timed_passes, so the double-float form is timed on
+    its packed kernels).  L2 is flushed before each round trip.  Adds the
+    sums fft_forward / fft_backward of the three axis passes."""
     import torch
-    names = ["angl2proj", "fft_forward", "oz", "fft_backward", "proj2angl"]
-    tot = dict.fromkeys(names, 0.0)
+    tot = dict.fromkeys(STAGES, 0.0)
     for _ in range(reps):
         flush.zero_()
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(10)]
         ev[0].record()
         P["opt"].angl2proj(P["dr"], P["p"])
-        P["conv"].execute_timed(P["p"], ev[1:5])
+        P["conv"].execute_timed_passes(P["p"], ev[1:9])
         P["opt"].proj2angl(P["p"], P["vexc"])
-        ev[5].record()
+        ev[9].record()
         torch.cuda.synchronize()
-        for i, n in enumerate(names):
+        for i, n in enumerate(STAGES):
             tot[n] += ev[i].elapsed_time(ev[i + 1]) / 1e3
-    return {n: t / reps for n, t in tot.items()}
+    out = {n: t / reps for n, t in tot.items()}
+    out["fft_forward"] = out["fft_fwd_z"] + out["fft_fwd_y"] + out["fft_fwd_x"]
+    out["fft_backward"] = out["fft_inv_x"] + out["fft_inv_y"] + out["fft_inv_z"]
+    return out
 
 
 def e2e_steps(P, K, warm):
@@ -286,59 +328,19 @@ def e2e_steps(P, K, warm):
     return piped, serial, nbytes, h_out[0].numel() * h_out[0].element_size()
 
 
-def fp64_peak_tflops():
-    """cuBLAS DGEMM throughput (4096^3), the FP64 roof of this GPU."""
-    import torch
-    n = 4096
-    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
-    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
-    for _ in range(2):
-        torch.matmul(a, b)
-    torch.cuda.synchronize()
-    best = 1e9
-    for _ in range(3):
-        s = torch.cuda.Event(enable_timing=True)
-        e = torch.cuda.Event(enable_timing=True)
-        s.record()
-        torch.matmul(a, b)
-        e.record()
-        torch.cuda.synchronize()
-        best = min(best, s.elapsed_time(e) / 1e3)
-    return 2.0 * n ** 3 / best / 1e12
+TRAFFIC_JSON = os.path.join(ROOT, "profiles", "dram_traffic_64cubed_mmax3.json")
 
 
-def stage_flops(s):
-    """Algorithmic FP64 flops per stage launch (counts of the arithmetic in
-    each kernel's inner loops; 5 n log2 n per complex FFT of length n)."""
-    import math
-    N, nt, nphi, npsi, np_ = s["N"], s["ntheta"], s["nphi"], s["npsi"], s["np"]
-    K1 = (npsi - 1) // 2 + 1
-    mmax = WORKLOAD["mmax"]
-    from mini_mdft_gb300 import inputs as I
-    ms = [m for m in range(mmax + 1) for _ in range(-m, m + 1) for _ in range(m // WORKLOAD["mrso"] + 1)]
-    srot = sum(2 * m + 1 for m in ms)
-    nrec = sum(2 * l * l + 2 * l + 1 for l in range(2, mmax + 1))
-    a2p = N * (nt * nphi * K1 * (npsi * 2) + nt * nphi * K1 * nphi * 8 + np_ * nt * 4)
-    npairs = N // 2 + 4
-    # R(q) comes from the per-plan table, so the recursion is not per-apply work
-    oz = npairs * (4 * srot * 8 + s["np_new"] * 22)
-    n = WORKLOAD["n"][0]
-    fft_axis = N * np_ // n * 5 * n * math.log2(n)
-    return {"angl2proj": a2p, "proj2angl": a2p, "oz": oz, "fft_axis": fft_axis}
-
-
-def read_traffic(kernel):
-    """dram read+write bytes per launch of `kernel` from the committed ncu
-    summary (profiles/dram_traffic_64cubed_mmax3.md), or None."""
-    import re
-    path = os.path.join(ROOT, "profiles", "dram_traffic_64cubed_mmax3.md")
-    if not os.path.exists(path):
-        return None
-    for line in open(path):
-        m = re.match(r"^\|\s*([a-z0-9_]+)\s*\|\s*(\d+)\s*\|", line)
-        if m and m.group(1) == kernel:
-            return int(m.group(2))
-    return None
+def profiled_traffic(form, launch):
+    """DRAM bytes (read + write) per launch of `launch` in `form`, from the
+    ncu capture recorded in profiles/dram_traffic_64cubed_mmax3.json (the
+    command that made it is in the file), or None.  Not measured in this run:
+    a bench run is never timed under a profiler."""
+    if not os.path.exists(TRAFFIC_JSON):
+        return None, None
+    d = json.load(open(TRAFFIC_JSON))
+    v = d.get("forms", {}).get(form, {}).get(launch)
+    return (int(v["bytes"]) if v else None), d.get("command")
 
 
 # c(q) amplitude of the minimiser workloads: the execute step is unnormalised
@@ -893,28 +895,17 @@ def run_ours(args):
         ff[f] = M.get_delta_f(x, P[f]["vexc"], w, torch.zeros_like(x), rho0, pref)
     ff_err = {f: abs(ff[f] - ff["f64"]) / abs(ff["f64"]) for f in ("f64df", "f32")}
 
-    ab = algorithmic_bytes(s, 8)
-    sh = st[head]
-    per_launch = {
-        "angl2proj": (sh["angl2proj"], ab["angl2proj"]),
-        "fft_axis": ((sh["fft_forward"] + sh["fft_backward"]) / 6.0, ab["fft_axis"]),
-        "oz": (sh["oz"], ab["oz"]),
-        "proj2angl": (sh["proj2angl"], ab["proj2angl"]),
-    }
-    share = {"angl2proj": sh["angl2proj"], "fft_axis": sh["fft_forward"] + sh["fft_backward"],
-             "oz": sh["oz"], "proj2angl": sh["proj2angl"]}
-    dom = max(share, key=share.get)
-    t_launch, b_launch = per_launch[dom]
     peaks = {}
     pk_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(pk_path):
         peaks = json.load(open(pk_path))
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    achieved = b_launch / t_launch / 1e9
-    traffic = read_traffic(dom)
-    fp64_peak = fp64_peak_tflops()
-    fl_launch = stage_flops(s)[dom]
+    ab = algorithmic_bytes(s, 8)
+    # the dominant single launch of the headline form's round trip
+    table = {f: per_kernel_table(st[f], f, s, hbm_peak) for f in forms}
+    dom = max(table[head], key=lambda r: r["ms"])
+    traffic, traffic_cmd = profiled_traffic(head, dom["launch"])
     kernels_per_step = 1 + 3 + 1 + 3 + 1
 
     def form_entry(f):
@@ -922,7 +913,8 @@ def run_ours(args):
         e = {"value": whole_job_value(ws, K, form_secs[f]), "unit": "applies/s", "arithmetic": FORM_NAMES[f],
              "ms_per_step": form_secs[f] / K * 1e3,
              "round_trip_hbm_frac": bytes_rt / (form_secs[f] / K) / 1e9 / hbm_peak,
-             "stages_ms": {k: v * 1e3 for k, v in st[f].items()}}
+             "stages_ms": {k: v * 1e3 for k, v in st[f].items()},
+             "kernels": table[f]}
         if f != "f64":
             e["vexc_rel_err_vs_f64"] = err[f]
             e["ff_rel_err_vs_f64"] = ff_err[f]
@@ -931,7 +923,7 @@ def run_ours(args):
     out = {
         "metric": METRIC, "value": value, "unit": "applies/s", "n_gpus": ws, "steps": K,
         "warmup": W, "ms_per_step": secs / K * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "scaling": "weak", "vs_baseline": None, "dtype": head, "data": "synthetic",
         "arithmetic": FORM_NAMES[head],
         "config": {
             "workload": "64^3 grid, box 30 A, mmax 3, mrso 2 (ntheta 4, nphi 7, npsi 3, np 28): "
@@ -951,14 +943,15 @@ def run_ours(args):
         "gpu_launches": kernels_per_step * K,
         "clocks": clk,
         "roofline": {
-            "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
-            "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
+            "bound": "hbm", "kernel": dom["kernel"], "launch": dom["launch"], "form": head,
+            "achieved": dom["achieved_gbs"], "peak": hbm_peak, "unit": "GB/s",
+            "frac": dom["achieved_gbs"] / hbm_peak, "traffic": traffic,
+            "traffic_source": ("ncu capture (not this run): profiles/dram_traffic_64cubed_mmax3.json, "
+                               "command: %s" % traffic_cmd) if traffic is not None else None,
             "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)",
-            "algorithmic_bytes_per_launch": b_launch, "launch_ms": t_launch * 1e3,
-            "fp64_equivalent": {"achieved_tflops": fl_launch / t_launch / 1e12,
-                                "fp64_peak_tflops": fp64_peak,
-                                "frac_of_fp64_peak": fl_launch / t_launch / 1e12 / fp64_peak,
-                                "peak_source": "measured cuBLAS DGEMM 4096^3 in this run"},
+            "algorithmic_bytes_per_launch": dom["algorithmic_bytes"], "launch_ms": dom["ms"],
+            "timing": "CUDA events around the launch on its stream, mean of 10 L2-flushed round trips",
+            "kernels": table[head],
         },
         "round_trip_hbm_frac": ab["round_trip"] / (secs / K) / 1e9 / hbm_peak,
         "forms": {f: form_entry(f) for f in forms},

@@ -51,7 +51,10 @@ typedef enum {
   MDFT_ERR_CUDA = 2,        /* a CUDA runtime call failed */
   MDFT_ERR_IO = 3,          /* c(q) file missing or malformed */
   MDFT_ERR_UNSUPPORTED = 4, /* size outside what the kernels handle */
-  MDFT_ERR_NOMEM = 5        /* device allocation failed */
+  MDFT_ERR_NOMEM = 5,       /* device allocation failed */
+  MDFT_ERR_TIMEOUT = 6      /* a bounded device wait of an earlier launch on
+                               this device ran out: that launch's results are
+                               wrong (see mdft_wait_timeouts) */
 } mdft_status;
 
 /* MDFT_F64: double fields, FP64 arithmetic (the reference's
@@ -148,6 +151,10 @@ int mdft_conv_execute(mdft_conv_t h, void* p, void* stream);
  * double-float form keeps the projections packed between its stages, which
  * the separate mdft_conv_fft / mdft_conv_kspace calls below do not). */
 int mdft_conv_execute_timed(mdft_conv_t h, void* p, void* stream, void* const* events);
+/* Same, timed per kernel: events[0..7] are recorded before the forward FFT,
+ * after each of its three axis passes (z, y, x), after the k-space step and
+ * after each inverse pass (x, y, z).  No counterpart in the reference. */
+int mdft_conv_execute_timed_passes(mdft_conv_t h, void* p, void* stream, void* const* events);
 /* The two 3-D FFT passes of execute on their own (sign -1 forward,
  * +1 backward; unnormalised), and the k-space step alone. */
 int mdft_conv_fft(mdft_conv_t h, void* p, int sign, void* stream);
@@ -203,18 +210,30 @@ int mdft_get_delta_f(const void* xi, const void* vexc, const double* w,
  * it calls no allocation routine.  Limit: nxyz <= 2,097,152 grid points
  * (128^3); larger grids return MDFT_ERR_UNSUPPORTED.  All calls share the
  * array, so calls that overlap on the GPU race and must be serialised by the
- * caller.  The first call on a device looks up the array's address for that
- * device; make it before any stream capture. */
+ * caller.  A call on a stream that is not capturing looks the array's
+ * address up on the current device (so a context reset by cudaDeviceReset is
+ * picked up); a call on a capturing stream reuses the address of the last
+ * such lookup on that device, so the first call on a device must come before
+ * any stream capture. */
 int mdft_get_delta_f_noalloc(const void* xi, const void* vexc, const double* w,
                              void* delta_f, double* ff_dev, size_t nxyz, int no,
                              double rho0, double prefactor, int precision,
                              void* stream);
 
-/* Diagnostics: number of waits on asynchronous copies (the tensor-memory-
- * access tiles of the FFT) that ran out of time on the current device since
- * the library was loaded; such a kernel leaves its tile untouched, so a
- * non-zero count means wrong results.  No counterpart in the reference. */
+/* Diagnostics: number of bounded device waits (on the asynchronous copies of
+ * the FFT's tensor-memory-access tiles, or on the flags of the server's
+ * persistent kernels) that ran out of time on the current device since the
+ * library was loaded; such a kernel leaves its output wrong.  Each new
+ * timeout also makes the next call that launches that kind of work on the
+ * device return MDFT_ERR_TIMEOUT, so callers need not poll this.  No
+ * counterpart in the reference. */
 int mdft_wait_timeouts(int* count);
+/* Diagnostics: exercises the error path of those waits without a fault or a
+ * hang -- one CTA waits on a barrier that nothing completes, gives up after
+ * `spins` polls (1 <= spins <= 2^20) and records the timeout as a real one;
+ * the next FFT launch on the device then returns MDFT_ERR_TIMEOUT.  No
+ * counterpart in the reference. */
+int mdft_wait_selftest(int spins, void* stream);
 
 /* ---- job server -----------------------------------------------------------
  * No counterpart in the reference (which evaluates one field per call).  A

@@ -21,6 +21,7 @@ from .api import (  # noqa: F401
     luc_write,
     solute_vext,
     wait_timeouts,
+    wait_selftest,
 )
 from ._lib import LIB_PATH, lib  # noqa: F401
 from .solvent import Solvents, check_mole_fractions, mole_fractions  # noqa: F401

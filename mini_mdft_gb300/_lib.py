@@ -12,6 +12,7 @@ LIB_PATH = os.path.join(_PKG, "lib", "libmdft_gb300.so")
 HEADER_PATH = os.path.join(os.path.dirname(_PKG), "include", "mdft_gb300.h")
 
 MDFT_OK = 0
+MDFT_ERR_TIMEOUT = 6
 MDFT_F64 = 0
 MDFT_F32 = 1
 MDFT_F64_DF = 2
@@ -46,6 +47,7 @@ SIGNATURES = {
     "mdft_conv_destroy": (i32, [vp]),
     "mdft_conv_execute": (i32, [vp, vp, vp]),
     "mdft_conv_execute_timed": (i32, [vp, vp, vp, C.POINTER(vp)]),
+    "mdft_conv_execute_timed_passes": (i32, [vp, vp, vp, C.POINTER(vp)]),
     "mdft_conv_fft": (i32, [vp, vp, i32, vp]),
     "mdft_conv_kspace": (i32, [vp, vp, vp]),
     "mdft_conv_info": (i32, [vp, ip, dp]),
@@ -57,6 +59,7 @@ SIGNATURES = {
     "mdft_get_delta_f": (i32, [vp, vp, vp, vp, vp, sz, i32, f64, f64, i32, vp]),
     "mdft_get_delta_f_noalloc": (i32, [vp, vp, vp, vp, vp, sz, i32, f64, f64, i32, vp]),
     "mdft_wait_timeouts": (i32, [ip]),
+    "mdft_wait_selftest": (i32, [i32, vp]),
     "mdft_server_create": (i32, [C.POINTER(vp), i32, i32, sz]),
     "mdft_server_destroy": (i32, [vp]),
     "mdft_server_add_solvent": (i32, [vp, i32, i32, ip, dp, i32, i32, f64, f64, f64, ip]),

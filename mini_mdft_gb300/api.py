@@ -296,6 +296,21 @@ class Convolution:
         arr = (C.c_void_p * 4)(*[C.c_void_p(e.cuda_event) for e in events])
         check(lib().mdft_conv_execute_timed(self.h, _dptr(deltarho_p), _stream(), arr))
 
+    def execute_timed_passes(self, deltarho_p, events):
+        """execute() timed per kernel: ``events`` are eight
+        torch.cuda.Event(enable_timing=True), recorded on the current stream
+        before the forward FFT, after each of its axis passes (z, y, x), after
+        the k-space step and after each inverse pass (x, y, z)
+        (mdft_conv_execute_timed_passes).  No counterpart in the reference."""
+        _check_field(deltarho_p, self.N * self.batch * self.np, self._cdt(), "deltarho_p")
+        if len(events) != 8:
+            raise ValueError("execute_timed_passes needs eight events")
+        for e in events:
+            if not e.cuda_event:
+                e.record()
+        arr = (C.c_void_p * 8)(*[C.c_void_p(e.cuda_event) for e in events])
+        check(lib().mdft_conv_execute_timed_passes(self.h, _dptr(deltarho_p), _stream(), arr))
+
     def fft(self, p, sign):
         _check_field(p, self.N * self.batch * self.np, self._cdt(), "p")
         check(lib().mdft_conv_fft(self.h, _dptr(p), int(sign), _stream()))
@@ -571,9 +586,16 @@ def luc_write(path, luc_index, table, dq, header="c(q) table"):
 
 
 def wait_timeouts():
-    """Waits on asynchronous FFT tile copies that ran out of time on the
-    current device since the library was loaded (mdft_wait_timeouts); must
-    stay 0."""
+    """Bounded device waits (FFT tile copies, persistent-kernel flags) that
+    ran out of time on the current device since the library was loaded
+    (mdft_wait_timeouts); stays 0 unless wait_selftest ran."""
     c = C.c_int()
     check(lib().mdft_wait_timeouts(C.byref(c)))
     return c.value
+
+
+def wait_selftest(spins=1024, stream=None):
+    """Launches one CTA whose bounded wait runs out (nothing completes its
+    barrier) and is recorded as a timeout (mdft_wait_selftest): the next FFT
+    launch on the device then raises MdftError with code MDFT_ERR_TIMEOUT."""
+    check(lib().mdft_wait_selftest(int(spins), _stream() if stream is None else C.c_void_p(stream)))

@@ -374,9 +374,12 @@ ConvLaunch conv_launch(const mdft_conv_s* h, int k) {
   return L;
 }
 
+// One 3-D transform as three axis passes (z, y, x forward; x, y, z
+// inverse).  after (optional): three events, each recorded once its pass has
+// been enqueued (a length-1 axis records at once).
 template <typename S, typename T>
 void conv_fft(ConvLaunch& L, void* p, int sign, cudaStream_t s, bool in_packed = false,
-              bool out_packed = false) {
+              bool out_packed = false, cudaEvent_t const* after = nullptr) {
   mdft::FftAxis* order[3];
   if (sign < 0) {
     order[0] = &L.az;
@@ -387,26 +390,37 @@ void conv_fft(ConvLaunch& L, void* p, int sign, cudaStream_t s, bool in_packed =
     order[1] = &L.ay;
     order[2] = &L.az;
   }
+  auto mark = [&](int i) {
+    if (after) mdft::cuda_check(cudaEventRecord(after[i], s), "pass event record");
+  };
   if constexpr (std::is_same<T, mdft::DF>::value) {
-    mdft::FftAxis* live[3];
     int nl = 0;
     for (auto* a : order)
-      if (a->n > 1) live[nl++] = a;
+      if (a->n > 1) ++nl;
     throw_if(nl == 0 && in_packed != out_packed, "internal: no FFT pass to change the format", 4);
-    for (int i = 0; i < nl; ++i) {
-      const bool src = i == 0 ? in_packed : true;
-      const bool dst = i == nl - 1 ? out_packed : true;
-      if (!src && !dst)
-        mdft::launch_fft_axis<double, double, T>(*live[i], p, sign, s);
-      else if (!src && dst)
-        mdft::launch_fft_axis<double, mdft::DF, T>(*live[i], p, sign, s);
-      else if (src && dst)
-        mdft::launch_fft_axis<mdft::DF, mdft::DF, T>(*live[i], p, sign, s);
-      else
-        mdft::launch_fft_axis<mdft::DF, double, T>(*live[i], p, sign, s);
+    int li = 0;
+    for (int k = 0; k < 3; ++k) {
+      mdft::FftAxis* a = order[k];
+      if (a->n > 1) {
+        const bool src = li == 0 ? in_packed : true;
+        const bool dst = li == nl - 1 ? out_packed : true;
+        if (!src && !dst)
+          mdft::launch_fft_axis<double, double, T>(*a, p, sign, s);
+        else if (!src && dst)
+          mdft::launch_fft_axis<double, mdft::DF, T>(*a, p, sign, s);
+        else if (src && dst)
+          mdft::launch_fft_axis<mdft::DF, mdft::DF, T>(*a, p, sign, s);
+        else
+          mdft::launch_fft_axis<mdft::DF, double, T>(*a, p, sign, s);
+        ++li;
+      }
+      mark(k);
     }
   } else {
-    for (auto* a : order) mdft::launch_fft_axis<S, S, T>(*a, p, sign, s);
+    for (int k = 0; k < 3; ++k) {
+      mdft::launch_fft_axis<S, S, T>(*order[k], p, sign, s);
+      mark(k);
+    }
   }
 }
 
@@ -623,6 +637,7 @@ int mdft_conv_fft(mdft_conv_t h, void* p, int sign, void* stream) {
     throw_if(!h || !p, "NULL argument");
     throw_if(sign != -1 && sign != 1, "sign must be -1 or +1");
     check_device(h->device);
+    mdft::check_device_waits();
     with_types(h->prec, [&](auto st, auto ct) {
       ConvLaunch L = conv_launch(h, h->batch);
       conv_fft<decltype(st), decltype(ct)>(L, p, sign, as_stream(stream));
@@ -634,6 +649,7 @@ int mdft_conv_kspace(mdft_conv_t h, void* p, void* stream) {
   return guarded([&] {
     throw_if(!h || !p, "NULL argument");
     check_device(h->device);
+    mdft::check_device_waits();
     with_types(h->prec, [&](auto st, auto ct) {
       using S = decltype(st);
       mdft::launch_oz<S, decltype(ct)>(h->oz, static_cast<Cx<S>*>(p), as_stream(stream));
@@ -643,11 +659,19 @@ int mdft_conv_kspace(mdft_conv_t h, void* p, void* stream) {
 
 namespace {
 // execute(): forward FFT, k-space step, inverse FFT.  ev (optional) receives
-// an event record before the forward FFT and after each of the three stages.
-void conv_execute(mdft_conv_s* h, void* p, cudaStream_t s, cudaEvent_t const* ev, int k = 0) {
+// an event record before the forward FFT and after each of the three stages;
+// pev (optional) eight records: before the forward FFT, after each of its
+// three axis passes, after the k-space step and after each inverse pass.
+void conv_execute(mdft_conv_s* h, void* p, cudaStream_t s, cudaEvent_t const* ev, int k = 0,
+                  cudaEvent_t const* pev = nullptr) {
   auto mark = [&](int i) {
     if (ev) mdft::cuda_check(cudaEventRecord(ev[i], s), "stage event record");
   };
+  auto pmark = [&](int i) {
+    if (pev) mdft::cuda_check(cudaEventRecord(pev[i], s), "pass event record");
+  };
+  const cudaEvent_t* fwd = pev ? pev + 1 : nullptr;
+  const cudaEvent_t* inv = pev ? pev + 5 : nullptr;
   ConvLaunch L = conv_launch(h, k > 0 ? k : h->batch);
   with_types(h->prec, [&](auto st, auto ct) {
     using S = decltype(st);
@@ -655,21 +679,25 @@ void conv_execute(mdft_conv_s* h, void* p, cudaStream_t s, cudaEvent_t const* ev
     if constexpr (std::is_same<C, mdft::DF>::value) {
       if (h->df_packed) {
         mark(0);
-        conv_fft<S, C>(L, p, -1, s, false, true);
+        pmark(0);
+        conv_fft<S, C>(L, p, -1, s, false, true, fwd);
         mark(1);
         mdft::launch_oz<mdft::DF, C>(L.oz, static_cast<Cx<mdft::DF>*>(p), s);
         mark(2);
-        conv_fft<S, C>(L, p, +1, s, true, false);
+        pmark(4);
+        conv_fft<S, C>(L, p, +1, s, true, false, inv);
         mark(3);
         return;
       }
     }
     mark(0);
-    conv_fft<S, C>(L, p, -1, s);
+    pmark(0);
+    conv_fft<S, C>(L, p, -1, s, false, false, fwd);
     mark(1);
     mdft::launch_oz<S, C>(L.oz, static_cast<Cx<S>*>(p), s);
     mark(2);
-    conv_fft<S, C>(L, p, +1, s);
+    pmark(4);
+    conv_fft<S, C>(L, p, +1, s, false, false, inv);
     mark(3);
   });
 }
@@ -679,6 +707,7 @@ int mdft_conv_execute(mdft_conv_t h, void* p, void* stream) {
   return guarded([&] {
     throw_if(!h || !p, "NULL argument");
     check_device(h->device);
+    mdft::check_device_waits();
     conv_execute(h, p, as_stream(stream), nullptr);
   });
 }
@@ -688,7 +717,18 @@ int mdft_conv_execute_timed(mdft_conv_t h, void* p, void* stream, void* const* e
     throw_if(!h || !p || !events, "NULL argument");
     for (int i = 0; i < 4; ++i) throw_if(!events[i], "NULL event");
     check_device(h->device);
+    mdft::check_device_waits();
     conv_execute(h, p, as_stream(stream), reinterpret_cast<cudaEvent_t const*>(events));
+  });
+}
+
+int mdft_conv_execute_timed_passes(mdft_conv_t h, void* p, void* stream, void* const* events) {
+  return guarded([&] {
+    throw_if(!h || !p || !events, "NULL argument");
+    for (int i = 0; i < 8; ++i) throw_if(!events[i], "NULL event");
+    check_device(h->device);
+    mdft::check_device_waits();
+    conv_execute(h, p, as_stream(stream), nullptr, 0, reinterpret_cast<cudaEvent_t const*>(events));
   });
 }
 
@@ -818,6 +858,10 @@ int mdft_luc_write(const char* path, const int* luc_index, const double* luc, in
     std::memcpy(t.tab.data(), luc, sizeof(double) * 2 * t.tab.size());
     mdft::write_luc_file(path, t, header ? header : "c(q) table");
   });
+}
+
+int mdft_wait_selftest(int spins, void* stream) {
+  return guarded([&] { mdft::launch_wait_selftest(spins, static_cast<cudaStream_t>(stream)); });
 }
 
 int mdft_wait_timeouts(int* count) {

@@ -477,11 +477,34 @@ struct FftAxis {
   int fixed;      // 1: compile-time-length kernel for n, 0: runtime-radix kernel
   int tma;        // 1: S > 1 tiles may move by tensor-memory-access copies
   int* err;       // device counter of timed-out copy waits (this device's)
+  int* flag;      // host-mapped word set to 1 by a timed-out wait (this device's)
   const void* tw;  // (n) Cx<T> : exp(-2 pi i t / n)
 };
-// The current device's counter of timed-out waits on asynchronous copies in
-// the FFT kernels (allocated on first use; call outside stream capture).
+// The current device's record of bounded device waits that ran out: a
+// device counter (exact count, read by mdft_wait_timeouts) and a word of
+// mapped page-locked host memory that the timed-out kernel sets, so the host
+// sees it without a synchronisation.  Created on first use (call outside
+// stream capture).
+struct WaitStatus {
+  int* count;                // device memory
+  int* flag_dev;             // device address of the mapped host word
+  volatile int* flag_host;   // host address of the same word
+};
+const WaitStatus& device_wait_status();
 int* fft_wait_error_counter();
+// Throws Error(MDFT_ERR_TIMEOUT) if a kernel launched earlier on the current
+// device reported a timed-out wait since the last check, and clears the
+// report: a kernel that gives up on a wait leaves its output wrong, and the
+// next call that launches work on the device says so.
+void check_device_waits();
+// Launches a one-CTA kernel whose bounded wait runs out (nothing arrives).
+void launch_wait_selftest(long long spins, cudaStream_t s);
+// Device side of a timed-out wait: count it and raise the host-visible word.
+__device__ __forceinline__ void note_wait_timeout(int* count, int* flag) {
+  atomicAdd(count, 1);
+  *reinterpret_cast<volatile int*>(flag) = 1;
+  __threadfence_system();
+}
 bool fft_factor(int n, FftAxis& a);  // false if n has a prime factor > 13
 // Si / So: storage type of the tile on load / store (the same size, in
 // place); the double-float form keeps the projections as packed DF pairs

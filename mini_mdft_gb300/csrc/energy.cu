@@ -279,9 +279,12 @@ template void launch_delta_f<float>(const float*, const float*, const double*, f
 // it keeps the last call's contents, so calls that overlap on the GPU (on
 // different streams, or from different threads) race and must be ordered by
 // the caller.  The completion counter is cleared on the caller's stream at
-// the start of every call.  The first call on a device looks up the array's
-// device address (cudaGetSymbolAddress) for that device and caches it; make
-// that first call before any stream capture.
+// the start of every call.  Every call made outside stream capture looks up
+// the array's device address (cudaGetSymbolAddress) on the current device
+// and caches it, so a context torn down and created again (cudaDeviceReset)
+// is seen at the next such call; a call on a capturing stream uses the
+// cached address, so the first call on a device must come before any stream
+// capture.
 // ---------------------------------------------------------------------------
 namespace {
 constexpr size_t kNoAllocMaxPartials = size_t(1) << 16;
@@ -292,19 +295,25 @@ constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mu;
 void* g_noalloc_ptr[kMaxDevices] = {nullptr};
 
-// Device address of g_noalloc_scratch on the current device, looked up once
-// per device with that device current.
-void* noalloc_scratch_for_current_device() {
+// Device address of g_noalloc_scratch on the current device.  Looked up with
+// that device current whenever `stream` is not capturing (a reset context
+// loads the module again, possibly at another address); a capturing stream
+// takes the address cached by an earlier call.
+void* noalloc_scratch_for_current_device(cudaStream_t stream) {
   int dev = 0;
   cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
   throw_if(dev < 0 || dev >= kMaxDevices, "device index out of range for the fixed scratch table");
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cuda_check(cudaStreamIsCapturing(stream, &cap), "cudaStreamIsCapturing");
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
+  if (cap == cudaStreamCaptureStatusNone) {
     void* ptr = nullptr;
     cuda_check(cudaGetSymbolAddress(&ptr, g_noalloc_scratch), "cudaGetSymbolAddress(fixed scratch)");
     throw_if(ptr == nullptr, "cudaGetSymbolAddress returned a null scratch address", 2);
     g_noalloc_ptr[dev] = ptr;
   }
+  throw_if(!g_noalloc_ptr[dev],
+           "mdft_get_delta_f_noalloc: the first call on a device must come before any stream capture", 2);
   return g_noalloc_ptr[dev];
 }
 }  // namespace
@@ -328,7 +337,7 @@ extern "C" int mdft_get_delta_f_noalloc(const void* xi, const void* vexc, const 
                  std::to_string(kNoAllocMaxPartials * 32) + " points",
              4);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    unsigned char* scratch = static_cast<unsigned char*>(noalloc_scratch_for_current_device());
+    unsigned char* scratch = static_cast<unsigned char*>(noalloc_scratch_for_current_device(s));
     // partials first, then the completion counter, which must start at zero
     unsigned char* counter = scratch + sizeof(double2) * nb;
     cuda_check(cudaMemsetAsync(counter, 0, sizeof(unsigned), s), "cudaMemsetAsync(fixed scratch counter)");

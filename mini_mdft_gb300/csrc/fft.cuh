@@ -628,7 +628,7 @@ fft_tma_kernel(const __grid_constant__ CUtensorMap tm, const FftAxis A, long lon
   const bool late = !mbar_wait(bar_a, 0, kTmaWaitLimit);
   if (__syncthreads_or(late)) {
     if (tid == 0) {
-      atomicAdd(A.err, 1);
+      note_wait_timeout(A.err, A.flag);
       mbar_wait(bar_a, 0, kTmaWaitLimit);  // the copy may still be writing the tile
     }
     return;
@@ -748,12 +748,14 @@ template <typename Si, typename So, typename C>
 void fft_axis_finish(FftAxis& a) {
   a.tma = 0;
   a.err = nullptr;
+  a.flag = nullptr;
   if (fixed_supported(a.n)) {
     a.fixed = 1;
     a.cols = fixed_cols<C>();
     fixed_setup<Si, So, C>(a.n, a.smem);
     if (a.S > 1) {
-      a.err = fft_wait_error_counter();
+      a.err = device_wait_status().count;
+      a.flag = device_wait_status().flag_dev;
       tma_setup<Si, So, C>(a.n);
       a.tma = 1;
     }

@@ -1,0 +1,137 @@
+"""The cproj stages at the workload sizes, against the oracle on the same
+seeded inputs:
+
+* 64^3 / 30 A / mmax 3 -- the configuration the bench times;
+* 96^3 / 40 A / mmax 4 -- FFT length 96 (radix-3 stages), np 55, ntheta 5;
+* 128^3 / 50 A / mmax 5 -- FFT length 128, np 88, ntheta 6, nq 1395;
+
+all mrso 2, with the generators of mini_mdft_gb300/inputs.py: delta_rho ~
+U[-0.1, 0.1] (seed 0), c_i(q) = a_i exp(-s_i q^2) in the Luc layout (seed 2,
+dq 0.01, nq = int(q_max/dq + 0.5) + 2 as the reference's reader derives it)
+and xi ~ U[0.9, 1.1] (seed 1).  Each form (FP64, double-float on FP64
+fields, FP32 fields) is compared stage by stage with the oracle's FP64
+restatement of src/mini-mdft.hpp:137-183:
+
+    p = angl2proj(delta_rho)            MDFT_OrientationProjectionTransform.hpp:270-380
+    execute(p)                          MDFT_Convolution.hpp:326-548
+    vexc = proj2angl(p)                 MDFT_OrientationProjectionTransform.hpp:391-484
+    df, ff = get_delta_f(xi, vexc)      MDFT_Solvent.hpp:617-660
+    angl2proj(rho0 (xi^2 - 1))          MDFT_Solvent.hpp:578-596 fused into the load
+
+Tolerances (max-norm relative): FP64 and double-float 1e-12 on every field
+and on ff; FP32 1e-4 on fields and 1e-6 on ff.  The oracle runs on all host
+cores (OpenMP); its outputs are moved to the GPU, where the comparisons run.
+"""
+import gc
+
+import numpy as np
+import pytest
+
+import oracle as O
+from mini_mdft_gb300 import inputs as I
+
+pytestmark = pytest.mark.gpu
+
+MRSO = 2
+DQ = 0.01
+CONFIGS = [
+    pytest.param((64, 64, 64), (30., 30., 30.), 3, id="64cubed-30A-mmax3"),
+    pytest.param((96, 96, 96), (40., 40., 40.), 4, id="96cubed-40A-mmax4"),
+    pytest.param((128, 128, 128), (50., 50., 50.), 5, id="128cubed-50A-mmax5"),
+]
+TOL = {"f64": (1e-12, 1e-12), "f64df": (1e-12, 1e-12), "f32": (1e-4, 1e-6)}
+
+
+def _rel(a, b):
+    """max |a - b| / max |b| on the device, in FP64."""
+    import torch
+    d = a.to(b.dtype) - b
+    return (torch.max(torch.abs(d)) / torch.max(torch.abs(b))).item()
+
+
+def _free():
+    import torch
+    gc.collect()
+    torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("n,box,mmax", CONFIGS)
+def test_cproj_stages_against_oracle(gpu_lib, n, box, mmax):
+    import torch
+    M = gpu_lib
+    # ---- oracle (FP64, host) ----
+    o = O.Oracle(n, box, mmax, MRSO)
+    nq = I.nq_for(n, box, DQ)
+    assert nq == o.nq_for_dq(DQ)
+    idx, tab = I.synthetic_cq(mmax, MRSO, nq, DQ)
+    o.set_luc(idx, tab, DQ)
+    N = o.N
+    shape_o = (N, o.ntheta, o.nphi, o.npsi)
+    rho0, pref = I.tip3p_constants(MRSO)
+    _, _, w = o.angular()
+    dev = lambda a: torch.from_numpy(a).cuda()
+
+    dr = I.synthetic_delta_rho(N, mmax, MRSO)
+    p_ref = o.angl2proj(dr)
+    ref = {"p": dev(p_ref)}
+    pc_ref = o.conv_execute(p_ref)
+    del p_ref
+    ref["pc"] = dev(pc_ref)
+    vexc_ref = o.proj2angl(pc_ref)
+    del pc_ref
+    ref["vexc"] = dev(vexc_ref)
+    dr_dev = dev(dr)
+    del dr
+    xi = I.synthetic_xi(N, mmax, MRSO)
+    df_ref, ff_ref = O.delta_f(xi, vexc_ref, w, rho0, pref)
+    del vexc_ref
+    ref["df"] = dev(df_ref)
+    del df_ref
+    ref["p_xi"] = dev(o.angl2proj(O.delta_rho(xi, rho0)))
+    xi_dev = dev(xi)
+    del xi
+    del o
+    gc.collect()
+    w_t = torch.from_numpy(w)
+
+    # ---- the three forms through the C ABI ----
+    errors = {}
+    sg, ag = M.SpatialGrid(n, box), M.AngularGrid(mmax, MRSO)
+    for prec in ("f64", "f64df", "f32"):
+        rd, cd = (torch.float32, torch.complex64) if prec == "f32" else (torch.float64, torch.complex128)
+        opt = M.OrientationProjectionTransform(sg, ag, M.OrientationProjectionMap(ag), precision=prec)
+        conv = M.Convolution.from_table(idx, tab, DQ, sg, ag, precision=prec)
+        x = dr_dev.to(rd)
+        p = torch.zeros((ag.m_np,) + tuple(n), dtype=cd, device="cuda")
+        e = {}
+        opt.angl2proj(x, p)
+        e["p"] = _rel(p, ref["p"])
+        conv.execute(p)
+        e["pc"] = _rel(p, ref["pc"])
+        vexc = torch.zeros(shape_o, dtype=rd, device="cuda")
+        opt.proj2angl(p, vexc)
+        e["vexc"] = _rel(vexc, ref["vexc"])
+        del x
+        xr = xi_dev.to(rd)
+        df = torch.zeros_like(xr)
+        ff = M.get_delta_f(xr, vexc, w_t, df, rho0, pref)
+        e["df"] = _rel(df, ref["df"])
+        e["ff"] = abs(ff - ff_ref) / abs(ff_ref)
+        del df, vexc
+        opt.angl2proj_from_xi(xr, rho0, p)
+        e["p_xi"] = _rel(p, ref["p_xi"])
+        torch.cuda.synchronize()
+        errors[prec] = e
+        del opt, conv, p, xr
+        _free()
+    del ref, dr_dev, xi_dev
+    _free()
+
+    bad = []
+    for prec, e in errors.items():
+        tf, te = TOL[prec]
+        for k, v in e.items():
+            lim = te if k == "ff" else tf
+            if not v <= lim:
+                bad.append("%s %s: %.3e > %.0e" % (prec, k, v, lim))
+    assert not bad, "; ".join(bad) + " | all errors: %r" % errors

@@ -2,7 +2,9 @@
 cannot allocate device memory during their solve (e.g. an application whose
 pool allocator owns the whole GPU, or a loop that must not pay for an
 allocation call).  Its scratch is a fixed array inside the library, so it
-must give what mdft_get_delta_f gives, call after call.
+must give what mdft_get_delta_f gives, call after call, and draw nothing from
+the device's stream-ordered memory pool (the pool mdft_get_delta_f takes its
+temporary from).
 
 Collected last (file name) so that a run stopping at the first failure has
 run every other test first.  Calls go straight through the C ABI."""
@@ -14,6 +16,9 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 MAX_POINTS = 1 << 21  # 2,097,152 grid points (128^3): the fixed scratch limit
+
+# CUmemPool_attribute value of CU_MEMPOOL_ATTR_USED_MEM_HIGH (cuda.h)
+_USED_MEM_HIGH = 8
 
 
 def _ptr(t):
@@ -27,28 +32,61 @@ def _run(L, fn, xi, vexc, w, df, ff, prec, stream):
     return rc
 
 
-@pytest.mark.parametrize("prec", [0, 1])
+class _PoolWatermark:
+    """High-water mark of the current device's stream-ordered memory pool
+    (the one cudaMallocAsync draws from), read through the driver API."""
+
+    def __init__(self):
+        self.cu = C.CDLL("libcuda.so.1")
+        dev = C.c_int(0)
+        assert self.cu.cuCtxGetDevice(C.byref(dev)) == 0
+        self.pool = C.c_void_p(0)
+        assert self.cu.cuDeviceGetMemPool(C.byref(self.pool), dev) == 0
+
+    def reset(self):
+        zero = C.c_uint64(0)
+        assert self.cu.cuMemPoolSetAttribute(self.pool, _USED_MEM_HIGH, C.byref(zero)) == 0
+
+    def high(self):
+        v = C.c_uint64(0)
+        assert self.cu.cuMemPoolGetAttribute(self.pool, _USED_MEM_HIGH, C.byref(v)) == 0
+        return v.value
+
+
+@pytest.mark.parametrize("prec", [0, 1, 2])
 def test_noalloc_matches_allocating_entry_point_twice(gpu_lib, prec):
+    """FP64 (0), FP32 (1) and double-float on FP64 fields (2): two calls in a
+    row through the fixed scratch give the allocating call's df bit for bit
+    and its ff; the pool's high-water mark stays zero across them, and a
+    positive control shows the allocating call does move it."""
     import torch
     L = gpu_lib.lib()
-    dt = torch.float64 if prec == 0 else torch.float32
+    dt = torch.float32 if prec == 1 else torch.float64
     rng = np.random.default_rng(2024)
     shape = (40, 40, 40, 84)
     xi = torch.from_numpy(rng.uniform(0.9, 1.1, shape)).to("cuda", dt)
     vexc = torch.from_numpy(rng.uniform(-1.0, 1.0, shape)).to("cuda", dt)
     w = torch.from_numpy(rng.uniform(0.0, 1.0, 84)).to("cuda", torch.float64)
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    pool = _PoolWatermark()
 
     df_ref = torch.zeros_like(xi)
     ff_ref = torch.zeros(1, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    pool.reset()
     assert _run(L, L.mdft_get_delta_f, xi, vexc, w, df_ref, ff_ref, prec, stream) == 0
+    torch.cuda.synchronize()
+    assert pool.high() > 0  # the allocating entry point draws its temporary from the pool
 
     for _ in range(2):  # two calls in a row share the fixed scratch
         df = torch.full_like(xi, 7.0)
         ff = torch.full((1,), 7.0, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        pool.reset()
         assert _run(L, L.mdft_get_delta_f_noalloc, xi, vexc, w, df, ff, prec, stream) == 0, \
             L.mdft_last_error()
         torch.cuda.synchronize()
+        assert pool.high() == 0
         assert torch.equal(df, df_ref)
         a, b = float(ff.item()), float(ff_ref.item())
         assert abs(a - b) <= 1e-12 * abs(b)
