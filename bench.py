@@ -39,6 +39,11 @@ if ROOT not in sys.path:
 
 WORKLOAD = dict(n=(64, 64, 64), box=(30.0, 30.0, 30.0), mmax=3, mrso=2, dq=0.01)
 METRIC = "conv applies/s @64^3 mmax3"
+# the mixed-form accuracy workload (96^3 / 40 A / mmax 4) and the large
+# single solve's grid (128^3 / 50 A / mmax 5), timed per kernel beside the
+# headline
+WORKLOAD_96 = dict(n=(96, 96, 96), box=(40.0, 40.0, 40.0), mmax=4, mrso=2, dq=0.01)
+WORKLOAD_128 = dict(n=(128, 128, 128), box=(50.0, 50.0, 50.0), mmax=5, mrso=2, dq=0.01)
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -51,7 +56,10 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true", help="skip the job-server leg")
     ap.add_argument("--no-minimizer", action="store_true", help="skip the solute minimiser leg")
-    ap.add_argument("--no-large-solve", action="store_true", help="skip the 128^3 / mmax 5 solve")
+    ap.add_argument("--no-large-solve", action="store_true",
+                    help="skip the 128^3 / mmax 5 solve and per-kernel table")
+    ap.add_argument("--no-96", action="store_true",
+                    help="skip the 96^3 / mmax 4 per-kernel table and accuracy check")
     ap.add_argument("--mode", choices=["full", "steps", "energy"], default="full",
                     help="steps: only W warm-up + K timed FP64 and FP32 round trips; energy: "
                          "get_delta_f and a short solute minimisation (short, fixed launch "
@@ -255,6 +263,92 @@ def stage_times(P, reps, flush):
     out["fft_forward"] = out["fft_fwd_z"] + out["fft_fwd_y"] + out["fft_fwd_x"]
     out["fft_backward"] = out["fft_inv_x"] + out["fft_inv_y"] + out["fft_inv_z"]
     return out
+
+
+def workload_leg(wl, forms, K, W, flush, hbm_peak):
+    """Every form of the round trip on another workload: W warm-up and K
+    timed round trips (CUDA events, L2 flushed between them), the per-kernel
+    table and the round trip's fraction of the HBM roof.  Returns (entry,
+    problems); the problems stay resident for the accuracy check."""
+    import torch
+    s = sizes(wl)
+    n = wl["n"]
+    out = {"workload": "%dx%dx%d grid, box %g A, mmax %d, mrso %d (no %d, np %d, np_new %d): "
+                       "angl2proj + Convolution::execute + proj2angl"
+                       % (n[0], n[1], n[2], wl["box"][0], wl["mmax"], wl["mrso"], s["no"], s["np"], s["np_new"]),
+           "forms": {}}
+    probs = {}
+    for f in forms:
+        P = make_problem(f, wl)
+        for _ in range(W):
+            step(P)
+        torch.cuda.synchronize()
+        secs = timed_steps(P, K, flush)
+        st = stage_times(P, 3, flush)
+        rt = algorithmic_bytes(s, 4 if f == "f32" else 8)["round_trip"]
+        out["forms"][f] = {"applies_per_s": K / secs, "ms_per_step": secs / K * 1e3,
+                           "round_trip_hbm_frac": rt / (secs / K) / 1e9 / hbm_peak,
+                           "arithmetic": FORM_NAMES[f],
+                           "kernels": per_kernel_table(st, f, s, hbm_peak)}
+        probs[f] = P
+    return out, probs
+
+
+def oracle_errors(probs, wl):
+    """Checker (CPU-baseline leg only): the oracle's FP64 stages on the same
+    seeded inputs, and every form's relative error (max norm) against them
+    in projections (angl2proj), convolved projections (execute), vexc, the
+    gradient df and the energy ff of get_delta_f (xi ~ U[0.9, 1.1], seed 1;
+    TIP3P rho0 and prefactor)."""
+    import torch
+
+    import mini_mdft_gb300 as M
+    import oracle as O
+    from mini_mdft_gb300 import inputs as I
+    n, box, mmax, mrso, dq = (wl[k] for k in ("n", "box", "mmax", "mrso", "dq"))
+    t0 = time.perf_counter()
+    o = O.Oracle(n, box, mmax, mrso, threads=os.cpu_count() or 1)
+    any_p = next(iter(probs.values()))
+    o.set_luc(any_p["idx"], any_p["tab"], dq)
+    p_ref = o.angl2proj(any_p["dr_host"])
+    ref = {"p": torch.from_numpy(p_ref).cuda()}
+    pc_ref = o.conv_execute(p_ref)
+    del p_ref
+    ref["pc"] = torch.from_numpy(pc_ref).cuda()
+    vexc_ref = o.proj2angl(pc_ref)
+    del pc_ref
+    rho0, pref = I.tip3p_constants(mrso)
+    xi = I.synthetic_xi(o.N, mmax, mrso)
+    _, _, w = o.angular()
+    df_ref, ff_ref = O.delta_f(xi, vexc_ref, w, rho0, pref)
+    ref["vexc"] = torch.from_numpy(vexc_ref).cuda()
+    ref["df"] = torch.from_numpy(df_ref).cuda()
+    del vexc_ref, df_ref, o
+    oracle_s = time.perf_counter() - t0
+    xt = torch.from_numpy(xi).cuda()
+    wt = torch.from_numpy(w)
+
+    def rel(a, b):
+        return (torch.max(torch.abs(a.to(b.dtype) - b)) / torch.max(torch.abs(b))).item()
+
+    errs = {}
+    for f, P in probs.items():
+        P["opt"].angl2proj(P["dr"], P["p"])
+        e = {"projections": rel(P["p"], ref["p"])}
+        P["conv"].execute(P["p"])
+        e["convolved_projections"] = rel(P["p"], ref["pc"])
+        P["opt"].proj2angl(P["p"], P["vexc"])
+        e["vexc"] = rel(P["vexc"], ref["vexc"])
+        x = xt.to(P["rd"])
+        df = torch.empty_like(x)
+        ff = M.get_delta_f(x, P["vexc"], wt, df, rho0, pref)
+        e["gradient_df"] = rel(df, ref["df"])
+        e["energy_ff"] = abs(ff - ff_ref) / abs(ff_ref)
+        errs[f] = e
+        del x, df
+    torch.cuda.synchronize()
+    return {"vs": "FP64 oracle (CPU restatement) on the same seeded inputs, max-norm relative",
+            "oracle_seconds": oracle_s, "errors": errs}
 
 
 def e2e_steps(P, K, warm):
@@ -957,6 +1051,13 @@ def run_ours(args):
         "forms": {f: form_entry(f) for f in forms},
         "mixed": dict(form_entry("f32"), speedup_vs_f64_form=form_secs[head] / form_secs["f32"]),
     }
+    P96 = None
+    if rank == 0 and not args.no_96:
+        out["workload_96"], P96 = workload_leg(WORKLOAD_96, forms, 10, 3, flush, hbm_peak)
+    if rank == 0 and not args.no_large_solve:
+        out["workload_128"], P128 = workload_leg(WORKLOAD_128, forms, 5, 3, flush, hbm_peak)
+        del P128
+        torch.cuda.empty_cache()
     if rank == 0 and not args.no_serving:
         out["serving"] = serving_run(head)
     if rank == 0 and not args.no_minimizer:
@@ -970,6 +1071,10 @@ def run_ours(args):
         out["cpu_baseline"] = {"value": rate, "unit": "applies/s", "cores": cores, "kind": "port",
                                "sample": "%d full 64^3 FP64 round trips in %.1f s (CPU restatement, "
                                          "OpenMP, all host threads)" % (reps, el)}
+        if P96 is not None:  # the oracle as the checker of the 96^3 / mmax 4 forms
+            out["workload_96"]["accuracy"] = oracle_errors(P96, WORKLOAD_96)
+    P96 = None
+    torch.cuda.empty_cache()
     if rank == 0:
         print(json.dumps(out), flush=True)
     if dist:

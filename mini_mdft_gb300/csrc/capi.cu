@@ -320,6 +320,24 @@ void conv_build(mdft_conv_s* h, const mdft::LucTable& t) {
         h->ceff.upload(ce.data(), sizeof(Cx<T>) * ce.size());
         for (int i = 0; i < h->npairs; ++i) info[i].z = row_of[i];
         O.ceff = h->ceff.ptr;
+        // The FP32 split kernel stages its CTA's rows in shared memory (the
+        // pairs run in |q| order, so rows increase along the list): at mmax
+        // <= 3 that took the 64^3 k-space step from 134 to 123 us on one
+        // GB300; at mmax 4 (96^3) the larger rows cost more than they saved
+        // (1.46 -> 1.96 ms), and the double-float kernel, issue-bound on a
+        // list in linear order, gained nothing from a |q| order with staged
+        // rows (331 -> 379 us).
+        if (by_q && g.mmax <= 3) {
+          const int budget = 16 << 10;
+          const size_t row_bytes = sizeof(Cx<T>) * (size_t)g.np_new;
+          O.crow_stage = (int)std::min<size_t>(16, (size_t)budget / row_bytes);
+          if (O.crow_stage > 0) {
+            O.cstage_off = (O.smem + 15) & ~size_t(15);
+            O.smem = O.cstage_off + row_bytes * O.crow_stage;
+            mdft::oz_lane_attr<S, T>(O);
+            if constexpr (!std::is_same<S, T>::value) mdft::oz_lane_attr<T, T>(O);
+          }
+        }
       }
     }
     h->pinfo.upload(info.data(), sizeof(int4) * info.size());

@@ -539,6 +539,11 @@ struct OzPlan {
   // (nu, np_new) Cx<C>: c(|q|) already interpolated for each distinct |q| of
   // the pair list (lane path; pinfo.z then indexes its rows), or null
   const void* ceff;
+  // split lane kernel on a pair list sorted by |q| (ceff rows in increasing
+  // |q|): up to crow_stage consecutive ceff rows, from the row of the CTA's
+  // first pair, are staged in shared memory at byte offset cstage_off
+  int crow_stage;
+  size_t cstage_off;
   int warps_per_cta;
   size_t smem;
   // Lane-per-pair path: per-pair geometry computed once at plan creation.

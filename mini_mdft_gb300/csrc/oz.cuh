@@ -595,6 +595,23 @@ oz_lane_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
   // column for the conjugated terms.
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int side = lane >> 4;
+  // c(|q|) rows of the CTA's pairs: the list is sorted by |q|, so the CTA's
+  // pairs use a short run of consecutive rows from the row of its first
+  // pair; up to P.crow_stage of them are copied to shared memory by all
+  // threads (before any warp leaves), later rows are read from global memory
+  int r0 = 0, nst = 0;
+  Cx<C>* cst = nullptr;
+  if (P.crow_stage > 0) {
+    const long long first = (long long)blockIdx.x * P.warps_per_cta * 16;
+    const long long last = min(first + (long long)P.warps_per_cta * 16, (long long)P.npairs) - 1;
+    r0 = P.pinfo[first].z;
+    nst = min(P.crow_stage, P.pinfo[last].z - r0 + 1);
+    cst = reinterpret_cast<Cx<C>*>(sm + P.cstage_off);
+    const Cx<C>* src = static_cast<const Cx<C>*>(P.ceff) + (size_t)r0 * P.np_new;
+    const int cnt = nst * P.np_new;
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) cst[i] = src[i];
+    __syncthreads();
+  }
   const long long grp = (long long)blockIdx.x * P.warps_per_cta + wib;
   if (grp * 16 >= P.npairs) return;  // whole warp exits together
   const long long pair = grp * 16 + (lane & 15);
@@ -690,7 +707,10 @@ oz_lane_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
   const C alpha = static_cast<const C*>(P.palpha)[pair];
   const C beta = C(1) - alpha;
   const bool pre = P.ceff != nullptr;
-  const Cx<C>* clo = static_cast<const Cx<C>*>(pre ? P.ceff : P.ctab) + (size_t)iq * P.np_new;
+  const int slot = iq - r0;  // staged row of this pair (padding pairs may fall outside)
+  const Cx<C>* clo = (slot >= 0 && slot < nst)
+                         ? cst + (size_t)slot * P.np_new
+                         : static_cast<const Cx<C>*>(pre ? P.ceff : P.ctab) + (size_t)iq * P.np_new;
   const Cx<C>* chi = clo + P.np_new;
   const int other = lane ^ 16;
   // c(|q|) of coefficient ia, and term (n, nu2) of the OZ sum of projection

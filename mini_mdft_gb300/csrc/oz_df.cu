@@ -10,5 +10,6 @@ template void oz_build_rtab<DF>(const OzPlan&, DevBuf&);
 template void launch_oz<double, DF>(const OzPlan&, Cx<double>*, cudaStream_t);
 template void launch_oz<DF, DF>(const OzPlan&, Cx<DF>*, cudaStream_t);
 template void oz_lane_attr<DF, DF>(const OzPlan&);
+template void oz_lane_attr<double, DF>(const OzPlan&);
 
 }  // namespace mdft
