@@ -93,6 +93,12 @@ int mdft_grid_angular(mdft_grid_t g, double* theta, double* wtheta, double* w);
  * p (mmax+1, 2mmax+1, mmax/mrso+1), the rest (np), wigner (ntheta, np). */
 int mdft_grid_opmap(mdft_grid_t g, int* p, int* m, int* mup, int* mu,
                     int* mu2, double* wigner);
+/* The angular transforms at one grid point as dense real matrices (FP64,
+ * row-major), the operators the tensor-core path multiplies by: a2p
+ * (2 np, no) maps the orientation values to (Re, Im) of the projections
+ * (MDFT_OrientationProjectionTransform.hpp:270-380), p2a (no, 2 np) maps
+ * them back (:391-484).  Host-only.  No counterpart in the reference. */
+int mdft_grid_ang_matrices(mdft_grid_t g, double* a2p, double* p2a);
 
 /* ---- OrientationProjectionTransform ------------------------------------
  * Constructor (MDFT_OrientationProjectionTransform.hpp:217-257): uploads the

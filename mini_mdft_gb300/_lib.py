@@ -35,6 +35,7 @@ SIGNATURES = {
     "mdft_grid_kvectors": (i32, [vp, dp, dp, dp]),
     "mdft_grid_angular": (i32, [vp, dp, dp, dp]),
     "mdft_grid_opmap": (i32, [vp, ip, ip, ip, ip, ip, dp]),
+    "mdft_grid_ang_matrices": (i32, [vp, dp, dp]),
     "mdft_opt_create": (i32, [C.POINTER(vp), vp, i32]),
     "mdft_opt_create_batched": (i32, [C.POINTER(vp), vp, i32, i32]),
     "mdft_opt_destroy": (i32, [vp]),

@@ -149,6 +149,19 @@ class OrientationProjectionMap:
     def wigner_small_d(self):
         return self._wig
 
+    def dense_matrices(self):
+        """(a2p, p2a): the angular transforms at one grid point as dense
+        real FP64 matrices, a2p (2 np, no) and p2a (no, 2 np); row 2 ip + c
+        of a2p (column of p2a) is the real (c = 0) or imaginary (c = 1)
+        part of projection ip (mdft_grid_ang_matrices).  No counterpart in
+        the reference."""
+        ag = self.angular_grid
+        g = _GridHandle((1, 1, 1), (1.0, 1.0, 1.0), ag.m_mmax, ag.m_molrotsymorder)
+        a2p = np.zeros((2 * g.np, g.no))
+        p2a = np.zeros((g.no, 2 * g.np))
+        check(lib().mdft_grid_ang_matrices(g.h, _np_d(a2p), _np_d(p2a)))
+        return a2p, p2a
+
 
 def _precision_of(dtype):
     torch = _torch()

@@ -20,7 +20,7 @@ LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libmdft_gb300.so")
 HEADER = os.path.join(ROOT, "include", "mdft_gb300.h")
 
-CU_SOURCES = ["capi.cu", "angular.cu", "angular_fast_f64.cu", "angular_fast_f32.cu", "angular_fast_df.cu", "fft_f64.cu", "fft_f32.cu", "fft_df.cu", "oz_f64.cu", "oz_f32.cu", "oz_df.cu", "oz_r2_f32.cu", "oz_r2_df.cu", "energy.cu", "server.cu", "solver.cu"]
+CU_SOURCES = ["capi.cu", "angular.cu", "angular_tc.cu", "angular_fast_f64.cu", "angular_fast_f32.cu", "angular_fast_df.cu", "fft_f64.cu", "fft_f32.cu", "fft_df.cu", "oz_f64.cu", "oz_f32.cu", "oz_df.cu", "oz_r2_f32.cu", "oz_r2_df.cu", "energy.cu", "server.cu", "solver.cu"]
 CPP_SOURCES = ["host_setup.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

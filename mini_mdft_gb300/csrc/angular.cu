@@ -12,6 +12,8 @@
 // directions and the theta contraction run out of shared memory, and p is
 // written (or read) in (np, N) layout with consecutive threads on
 // consecutive points, so no o_hat round trip to HBM exists.
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace mdft {
@@ -254,6 +256,12 @@ template <typename S, typename C>
 void launch_angl2proj(const AngPlan& P, const S* o, Cx<S>* p, bool from_xi,
                       double rho0, cudaStream_t s) {
   if (P.N == 0) return;
+  if constexpr (!std::is_same<C, double>::value) {
+    if ((P.tc & 1) && !from_xi) {
+      ang_tc_launch<S>(P, 0, o, reinterpret_cast<S*>(p), s);
+      return;
+    }
+  }
   if (P.fast) {
     clear_stale_error();
     ang_fast_a2p<S, C>(P, o, p, from_xi, rho0, s);
@@ -273,6 +281,12 @@ void launch_angl2proj(const AngPlan& P, const S* o, Cx<S>* p, bool from_xi,
 template <typename S, typename C>
 void launch_proj2angl(const AngPlan& P, const Cx<S>* p, S* o, cudaStream_t s) {
   if (P.N == 0) return;
+  if constexpr (!std::is_same<C, double>::value) {
+    if (P.tc & 2) {
+      ang_tc_launch<S>(P, 1, reinterpret_cast<const S*>(p), o, s);
+      return;
+    }
+  }
   if (P.fast) {
     clear_stale_error();
     ang_fast_p2a<S, C>(P, p, o, s);

@@ -14,6 +14,8 @@
 #include <type_traits>
 #include <vector>
 
+#include <cstdlib>
+
 #include "../../include/mdft_gb300.h"
 #include "common.cuh"
 #include "handles.hpp"
@@ -145,6 +147,18 @@ void opt_build(mdft_opt_s* h) {
   P.ip_mu2 = h->ip_mu2.as<int>();
   P.pmap = h->pmap.as<int>();
   mdft::ang_plan_finish<S, T>(P);
+  // the double-float and FP32 forms run the transforms as tensor-core GEMMs
+  // with exact digit slicing where the shape fits that kernel
+  if constexpr (!std::is_same<T, double>::value) {
+    const char* env = std::getenv("MDFT_ANG_TC");
+    const bool use = !(env && env[0] == '0');
+    if (use && mdft::ang_tc_setup<S>(P.tc_a2p, mdft::ang_matrix_a2p(g), 2 * np, g.no, h->tc_bsl_a2p,
+                                     h->tc_fexp_a2p))
+      P.tc |= 1;
+    if (use && mdft::ang_tc_setup<S>(P.tc_p2a, mdft::ang_matrix_p2a(g), g.no, 2 * np, h->tc_bsl_p2a,
+                                     h->tc_fexp_p2a))
+      P.tc |= 2;
+  }
 }
 
 template <typename ST, typename T>
@@ -525,6 +539,15 @@ int mdft_grid_opmap(mdft_grid_t h, int* p, int* m, int* mup, int* mu, int* mu2, 
     std::memcpy(mu, g.mu.data(), sizeof(int) * g.np);
     std::memcpy(mu2, g.mu2.data(), sizeof(int) * g.np);
     std::memcpy(wigner, g.wigner.data(), sizeof(double) * g.wigner.size());
+  });
+}
+
+int mdft_grid_ang_matrices(mdft_grid_t h, double* a2p, double* p2a) {
+  return guarded([&] {
+    throw_if(!h || !a2p || !p2a, "NULL argument");
+    const auto A = mdft::ang_matrix_a2p(h->g), B = mdft::ang_matrix_p2a(h->g);
+    std::memcpy(a2p, A.data(), sizeof(double) * A.size());
+    std::memcpy(p2a, B.data(), sizeof(double) * B.size());
   });
 }
 

@@ -7,6 +7,7 @@
 #include <cstdint>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "host_setup.hpp"
 
@@ -428,10 +429,26 @@ struct DevBuf {
 // ---------------------------------------------------------------------------
 // Orientation <-> projection transform plan (device tables).
 // ---------------------------------------------------------------------------
+// One direction of the tensor-core angular transform (angular_tc.cu): the
+// dense per-point matrix of ang_matrix_a2p / ang_matrix_p2a applied to all
+// grid points as one GEMM, both operands as exact BF16 digit slices.
+struct AngTcDir {
+  int K, nkc;            // real inputs per point; 16-wide K chunks
+  int NOUT, NC, nnc;     // real outputs per point; N-chunk width; N-chunks
+  int tcols;             // tensor-memory columns per CTA
+  int nsm;               // persistent grid: one CTA per SM
+  size_t raw_bytes;      // shared-memory bytes of one raw input tile
+  size_t smem;           // dynamic shared memory per CTA
+  const uint16_t* bsl;   // (nnc, nkc, digits, 2, NC/8, 8, 8) BF16 digits of the matrix
+  const int* fexp;       // (nnc NC) exponent of each output column's digits
+};
+
 struct AngPlan {
   long long N;  // grid points
   int ntheta, nphi, npsi, K, mmax, mrso, np, no;
   int tile_a2p, tile_p2a;           // points per CTA
+  int tc;                           // bit 0 / 1: angl2proj / proj2angl on the tensor cores
+  AngTcDir tc_a2p, tc_p2a;
   int fast;                         // 1: compile-time-shape kernels (angular_fast.cu)
   size_t smem_a2p, smem_p2a;        // dynamic shared memory bytes
   const void* coef_a2p;             // (ntheta, np) T : d * wtheta * fm / (nphi*npsi)
@@ -453,6 +470,14 @@ template <typename S, typename C>
 void launch_proj2angl(const AngPlan& P, const Cx<S>* p, S* o, cudaStream_t s);
 template <typename S, typename C>
 void ang_plan_finish(AngPlan& P);
+// Tensor-core path: digit slices of the dense matrices (host), launches.
+// S = double (FP64 fields, the double-float form) or float (mixed form).
+// ang_tc_setup returns false (and leaves D unused) when the shape does not fit
+// the kernel: K above the exact-sum limit, or the tiles beyond shared memory.
+template <typename S>
+bool ang_tc_setup(AngTcDir& D, const std::vector<double>& T, int nout, int k, DevBuf& bsl, DevBuf& fexp);
+template <typename S>
+void ang_tc_launch(const AngPlan& P, int dir, const S* in, S* out, cudaStream_t s);
 // Compile-time-shape kernels for (mmax, mrso) in {1..5} x {2}.
 bool ang_fast_supported(int mmax, int mrso);
 template <typename S, typename C>

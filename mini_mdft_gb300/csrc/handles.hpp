@@ -19,6 +19,7 @@ struct mdft_opt_s {
   int device;
   int batch = 1;  // same-shape fields per call, stored back to back
   mdft::DevBuf coef_a2p, coef_p2a, tw_phi, tw_psi, ip_m, ip_mup, ip_mu2, pmap;
+  mdft::DevBuf tc_bsl_a2p, tc_fexp_a2p, tc_bsl_p2a, tc_fexp_p2a;  // tensor-core path
   mdft::AngPlan plan{};
   explicit mdft_opt_s(const mdft::Grid& gg) : g(gg) {}
 };

@@ -60,6 +60,52 @@ void gauss_legendre(int n, double* x, double* w) {
   }
 }
 
+namespace {
+// 2 pi (a / na + b / nb) reduced exactly to [0, 2 pi) before the
+// trigonometric functions (long double)
+long double ang_angle(int a, int na, int b, int nb) {
+  const long long num = (long long)(((a % na) + na) % na) * nb + (long long)(((b % nb) + nb) % nb) * na;
+  const long long den = (long long)na * nb;
+  const long double pi = 3.141592653589793238462643383279502884L;
+  return 2.0L * pi * (long double)(num % den) / (long double)den;
+}
+}  // namespace
+
+std::vector<double> ang_matrix_a2p(const Grid& g) {
+  const int no = g.no, np = g.np;
+  std::vector<double> T((size_t)2 * np * no, 0.0);
+  const long double inv = 1.0L / (long double)(g.nphi * g.npsi);
+  for (int ip = 0; ip < np; ++ip)
+    for (int th = 0; th < g.ntheta; ++th) {
+      const long double c = (long double)g.wigner[(size_t)th * np + ip] * g.wtheta[th] * g.fm[g.m[ip]] * inv;
+      for (int f = 0; f < g.nphi; ++f)
+        for (int s = 0; s < g.npsi; ++s) {
+          const long double a = ang_angle(g.mup[ip] * f, g.nphi, g.mu2[ip] * s, g.npsi);
+          const size_t k = ((size_t)th * g.nphi + f) * g.npsi + s;
+          T[(size_t)(2 * ip) * no + k] = (double)(c * std::cos(a));
+          T[(size_t)(2 * ip + 1) * no + k] = (double)(c * std::sin(a));
+        }
+    }
+  return T;
+}
+
+std::vector<double> ang_matrix_p2a(const Grid& g) {
+  const int no = g.no, np = g.np;
+  std::vector<double> T((size_t)no * 2 * np, 0.0);
+  for (int ip = 0; ip < np; ++ip)
+    for (int th = 0; th < g.ntheta; ++th) {
+      const long double c = (long double)g.wigner[(size_t)th * np + ip] * g.fm[g.m[ip]] * (g.mu2[ip] == 0 ? 1 : 2);
+      for (int f = 0; f < g.nphi; ++f)
+        for (int s = 0; s < g.npsi; ++s) {
+          const long double a = ang_angle(g.mup[ip] * f, g.nphi, g.mu2[ip] * s, g.npsi);
+          const size_t k = ((size_t)th * g.nphi + f) * g.npsi + s;
+          T[k * 2 * np + 2 * ip] = (double)(c * std::cos(a));
+          T[k * 2 * np + 2 * ip + 1] = (double)(c * std::sin(a));
+        }
+    }
+  return T;
+}
+
 // wigner_small_d (common/MDFT_Wigner.hpp:63-130): Legendre recursion when
 // one index is zero, the closed-form sum otherwise.
 double wigner_small_d(int m, int mu, int mup, double theta) {

@@ -47,6 +47,23 @@ struct Grid {
   double qmax() const;
 };
 
+// The angular transforms at one grid point are linear maps between the no
+// real orientation values and the np complex projections; as dense real
+// matrices (row-major, FP64):
+//   angl2proj (MDFT_OrientationProjectionTransform.hpp:270-380): (2 np, no),
+//     row 2 ip + c is Re (c = 0) / Im (c = 1) of p(ip), column
+//     (theta nphi + phi) npsi + psi; entry
+//     d(theta, ip) wtheta fm(m) / (nphi npsi) x cos / sin of
+//     2 pi (mup phi / nphi + mu2 psi / npsi)  (the conjugated, unnormalised
+//     rfft2 over (phi, psi) read at (mup mod nphi, mu2), contracted over theta);
+//   proj2angl (:391-484): (no, 2 np), entry
+//     w(mu2) d(theta, ip) fm(m) x cos / sin of the same angle, w = 1 for
+//     mu2 = 0 and 2 otherwise (the synthesis over m, the scatter to FFT order
+//     and the unnormalised C2R transform, which keeps the real part of the
+//     kpsi = 0 column).
+std::vector<double> ang_matrix_a2p(const Grid& g);
+std::vector<double> ang_matrix_p2a(const Grid& g);
+
 double wigner_small_d(int m, int mu, int mup, double theta);
 void gauss_legendre(int n, double* x, double* w);
 
