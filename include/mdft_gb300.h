@@ -102,7 +102,15 @@ int mdft_grid_ang_matrices(mdft_grid_t g, double* a2p, double* p2a);
 
 /* ---- OrientationProjectionTransform ------------------------------------
  * Constructor (MDFT_OrientationProjectionTransform.hpp:217-257): uploads the
- * Wigner-d/quadrature tables to the current device. */
+ * Wigner-d/quadrature tables to the current device.  With MDFT_ANG_TC=1 in
+ * the environment at create time, MDFT_F64_DF and MDFT_F32 handles run
+ * angl2proj (except the fused form from xi) and proj2angl as tensor-core
+ * GEMMs over the dense per-point matrices (mdft_grid_ang_matrices) with exact
+ * BF16 digit slicing, where the shape fits that kernel (at most 288 inputs
+ * per point, and the input tile, digit stages and matrix within shared
+ * memory: mmax <= 3 for mrso 2); the results agree with the default kernels
+ * within each form's tolerance.  Off by default (slower on one GB300 at
+ * 64^3 / mmax 3). */
 int mdft_opt_create(mdft_opt_t* out, mdft_grid_t g, int precision);
 /* Batched plan: one call transforms `batch` same-shape fields stored back to
  * back, o (batch, nx*ny*nz, ntheta, nphi, npsi) and p (np, batch, nx, ny, nz).

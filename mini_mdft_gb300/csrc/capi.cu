@@ -147,15 +147,18 @@ void opt_build(mdft_opt_s* h) {
   P.ip_mu2 = h->ip_mu2.as<int>();
   P.pmap = h->pmap.as<int>();
   mdft::ang_plan_finish<S, T>(P);
-  // the double-float and FP32 forms run the transforms as tensor-core GEMMs
-  // with exact digit slicing where the shape fits that kernel
+  // MDFT_ANG_TC=1 at create time: the double-float and FP32 forms run the
+  // transforms as tensor-core GEMMs with exact digit slicing, where the
+  // shape fits that kernel.  Off by default: on one GB300 at 64^3 / mmax 3
+  // the CUDA-core kernels are faster (angl2proj / proj2angl: FP32 85 / 47 us
+  // against 137 / 174; double-float 217 / 189 against 252 / 312).
   if constexpr (!std::is_same<T, double>::value) {
     const char* env = std::getenv("MDFT_ANG_TC");
-    const bool use = !(env && env[0] == '0');
-    if (use && mdft::ang_tc_setup<S>(P.tc_a2p, mdft::ang_matrix_a2p(g), 2 * np, g.no, h->tc_bsl_a2p,
+    const bool use = env && env[0] == '1';
+    if (use && mdft::ang_tc_setup<S>(P.tc_a2p, mdft::ang_matrix_a2p(g), 2 * np, g.no, 0, h->tc_bsl_a2p,
                                      h->tc_fexp_a2p))
       P.tc |= 1;
-    if (use && mdft::ang_tc_setup<S>(P.tc_p2a, mdft::ang_matrix_p2a(g), g.no, 2 * np, h->tc_bsl_p2a,
+    if (use && mdft::ang_tc_setup<S>(P.tc_p2a, mdft::ang_matrix_p2a(g), g.no, 2 * np, 1, h->tc_bsl_p2a,
                                      h->tc_fexp_p2a))
       P.tc |= 2;
   }

@@ -475,7 +475,8 @@ void ang_plan_finish(AngPlan& P);
 // ang_tc_setup returns false (and leaves D unused) when the shape does not fit
 // the kernel: K above the exact-sum limit, or the tiles beyond shared memory.
 template <typename S>
-bool ang_tc_setup(AngTcDir& D, const std::vector<double>& T, int nout, int k, DevBuf& bsl, DevBuf& fexp);
+bool ang_tc_setup(AngTcDir& D, const std::vector<double>& T, int nout, int k, int dir, DevBuf& bsl,
+                  DevBuf& fexp);
 template <typename S>
 void ang_tc_launch(const AngPlan& P, int dir, const S* in, S* out, cudaStream_t s);
 // Compile-time-shape kernels for (mmax, mrso) in {1..5} x {2}.
