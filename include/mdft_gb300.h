@@ -248,6 +248,15 @@ int mdft_wait_timeouts(int* count);
  * the next FFT launch on the device then returns MDFT_ERR_TIMEOUT.  No
  * counterpart in the reference. */
 int mdft_wait_selftest(int spins, void* stream);
+/* Diagnostics: the same for the grid barrier of the persistent L-BFGS kernel
+ * (the minimiser's and the server's vector passes, one cooperative launch per
+ * step): one cooperative launch whose blocks meet at that barrier, which
+ * expects `missing` (0..1024) more arrivals than there are blocks.  With
+ * missing = 0 it passes; with missing > 0 every block gives up after about a
+ * second of polling and the timeout is recorded, so the next call that
+ * checks the device's waits returns MDFT_ERR_TIMEOUT.  No counterpart in the
+ * reference. */
+int mdft_grid_barrier_selftest(int missing, void* stream);
 
 /* ---- job server -----------------------------------------------------------
  * No counterpart in the reference (which evaluates one field per call).  A

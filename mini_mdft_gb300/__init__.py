@@ -22,6 +22,7 @@ from .api import (  # noqa: F401
     solute_vext,
     wait_timeouts,
     wait_selftest,
+    grid_barrier_selftest,
 )
 from ._lib import LIB_PATH, lib  # noqa: F401
 from .solvent import Solvents, check_mole_fractions, mole_fractions  # noqa: F401

@@ -61,6 +61,7 @@ SIGNATURES = {
     "mdft_get_delta_f_noalloc": (i32, [vp, vp, vp, vp, vp, sz, i32, f64, f64, i32, vp]),
     "mdft_wait_timeouts": (i32, [ip]),
     "mdft_wait_selftest": (i32, [i32, vp]),
+    "mdft_grid_barrier_selftest": (i32, [i32, vp]),
     "mdft_server_create": (i32, [C.POINTER(vp), i32, i32, sz]),
     "mdft_server_destroy": (i32, [vp]),
     "mdft_server_add_solvent": (i32, [vp, i32, i32, ip, dp, i32, i32, f64, f64, f64, ip]),

@@ -607,6 +607,14 @@ def wait_timeouts():
     return c.value
 
 
+def grid_barrier_selftest(missing, stream=None):
+    """One cooperative launch meeting at the persistent L-BFGS kernel's grid
+    barrier, which expects `missing` more arrivals than there are blocks
+    (mdft_grid_barrier_selftest): missing = 0 passes; missing > 0 runs out
+    after about a second and is recorded as a timed-out wait."""
+    check(lib().mdft_grid_barrier_selftest(int(missing), _stream() if stream is None else C.c_void_p(stream)))
+
+
 def wait_selftest(spins=1024, stream=None):
     """Launches one CTA whose bounded wait runs out (nothing completes its
     barrier) and is recorded as a timeout (mdft_wait_selftest): the next FFT

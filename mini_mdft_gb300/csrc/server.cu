@@ -182,6 +182,8 @@ struct Group {
   DevPtr xt, x, g, gt, vext, d, hs, hy, hinv, S, red;
   double* tails = nullptr;  // page-locked: 8 doubles per slot read back each step
   std::vector<mdft::Lbfgs> lb;
+  mdft::LbRunner lbr;  // one persistent launch per step runs every slot's L-BFGS operations
+  int queued = 1;      // fixed-step groups: steps queued by the last launch
   mdft::EgConst eg{};
   Solvent model;
   cudaStream_t stream = nullptr;
@@ -651,6 +653,7 @@ void mdft_server_s::run() {
       progress = true;
       try {
         ck(q, "server step");
+        mdft::check_device_waits();  // a persistent launch whose barrier ran out fails the group
         complete_step(*g);
       } catch (const Error& e) {
         fail_group(*g, e.what(), e.code);
@@ -662,7 +665,16 @@ void mdft_server_s::run() {
       if (g->inflight || g->k == 0) continue;
       live = true;
       try {
-        step(*g);
+        // fixed-step jobs: queue as many steps as the active job closest to
+        // its end still needs (one host round trip for all of them)
+        int r = 1;
+        if (g->kind == 0) {
+          r = 1 << 30;
+          for (auto& j : g->slots) r = std::min(r, j->n_steps - j->steps_done);
+          r = std::max(1, r);
+        }
+        g->queued = r;
+        for (int q = 0; q < r; ++q) step(*g);
         g->inflight = true;
         progress = true;
       } catch (const Error& e) {
@@ -682,12 +694,20 @@ void mdft_server_s::run() {
 // The group's step has finished: every job records it, solute jobs' minimisers
 // queue their next trial points, finished jobs leave.
 void mdft_server_s::complete_step(Group& g) {
-  for (auto& j : g.slots) j->steps_done += 1;
+  for (auto& j : g.slots) j->steps_done += g.kind == 1 ? 1 : g.queued;
   if (g.kind == 1) {
-    // highest slot first, so that a finished job's slot is refilled by a job
-    // that has already queued its own next point
-    for (int s = g.k - 1; s >= 0; --s)
-      if (g.lb[s].on_eval(g.tails + 8 * s, g.stream)) finish(g, s);
+    // every slot's minimiser decides on the host and queues its vector
+    // operations; one persistent launch runs them all; then the ended jobs
+    // leave, highest slot first, so that a finished job's slot is refilled by
+    // a job that has already queued its own next point
+    std::vector<int> ended;
+    std::vector<mdft::Lbfgs*> run;
+    for (int s = g.k - 1; s >= 0; --s) {
+      if (g.lb[s].on_eval(g.tails + 8 * s)) ended.push_back(s);
+      run.push_back(&g.lb[s]);
+    }
+    mdft::lbfgs_run(run.data(), (int)run.size(), g.lbr, g.stream);
+    for (int s : ended) finish(g, s);
   } else {
     for (int s = g.k - 1; s >= 0; --s)
       if (g.slots[s]->steps_done >= g.slots[s]->n_steps) finish(g, s);

@@ -35,7 +35,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -518,140 +520,232 @@ __global__ void __launch_bounds__(kRedThreads) eg_kernel(const EgArgs A) {
   });
 }
 
-// ---- L-BFGS vector passes --------------------------------------------------
+// ---- batched L-BFGS step: one persistent kernel over every field's ops ------
 // The search direction and the stored pairs (s, y) are FP32 vectors: the
 // two-loop recursion only forms a preconditioned direction, whose rounding
 // the line search absorbs, while the iterate and the gradient stay FP64.
 // Every dot product is a double-float Dot2 sum on the FP32 pipe (products
-// exact by FMA, compensated additions), and the threads' sums are combined
-// in double-float too (grid_reduce_df), so no pass leans on the narrow FP64
-// pipe.
-__device__ __forceinline__ DF as_df(float a) { return DF(a, 0.f); }
-__device__ __forceinline__ DF as_df(double a) { return df_from_double_bits(a); }
-__device__ __forceinline__ float as_f(float a) { return a; }
-__device__ __forceinline__ float as_f(double a) { return df_from_double_bits(a).hi; }  // nearest float
+// exact by FMA, compensated additions), so no pass leans on the narrow FP64
+// pipe.  Each field's elements are cut into kLbChunks fixed chunks; a chunk
+// is always handled by one CTA (the same in every round), its threads' sums
+// combined in a fixed order, and a field's chunk sums added in chunk order:
+// the result depends on neither the grid nor the other fields of the batch.
+constexpr int kLbChunks = 256;  // = threads per CTA: the final sum takes one chunk per thread
+constexpr int kLbMaxSlots = 16;
+constexpr int kLbMaxOps = 192;
+constexpr long long kLbSpin = 1LL << 24;  // polls of the grid barrier (x 64 ns sleep): ~1 s
 
-// x <- a x + c u with a = (ja >= 0 ? S[ja] : a0) (a = 0 does not read x) and
-// c = c0 + c1 S[i1] + c2 S[i2] (slots < 0 left out), then S[out] = scale (v . x)
-// when out >= 0, with scale = (js1 >= 0 ? S[js1] : sc0) (js2 >= 0 ? S[js2] : 1).
-template <typename TU, typename TV>
-struct PassArgs {
-  float* x;
-  const TU* u;
-  const TV* v;
-  long long n;
-  double a0;
-  int ja;
-  double c0, c1, c2;
-  int i1, i2;
-  double sc0;
-  int js1, js2, out;
+struct LbSlot {
+  double *x, *xt, *g, *gt;
+  float* d;
   double* S;
-  double* part;
-  unsigned* counter;
-  const float* h;  // when set: x <- (jh >= 0 ? S[jh] : 1) h * (a x + c u), element by element
-  int jh;
+  long long n;
+  int op0, nops;
+};
+struct LbBatch {
+  int nslots, maxops;
+  LbSlot slot[kLbMaxSlots];
+  LbOp op[kLbMaxOps];
 };
 
-template <typename TU, typename TV>
-__global__ void __launch_bounds__(kRedThreads) lbfgs_pass_kernel(const PassArgs<TU, TV> A) {
-  double c = A.c0;
-  if (A.i1 >= 0) c += A.c1 * A.S[A.i1];
-  if (A.i2 >= 0) c += A.c2 * A.S[A.i2];
-  const double a = A.ja >= 0 ? A.S[A.ja] : A.a0;
-  const float cf = (float)c, af = (float)a, hf = A.jh >= 0 ? (float)A.S[A.jh] : 1.f;
-  const bool rx = a != 0.0, dot = A.out >= 0;
-  Acc<DF> acc;
-  acc_zero(acc);
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  for (; i + 3 * stride < A.n; i += 4 * stride) {  // four elements' loads in flight
-    float xo[4], uo[4];
-    TV vo[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      xo[j] = rx ? A.x[i + j * stride] : 0.f;
-      uo[j] = as_f(A.u[i + j * stride]);
-      if (dot) vo[j] = A.v[i + j * stride];
-    }
-    float ho[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) ho[j] = A.h ? hf * A.h[i + j * stride] : 1.f;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const float xv = ho[j] * fmaf(cf, uo[j], af * xo[j]);
-      A.x[i + j * stride] = xv;
-      if (dot) acc_mac(acc, as_df(vo[j]), as_df(xv));
-    }
-  }
-  for (; i < A.n; i += stride) {
-    const float xv = (A.h ? hf * A.h[i] : 1.f) * fmaf(cf, as_f(A.u[i]), rx ? af * A.x[i] : 0.f);
-    A.x[i] = xv;
-    if (dot) acc_mac(acc, as_df(A.v[i]), as_df(xv));
-  }
-  if (!dot) return;
-  DF r[1] = {acc_get(acc)};
-  double* S = A.S;
-  const int out = A.out, js1 = A.js1, js2 = A.js2;
-  const double sc0 = A.sc0;
-  grid_reduce_df<1>(r, A.part, A.counter, [S, out, js1, js2, sc0](const double* t) {
-    const double scale = (js1 >= 0 ? S[js1] : sc0) * (js2 >= 0 ? S[js2] : 1.0);
-    S[out] = scale * t[0];
-  });
+__device__ __forceinline__ DF as_df(float a) { return DF(a, 0.f); }
+__device__ __forceinline__ DF as_df(double a) { return df_from_double_bits(a); }
+__device__ __forceinline__ float as_f(double a) { return df_from_double_bits(a).hi; }  // nearest float
+__device__ __forceinline__ float ldu(const void* p, int is64, long long i) {
+  return is64 ? as_f(static_cast<const double*>(p)[i]) : static_cast<const float*>(p)[i];
+}
+__device__ __forceinline__ DF ldv(const void* p, int is64, long long i) {
+  return is64 ? as_df(static_cast<const double*>(p)[i]) : as_df(static_cast<const float*>(p)[i]);
 }
 
-// xn = x + t d (one FP64 FMA per element; d widened exactly from its bits)
-__global__ void __launch_bounds__(256) step_kernel(double* __restrict__ xn, const double* __restrict__ x,
-                                                   const float* __restrict__ d, double t, long long n) {
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x)
-    xn[i] = fma(t, f2d_bits(d[i]), x[i]);
+// Grid barrier of a cooperative launch: bar[0] arrivals, bar[1] generation,
+// bar[2] abort.  The last of `expected` arrivals resets the count and
+// advances the generation; the others poll it with a bounded wait.  A wait
+// that runs out (or finds abort raised) raises abort and returns false.
+__device__ bool lb_grid_sync(unsigned* bar, unsigned expected) {
+  __shared__ int okb;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned* vb = bar;
+    int ok = vb[2] == 0u;
+    if (ok) {
+      const unsigned g0 = vb[1];
+      __threadfence();
+      if (atomicAdd(&bar[0], 1u) == expected - 1u) {
+        vb[0] = 0u;
+        __threadfence();
+        atomicAdd(&bar[1], 1u);
+      } else {
+        for (long long i = 0; vb[1] == g0; ++i) {
+          if (vb[2] != 0u || i > kLbSpin) {
+            ok = 0;
+            break;
+          }
+          __nanosleep(64);
+        }
+      }
+      __threadfence();
+    }
+    if (!ok) vb[2] = 1u;
+    okb = ok;
+  }
+  __syncthreads();
+  return okb != 0;
 }
 
-// s = t d, y = gn - g (rounded to FP32); S[o] = s . y, S[o + 1] = y . H0 y with
-// the diagonal H0 = h (y . y without one), S[orho] = 1 / (s . y) and
-// S[ogam] = (s . y) / (y . H0 y) when s . y > 1e-12 y . H0 y, else S[orho] = 0
-// (the pair then drops out of the recursion) and gamma stays
-__global__ void __launch_bounds__(kRedThreads)
-pair_kernel(float* __restrict__ s, float* __restrict__ y, const float* __restrict__ d,
-            const double* __restrict__ gn, const double* __restrict__ g, const float* __restrict__ h, double t,
-            long long n, double* S, int o, int orho, int ogam, double* part, unsigned* counter) {
-  const float tf = (float)t;
-  Acc<DF> sy, yy;
-  acc_zero(sy);
-  acc_zero(yy);
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  auto one = [&](long long k, float dv, double gnv, double gv) {
-    const float sv = tf * dv;
-    const float yv = (df_from_double_bits(gnv) - df_from_double_bits(gv)).hi;
-    s[k] = sv;
-    y[k] = yv;
-    acc_mac(sy, as_df(sv), as_df(yv));
-    acc_mac(yy, as_df(h ? h[k] * yv : yv), as_df(yv));
-  };
-  for (; i + 3 * stride < n; i += 4 * stride) {  // four elements' loads in flight
-    float dv[4];
-    double gnv[4], gv[4];
+// block sum of K double-float values (warps by shuffles, warp 0 over the
+// warps), valid in thread 0
+template <int K>
+__device__ __forceinline__ void lb_block_sum(DF (&v)[K]) {
+  __shared__ float2 sh[K][kRedThreads / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  df_warp_sum<K>(v);
+  __syncthreads();
+  if (lane == 0)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      dv[j] = d[i + j * stride];
-      gnv[j] = gn[i + j * stride];
-      gv[j] = g[i + j * stride];
+    for (int k = 0; k < K; ++k) sh[k][wid] = make_float2(v[k].hi, v[k].lo);
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const float2 q = lane < kRedThreads / 32 ? sh[k][lane] : make_float2(0.f, 0.f);
+      v[k] = DF(q.x, q.y);
     }
-#pragma unroll
-    for (int j = 0; j < 4; ++j) one(i + j * stride, dv[j], gnv[j], gv[j]);
+    df_warp_sum<K>(v);
   }
-  for (; i < n; i += stride) one(i, d[i], gn[i], g[i]);
-  DF r[2] = {acc_get(sy), acc_get(yy)};
-  grid_reduce_df<2>(r, part, counter, [S, o, orho, ogam](const double* t2) {
-    const double sy = t2[0], yy = t2[1];
-    S[o] = sy;
-    S[o + 1] = yy;
-    const bool ok = yy > 0.0 && sy > 1e-12 * yy;
-    S[orho] = ok ? 1.0 / sy : 0.0;
-    if (ok) S[ogam] = sy / yy;
-  });
+}
+
+__device__ __forceinline__ int lb_dots(const LbOp& op) {
+  return op.type == kOpPair ? 2 : (op.type == kOpPass && op.out >= 0 ? 1 : 0);
+}
+
+__global__ void __launch_bounds__(kRedThreads) lbfgs_batch_kernel(const __grid_constant__ LbBatch B,
+                                                                   float2* __restrict__ part, unsigned* bar,
+                                                                   int* err, int* flag) {
+  const int tid = threadIdx.x;
+  const long long items = (long long)B.nslots * kLbChunks;
+  bool ok = true;
+  for (int r = 0; r < B.maxops && ok; ++r) {
+    bool any_dot = false;
+    for (int j = 0; j < B.nslots; ++j)
+      if (r < B.slot[j].nops && lb_dots(B.op[B.slot[j].op0 + r])) any_dot = true;
+    // ---- element phase: chunk c of field j, every element once ----
+    for (long long it = blockIdx.x; it < items; it += gridDim.x) {
+      const int j = (int)(it / kLbChunks), c = (int)(it % kLbChunks);
+      const LbSlot& sl = B.slot[j];
+      if (r >= sl.nops) continue;
+      const LbOp& op = B.op[sl.op0 + r];
+      const long long len = (sl.n + kLbChunks - 1) / kLbChunks;
+      const long long i0 = (long long)c * len, i1 = min(sl.n, i0 + len);
+      Acc<DF> a0, a1;
+      acc_zero(a0);
+      acc_zero(a1);
+      const double* S = sl.S;
+      if (op.type == kOpPass) {
+        double cc = op.c0;
+        if (op.i1 >= 0) cc += op.c1 * __ldcg(S + op.i1);
+        if (op.i2 >= 0) cc += op.c2 * __ldcg(S + op.i2);
+        const double a = op.ja >= 0 ? __ldcg(S + op.ja) : op.a0;
+        const float cf = (float)cc, af = (float)a, hf = op.jh >= 0 ? (float)__ldcg(S + op.jh) : 1.f;
+        const bool rx = a != 0.0, dot = op.out >= 0;
+        float* __restrict__ x = op.f0;
+        long long i = i0 + tid;
+        for (; i + 3 * kRedThreads < i1; i += 4 * kRedThreads) {  // four elements' loads in flight
+          float xo[4], uo[4], ho[4];
+          DF vo[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const long long e = i + q * kRedThreads;
+            xo[q] = rx ? x[e] : 0.f;
+            uo[q] = ldu(op.u, op.u64, e);
+            ho[q] = op.h ? hf * op.h[e] : 1.f;
+            if (dot) vo[q] = ldv(op.v, op.v64, e);
+          }
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const float xv = ho[q] * fmaf(cf, uo[q], af * xo[q]);
+            x[i + q * kRedThreads] = xv;
+            if (dot) acc_mac(a0, vo[q], as_df(xv));
+          }
+        }
+        for (; i < i1; i += kRedThreads) {
+          const float xv = (op.h ? hf * op.h[i] : 1.f) * fmaf(cf, ldu(op.u, op.u64, i), rx ? af * x[i] : 0.f);
+          x[i] = xv;
+          if (dot) acc_mac(a0, ldv(op.v, op.v64, i), as_df(xv));
+        }
+      } else if (op.type == kOpPair) {
+        const float tf = (float)op.t;
+        for (long long i = i0 + tid; i < i1; i += kRedThreads) {
+          const double gn = sl.gt[i], go = sl.g[i];
+          const float sv = tf * sl.d[i];
+          const float yv = (df_from_double_bits(gn) - df_from_double_bits(go)).hi;
+          op.f0[i] = sv;
+          op.f1[i] = yv;
+          acc_mac(a0, as_df(sv), as_df(yv));
+          acc_mac(a1, as_df(op.h ? op.h[i] * yv : yv), as_df(yv));
+          sl.g[i] = gn;  // the accepted point
+          sl.x[i] = sl.xt[i];
+        }
+      } else if (op.type == kOpCopy) {
+        for (long long i = i0 + tid; i < i1; i += kRedThreads) {
+          sl.g[i] = sl.gt[i];
+          sl.x[i] = sl.xt[i];
+        }
+      } else {  // kOpStep: one FP64 FMA per element, d widened exactly from its bits
+        for (long long i = i0 + tid; i < i1; i += kRedThreads) sl.xt[i] = fma(op.t, f2d_bits(sl.d[i]), sl.x[i]);
+      }
+      const int nd = lb_dots(op);
+      if (nd) {
+        DF v[2] = {acc_get(a0), acc_get(a1)};
+        lb_block_sum<2>(v);
+        if (tid == 0) {
+          part[(it)*2] = make_float2(v[0].hi, v[0].lo);
+          part[(it)*2 + 1] = make_float2(v[1].hi, v[1].lo);
+        }
+      }
+    }
+    if (!lb_grid_sync(bar, gridDim.x)) {
+      ok = false;
+      break;
+    }
+    if (!any_dot) continue;
+    // ---- sums: field j's chunk sums in chunk order, one CTA per field ----
+    for (int j = blockIdx.x; j < B.nslots; j += gridDim.x) {
+      const LbSlot& sl = B.slot[j];
+      if (r >= sl.nops) continue;
+      const LbOp& op = B.op[sl.op0 + r];
+      if (!lb_dots(op)) continue;
+      const float2 q0 = __ldcg(&part[((long long)j * kLbChunks + tid) * 2]);
+      const float2 q1 = __ldcg(&part[((long long)j * kLbChunks + tid) * 2 + 1]);
+      DF v[2] = {DF(q0.x, q0.y), DF(q1.x, q1.y)};
+      lb_block_sum<2>(v);
+      if (tid == 0) {
+        double* S = sl.S;
+        const double t0 = df_to_double(v[0]), t1 = df_to_double(v[1]);
+        if (op.type == kOpPass) {
+          const double scale = (op.js1 >= 0 ? S[op.js1] : op.sc0) * (op.js2 >= 0 ? S[op.js2] : 1.0);
+          S[op.out] = scale * t0;
+        } else {
+          S[op.out] = t0;
+          S[op.out + 1] = t1;
+          const bool good = t1 > 0.0 && t0 > 1e-12 * t1;
+          S[op.i1] = good ? 1.0 / t0 : 0.0;
+          if (good) S[op.i2] = t0 / t1;
+        }
+        __threadfence();
+      }
+    }
+    if (!lb_grid_sync(bar, gridDim.x)) {
+      ok = false;
+      break;
+    }
+  }
+  if (!ok && blockIdx.x == 0 && tid == 0) note_wait_timeout(err, flag);
+}
+
+__global__ void __launch_bounds__(kRedThreads) grid_barrier_selftest_kernel(unsigned* bar, unsigned missing,
+                                                                            int* err, int* flag) {
+  if (!lb_grid_sync(bar, gridDim.x + missing) && blockIdx.x == 0 && threadIdx.x == 0) note_wait_timeout(err, flag);
 }
 
 // a field's scalar block at the start of a run: zero, gamma = 1
@@ -864,14 +958,29 @@ void Lbfgs::bind(const Bufs& b, long long n, int m) {
   m_ = m;
 }
 
-template <typename TU, typename TV>
-void Lbfgs::pass(float* x, const TU* u, const TV* v, double a0, int ja, double c1, int i1, double c2, int i2,
-                 double sc0, int js1, int js2, int out, cudaStream_t s, const float* h, int jh) {
-  double* part = static_cast<double*>(b_.scratch);
-  PassArgs<TU, TV> A{x,  u,   v,   n_,  a0,  ja,   0.0,  c1,   c2,  i1,  i2,
-                     sc0, js1, js2, out, b_.S, part, reinterpret_cast<unsigned*>(part + kRedBlocks * 7), h, jh};
-  lbfgs_pass_kernel<TU, TV><<<red_blocks(n_), kRedThreads, 0, s>>>(A);
-  launch_ok("L-BFGS pass launch");
+void Lbfgs::pass(float* x, const void* u, int u64, const void* v, int v64, double a0, int ja, double c0, double c1,
+                 int i1, double c2, int i2, double sc0, int js1, int js2, int out, const float* h, int jh) {
+  LbOp o{};
+  o.type = kOpPass;
+  o.f0 = x;
+  o.u = u;
+  o.u64 = u64;
+  o.v = v;
+  o.v64 = v64;
+  o.a0 = a0;
+  o.ja = ja;
+  o.c0 = c0;
+  o.c1 = c1;
+  o.i1 = i1;
+  o.c2 = c2;
+  o.i2 = i2;
+  o.sc0 = sc0;
+  o.js1 = js1;
+  o.js2 = js2;
+  o.out = out;
+  o.h = h;
+  o.jh = jh;
+  ops_.push_back(o);
 }
 
 // d = -H g by the two-loop recursion over the nh_ stored pairs, with the
@@ -880,50 +989,45 @@ void Lbfgs::pass(float* x, const TU* u, const TV* v, double a0, int ja, double c
 // (y . P y) of the newest pair (P alone before the first pair); S[gd] = g . d.  Every coefficient
 // comes from the device scalars: alpha_i = rho_i (s_i . q), beta_i =
 // rho_i (y_i . r).
-void Lbfgs::direction(cudaStream_t s) {
+void Lbfgs::direction() {
   float* d = b_.d;
   const double* g = b_.g;
   const float* h0 = b_.hinv;
   auto hs = [&](int i) { return b_.hs + (size_t)i * n_; };
   auto hy = [&](int i) { return b_.hy + (size_t)i * n_; };
-  // x <- [h0 *] (-g), dot with v
-  auto neg_g = [&](const auto* v, double sc0, int js1, int out, const float* h) {
-    double* part = static_cast<double*>(b_.scratch);
-    using TV = std::remove_const_t<std::remove_pointer_t<decltype(v)>>;
-    PassArgs<double, TV> A{d,   g,   v,  n_,  0.0,  -1,   -1.0, 0.0, 0.0, -1, -1,
-                           sc0, js1, -1, out, b_.S, part, reinterpret_cast<unsigned*>(part + kRedBlocks * 7), h, -1};
-    lbfgs_pass_kernel<double, TV><<<red_blocks(n_), kRedThreads, 0, s>>>(A);
-    launch_ok("L-BFGS pass launch");
-  };
-  if (nh_ == 0) {
-    neg_g(g, 1.0, -1, gd(), h0);
+  if (nh_ == 0) {  // d = h0 (-g); S[gd] = g . d
+    pass(d, g, 1, g, 1, 0.0, -1, -1.0, 0.0, -1, 0.0, -1, 1.0, -1, -1, gd(), h0);
     return;
   }
   auto idx = [&](int j) { return ((head_ - 1 - j) % m_ + m_) % m_; };  // j = 0: newest
-  neg_g(hs(idx(0)), 0.0, rho(idx(0)), alpha(idx(0)), nullptr);  // q = -g; alpha_newest = rho (s . q)
+  // q = -g; alpha_newest = rho (s . q)
+  pass(d, g, 1, hs(idx(0)), 0, 0.0, -1, -1.0, 0.0, -1, 0.0, -1, 0.0, rho(idx(0)), -1, alpha(idx(0)));
   for (int j = 0; j < nh_; ++j) {
     const int i = idx(j);
     if (j + 1 < nh_) {  // q -= alpha_i y_i; alpha_next = rho_next (s_next . q)
       const int nx = idx(j + 1);
-      pass(d, hy(i), hs(nx), 1.0, -1, -1.0, alpha(i), 0.0, -1, 0.0, rho(nx), -1, alpha(nx), s);
+      pass(d, hy(i), 0, hs(nx), 0, 1.0, -1, 0.0, -1.0, alpha(i), 0.0, -1, 0.0, rho(nx), -1, alpha(nx));
     } else {  // last: r = gamma h0 (q - alpha y); beta_oldest = rho_oldest (y_oldest . r)
-      pass(d, hy(i), hy(i), 1.0, -1, -1.0, alpha(i), 0.0, -1, 0.0, rho(i), -1, beta(0), s, h0, gamma());
+      pass(d, hy(i), 0, hy(i), 0, 1.0, -1, 0.0, -1.0, alpha(i), 0.0, -1, 0.0, rho(i), -1, beta(0), h0, gamma());
     }
   }
   for (int j = 0; j < nh_; ++j) {  // oldest first: r += (alpha_i - beta_i) s_i
     const int i = idx(nh_ - 1 - j);
     if (j + 1 < nh_) {
       const int nx = idx(nh_ - 2 - j);
-      pass(d, hs(i), hy(nx), 1.0, -1, 1.0, alpha(i), -1.0, beta(j), 0.0, rho(nx), -1, beta(j + 1), s);
+      pass(d, hs(i), 0, hy(nx), 0, 1.0, -1, 0.0, 1.0, alpha(i), -1.0, beta(j), 0.0, rho(nx), -1, beta(j + 1));
     } else {
-      pass(d, hs(i), g, 1.0, -1, 1.0, alpha(i), -1.0, beta(j), 1.0, -1, -1, gd(), s);
+      pass(d, hs(i), 0, g, 1, 1.0, -1, 0.0, 1.0, alpha(i), -1.0, beta(j), 1.0, -1, -1, gd());
     }
   }
 }
 
-void Lbfgs::step(cudaStream_t s) {
-  step_kernel<<<stream_blocks(n_), 256, 0, s>>>(b_.xt, b_.x, b_.d, t_, n_);
-  launch_ok("step kernel launch");
+void Lbfgs::step() {
+  LbOp o{};
+  o.type = kOpStep;
+  o.t = t_;
+  o.out = -1;
+  ops_.push_back(o);
 }
 
 void Lbfgs::start(double gtol, double ftol, int max_iter, cudaStream_t s) {
@@ -938,18 +1042,19 @@ void Lbfgs::start(double gtol, double ftol, int max_iter, cudaStream_t s) {
   launch_ok("L-BFGS init launch");
 }
 
-bool Lbfgs::on_eval(const double* tail, cudaStream_t s) {
+bool Lbfgs::on_eval(const double* tail) {
   const double c1 = 1e-4;
   const int max_ls = 40;
   const double gdv = tail[0];
   const double* Et = tail + 3;
+  ops_.clear();
   if (!first_) {
     if (!(gdv < 0.0)) {  // not a descent direction (rounding): restart from -H0 g
       nh_ = 0;
-      direction(s);
+      direction();
       t_ = 1.0;
       ls_ = 0;
-      step(s);
+      step();
       return false;
     }
     if (!(std::isfinite(Et[0]) && Et[0] <= E_[0] + c1 * t_ * gdv)) {
@@ -958,43 +1063,138 @@ bool Lbfgs::on_eval(const double* tail, cudaStream_t s) {
         status_ = kStalled;
         return true;
       }
-      step(s);
+      step();
       return false;
     }
-    // accepted: curvature pair into the ring slot head_
-    pair_kernel<<<red_blocks(n_), kRedThreads, 0, s>>>(
-        b_.hs + (size_t)head_ * n_, b_.hy + (size_t)head_ * n_, b_.d, b_.gt, b_.g, b_.hinv, t_, n_, b_.S, gd() + 1,
-        rho(head_), gamma(), static_cast<double*>(b_.scratch),
-        reinterpret_cast<unsigned*>(static_cast<double*>(b_.scratch) + kRedBlocks * 7));
-    launch_ok("pair kernel launch");
-    head_ = (head_ + 1) % m_;
-    nh_ = std::min(nh_ + 1, m_);
-    ++iter_;
   }
   const double Eprev = E_[0];
   std::copy(Et, Et + 5, E_);
   trace_.insert(trace_.end(), Et, Et + 5);
-  cuda_check(cudaMemcpyAsync(b_.x, b_.xt, sizeof(double) * (size_t)n_, cudaMemcpyDeviceToDevice, s), "iterate copy");
-  cuda_check(cudaMemcpyAsync(b_.g, b_.gt, sizeof(double) * (size_t)n_, cudaMemcpyDeviceToDevice, s),
-             "gradient copy");
+  if (!first_) {
+    // accepted: curvature pair into the ring slot head_, the point kept
+    LbOp o{};
+    o.type = kOpPair;
+    o.f0 = b_.hs + (size_t)head_ * n_;
+    o.f1 = b_.hy + (size_t)head_ * n_;
+    o.h = b_.hinv;
+    o.t = t_;
+    o.out = gd() + 1;
+    o.i1 = rho(head_);
+    o.i2 = gamma();
+    ops_.push_back(o);
+    head_ = (head_ + 1) % m_;
+    nh_ = std::min(nh_ + 1, m_);
+    ++iter_;
+  } else {
+    LbOp o{};
+    o.type = kOpCopy;
+    o.out = -1;
+    ops_.push_back(o);
+  }
+  bool done = false;
   if (E_[4] <= gtol_) {
     status_ = kConverged;
-    return true;
-  }
-  if (!first_ && std::fabs(Eprev - E_[0]) <= ftol_ * std::max(1.0, std::fabs(E_[0]))) {
+    done = true;
+  } else if (!first_ && std::fabs(Eprev - E_[0]) <= ftol_ * std::max(1.0, std::fabs(E_[0]))) {
     status_ = kFlat;
-    return true;
-  }
-  if (iter_ >= max_iter_) {
+    done = true;
+  } else if (iter_ >= max_iter_) {
     status_ = kMaxIter;
-    return true;
+    done = true;
   }
-  direction(s);
+  if (done) return true;  // the accepted point still has to be kept: the caller runs ops()
+  direction();
   t_ = 1.0;  // the diagonal preconditioner scales even the first step
   first_ = false;
   ls_ = 0;
-  step(s);
+  step();
   return false;
+}
+
+void LbRunner::init() {
+  const size_t part = sizeof(float2) * 2 * (size_t)kLbMaxSlots * kLbChunks;
+  buf.alloc(part + 64);
+  cuda_check(cudaMemset(buf.ptr, 0, part + 64), "L-BFGS batch state reset");
+  int dev = 0, nsm = 0, per = 0, coop = 0;
+  cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  cuda_check(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev), "cooperative launch attribute");
+  throw_if(!coop, "the device does not support cooperative launches", 4);
+  cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "SM count");
+  cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lbfgs_batch_kernel, kRedThreads, 0),
+             "L-BFGS batch occupancy");
+  throw_if(per < 1, "internal: the L-BFGS batch kernel does not fit an SM", 4);
+  // two CTAs per SM at most: enough loads in flight, and room left for the
+  // other groups' kernels while the batch waits at its barriers
+  blocks = nsm * std::min(per, 2);
+}
+
+namespace {
+void lb_launch(const LbBatch& B, LbRunner& r, cudaStream_t s) {
+  const size_t part = sizeof(float2) * 2 * (size_t)kLbMaxSlots * kLbChunks;
+  unsigned* bar = reinterpret_cast<unsigned*>(static_cast<unsigned char*>(r.buf.ptr) + part);
+  cuda_check(cudaMemsetAsync(bar, 0, 16, s), "grid barrier reset");
+  const WaitStatus& w = device_wait_status();
+  float2* pp = static_cast<float2*>(r.buf.ptr);
+  int* err = w.count;
+  int* flag = w.flag_dev;
+  void* args[] = {const_cast<LbBatch*>(&B), &pp, &bar, &err, &flag};
+  clear_stale_error();
+  cuda_check(cudaLaunchCooperativeKernel((const void*)lbfgs_batch_kernel, dim3(r.blocks), dim3(kRedThreads), args,
+                                         0, s),
+             "L-BFGS batch launch");
+}
+}  // namespace
+
+void lbfgs_run(Lbfgs* const* lbs, int k, LbRunner& r, cudaStream_t s) {
+  if (!r.buf.ptr) r.init();
+  LbBatch B;
+  B.nslots = 0;
+  B.maxops = 0;
+  int nop = 0;
+  auto flush = [&] {
+    if (B.nslots) lb_launch(B, r, s);
+    B.nslots = 0;
+    B.maxops = 0;
+    nop = 0;
+  };
+  for (int i = 0; i < k; ++i) {
+    std::vector<LbOp>& ops = lbs[i]->ops();
+    if (ops.empty()) continue;
+    throw_if((int)ops.size() > kLbMaxOps, "internal: L-BFGS program too long", 4);
+    if (B.nslots == kLbMaxSlots || nop + (int)ops.size() > kLbMaxOps) flush();
+    const Lbfgs::Bufs& b = lbs[i]->bufs();
+    LbSlot& sl = B.slot[B.nslots++];
+    sl.x = b.x;
+    sl.xt = b.xt;
+    sl.g = b.g;
+    sl.gt = b.gt;
+    sl.d = b.d;
+    sl.S = b.S;
+    sl.n = lbs[i]->size();
+    sl.op0 = nop;
+    sl.nops = (int)ops.size();
+    for (const LbOp& o : ops) B.op[nop++] = o;
+    B.maxops = std::max(B.maxops, sl.nops);
+    ops.clear();
+  }
+  flush();
+}
+
+void grid_barrier_selftest(int missing, LbRunner& r, cudaStream_t s) {
+  throw_if(missing < 0 || missing > 1024, "missing arrivals must be in [0, 1024]");
+  if (!r.buf.ptr) r.init();
+  const size_t part = sizeof(float2) * 2 * (size_t)kLbMaxSlots * kLbChunks;
+  unsigned* bar = reinterpret_cast<unsigned*>(static_cast<unsigned char*>(r.buf.ptr) + part);
+  cuda_check(cudaMemsetAsync(bar, 0, 16, s), "grid barrier reset");
+  const WaitStatus& w = device_wait_status();
+  unsigned miss = (unsigned)missing;
+  int* err = w.count;
+  int* flag = w.flag_dev;
+  void* args[] = {&bar, &miss, &err, &flag};
+  clear_stale_error();
+  cuda_check(cudaLaunchCooperativeKernel((const void*)grid_barrier_selftest_kernel, dim3(r.blocks),
+                                         dim3(kRedThreads), args, 0, s),
+             "grid barrier self-test launch");
 }
 
 }  // namespace mdft
@@ -1010,6 +1210,7 @@ struct mdft_solver_s {
   bool has_vext = false;
   DevBuf vext, w, p, vexc, xf, x, xt, g, gt, d, hs, hy, hinv, S, scratch;
   mdft::Lbfgs lb;
+  mdft::LbRunner lbr;
 };
 
 namespace {
@@ -1131,6 +1332,7 @@ int mdft_solver_minimize(mdft_solver_t h, double* xi, int max_iter, double gtol,
     throw_if(!h || !xi, "NULL argument");
     throw_if(max_iter < 0, "max_iter must be >= 0");
     throw_if(mdft::detail::current_device() != h->device, "the solver belongs to another device");
+    mdft::check_device_waits();
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const size_t fb = sizeof(double) * (size_t)h->n;
     cuda_check(cudaMemcpyAsync(h->xt.ptr, xi, fb, cudaMemcpyDeviceToDevice, s), "start copy");
@@ -1143,7 +1345,10 @@ int mdft_solver_minimize(mdft_solver_t h, double* xi, int max_iter, double gtol,
       cuda_check(cudaMemcpyAsync(tail, Sd + mdft::Lbfgs::tail_at(m), sizeof tail, cudaMemcpyDeviceToHost, s),
                  "tail read-back");
       cuda_check(cudaStreamSynchronize(s), "solver stream");
-      if (h->lb.on_eval(tail, s)) break;
+      const bool done = h->lb.on_eval(tail);
+      mdft::Lbfgs* one = &h->lb;
+      mdft::lbfgs_run(&one, 1, h->lbr, s);
+      if (done) break;
     }
     cuda_check(cudaMemcpyAsync(xi, h->x.ptr, fb, cudaMemcpyDeviceToDevice, s), "final iterate copy");
     cuda_check(cudaStreamSynchronize(s), "solver stream");
@@ -1156,6 +1361,19 @@ int mdft_solver_minimize(mdft_solver_t h, double* xi, int max_iter, double gtol,
 int mdft_solver_destroy(mdft_solver_t h) {
   delete h;
   return MDFT_OK;
+}
+
+int mdft_grid_barrier_selftest(int missing, void* stream) {
+  return solver_guard([&] {
+    static std::mutex mu;
+    static std::map<int, std::unique_ptr<mdft::LbRunner>> runners;
+    int dev = 0;
+    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    std::lock_guard<std::mutex> lk(mu);
+    auto& r = runners[dev];
+    if (!r) r = std::make_unique<mdft::LbRunner>();
+    mdft::grid_barrier_selftest(missing, *r, static_cast<cudaStream_t>(stream));
+  });
 }
 
 }  // extern "C"

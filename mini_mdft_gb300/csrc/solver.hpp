@@ -32,6 +32,48 @@ size_t reduction_scratch_bytes();
 // xi (double) -> float copy of n values
 void to_float(float* y, const double* x, long long n, cudaStream_t s);
 
+// One vector operation of a field's L-BFGS step (built on the host by
+// Lbfgs::on_eval, run for every field of a batch by lbfgs_run):
+//   kOpPass: x <- [hs h] (a x + c u), then S[out] = scale (v . x), with
+//     a = (ja >= 0 ? S[ja] : a0), c = c0 + c1 S[i1] + c2 S[i2] (slots < 0 left
+//     out), hs = (jh >= 0 ? S[jh] : 1), scale = (js1 >= 0 ? S[js1] : sc0)
+//     (js2 >= 0 ? S[js2] : 1); u and v are FP64 (u64, v64) or FP32 vectors;
+//   kOpPair: the curvature pair s = t d, y = gt - g (FP32, into f0 / f1),
+//     S[out] = s . y, S[out + 1] = y . h y, S[i1] = rho, S[i2] = gamma (when
+//     s . y > 1e-12 y . h y, else rho = 0), and the accepted point kept
+//     (x <- xt, g <- gt);
+//   kOpCopy: x <- xt, g <- gt;
+//   kOpStep: xt <- x + t d.
+enum { kOpPass = 0, kOpPair = 1, kOpCopy = 2, kOpStep = 3 };
+struct LbOp {
+  int type, ja, i1, i2, js1, js2, out, jh, u64, v64;
+  double a0, c0, c1, c2, sc0, t;
+  float* f0;
+  float* f1;
+  const void* u;
+  const void* v;
+  const float* h;
+};
+
+// Device state of a batch launch: the partial sums and the grid barrier.
+class Lbfgs;
+struct LbRunner {
+  DevBuf buf;  // partial sums, then the barrier words (count, generation, abort)
+  int blocks = 0;
+  void init();  // on the current device, outside stream capture
+};
+// Runs the queued operations of k fields' minimisers (on_eval since their
+// last run) in one persistent, cooperatively launched kernel: every field's
+// operations in order, grid-wide sums between them behind a bounded grid
+// barrier.  Each field's sums follow a fixed partition of its elements, so a
+// field gets the same results alone and in any batch.  A barrier that runs
+// out counts as a timed-out device wait (check_device_waits).
+void lbfgs_run(Lbfgs* const* lbs, int k, LbRunner& r, cudaStream_t s);
+// One cooperative launch whose blocks meet at the batch kernel's grid
+// barrier, expecting `missing` more arrivals than there are blocks: with
+// missing > 0 the barrier runs out and is recorded as a timed-out wait.
+void grid_barrier_selftest(int missing, LbRunner& r, cudaStream_t s);
+
 // L-BFGS (two-loop recursion with a diagonal initial inverse Hessian, the
 // inverse local curvature; Armijo backtracking) of one field.  The host
 // keeps only the line-search bookkeeping; every scalar of the recursion
@@ -40,8 +82,8 @@ void to_float(float* y, const double* x, long long n, cudaStream_t s);
 // rho = 0 (it then drops out of the recursion), so the host never waits for
 // a dot product.  After each evaluation of E and its gradient at xt the
 // caller reads back the block's tail (tail_at(m), 8 doubles: g.d, s.y, y.y,
-// the 5 energy terms) and calls on_eval, which launches the next trial point
-// into xt.
+// the 5 energy terms) and calls on_eval, which queues the vector operations
+// that form the next trial point in xt; lbfgs_run runs them.
 class Lbfgs {
  public:
   struct Bufs {
@@ -65,20 +107,24 @@ class Lbfgs {
   void bind(const Bufs& b, long long n, int m);
   // a new run from the point in xt: resets the scalars and the history
   void start(double gtol, double ftol, int max_iter, cudaStream_t s);
-  // the evaluation at xt is done: accept or backtrack, and launch the next
-  // trial point into xt; true when the run has ended
-  bool on_eval(const double* tail, cudaStream_t s);
+  // the evaluation at xt is done: accept or backtrack, and queue the
+  // operations of the next trial point into xt; true when the run has ended.
+  // The caller runs ops() (lbfgs_run) after every call: when the run ends at
+  // an accepted point they still keep that point in x.
+  bool on_eval(const double* tail);
+  long long size() const { return n_; }
+  std::vector<LbOp>& ops() { return ops_; }
   int iterations() const { return iter_; }
   Status status() const { return status_; }
   const std::vector<double>& trace() const { return trace_; }  // 5 terms per accepted iterate
   const Bufs& bufs() const { return b_; }
 
  private:
-  void direction(cudaStream_t s);
-  void step(cudaStream_t s);
-  template <typename TU, typename TV>
-  void pass(float* x, const TU* u, const TV* v, double a0, int ja, double c1, int i1, double c2, int i2, double sc0,
-            int js1, int js2, int out, cudaStream_t s, const float* h = nullptr, int jh = -1);
+  void direction();
+  void step();
+  void pass(float* x, const void* u, int u64, const void* v, int v64, double a0, int ja, double c0, double c1,
+            int i1, double c2, int i2, double sc0, int js1, int js2, int out, const float* h = nullptr,
+            int jh = -1);
   int alpha(int i) const { return i; }
   int rho(int i) const { return m_ + i; }
   int gamma() const { return 2 * m_; }
@@ -94,6 +140,7 @@ class Lbfgs {
   double E_[5] = {0, 0, 0, 0, 0};
   Status status_ = kRunning;
   std::vector<double> trace_;
+  std::vector<LbOp> ops_;
 };
 
 }  // namespace mdft

@@ -38,3 +38,30 @@ def test_timed_out_wait_fails_the_next_call_once(gpu_lib):
     conv.execute(q)
     torch.cuda.synchronize()
     assert torch.equal(q, ref)
+
+
+def test_persistent_kernel_barrier_timeout_is_reported(gpu_lib):
+    """The grid barrier of the persistent L-BFGS kernel: with every block
+    present it passes; with one arrival missing every block gives up (bounded
+    poll), the timeout is counted, and the next convolution call returns
+    MDFT_ERR_TIMEOUT once."""
+    import torch
+    M = gpu_lib
+    n, box, mmax, mrso, dq = (16, 16, 16), (10., 10., 10.), 2, 2, 0.01
+    idx, tab = I.synthetic_cq(mmax, mrso, I.nq_for(n, box, dq), dq)
+    sg, ag = M.SpatialGrid(n, box), M.AngularGrid(mmax, mrso)
+    conv = M.Convolution.from_table(idx, tab, dq, sg, ag, precision="f64")
+    p = torch.zeros((ag.m_np,) + n, device="cuda", dtype=torch.complex128)
+    before = M.wait_timeouts()
+    M.grid_barrier_selftest(0)
+    torch.cuda.synchronize()
+    assert M.wait_timeouts() == before
+    conv.execute(p)
+    M.grid_barrier_selftest(1)
+    torch.cuda.synchronize()
+    assert M.wait_timeouts() == before + 1
+    with pytest.raises(M.MdftError) as e:
+        conv.execute(p)
+    assert e.value.code == 6
+    conv.execute(p)
+    torch.cuda.synchronize()
