@@ -60,10 +60,12 @@ def parse_args():
                     help="skip the 128^3 / mmax 5 solve and per-kernel table")
     ap.add_argument("--no-96", action="store_true",
                     help="skip the 96^3 / mmax 4 per-kernel table and accuracy check")
-    ap.add_argument("--mode", choices=["full", "steps", "energy"], default="full",
+    ap.add_argument("--serving-jobs", type=int, default=None,
+                    help="requests in the solute serving stream (default 256)")
+    ap.add_argument("--mode", choices=["full", "steps", "energy", "serving"], default="full",
                     help="steps: only W warm-up + K timed FP64 and FP32 round trips; energy: "
                          "get_delta_f and a short solute minimisation (short, fixed launch "
-                         "sequences for ncu captures)")
+                         "sequences for ncu captures); serving: only the two job-server legs")
     return ap.parse_args()
 
 
@@ -696,22 +698,34 @@ def serving_run(prec):
     }
 
 
-SERVING_SOLUTE = dict(shapes=[((32, 32, 32), (20.0, 20.0, 20.0), 0.6), ((48, 64, 80), (24.0, 30.0, 36.0), 0.2),
-                              ((64, 64, 64), (30.0, 30.0, 30.0), 0.2)],
-                      mmax=(1, 3), mrso=2, sites=(5, 41), jobs=24, rate_per_s=40.0, gtol=1e-5, max_iter=300,
-                      max_batch=8, dq=0.05, amplitude=CQ_AMPLITUDE)
+SERVING_SOLUTE = dict(shapes=[((32, 32, 32), (20.0, 20.0, 20.0), 0.25), ((48, 64, 80), (24.0, 30.0, 36.0), 0.25),
+                              ((64, 64, 64), (30.0, 30.0, 30.0), 0.25), ((96, 96, 96), (40.0, 40.0, 40.0), 0.25)],
+                      mmax=(1, 3), mrso=2, sites=(5, 41), jobs=256, rate_per_s=40.0, gtol=1e-5, max_iter=300,
+                      max_batch=8, hbm_budget_bytes=120 * 10 ** 9, dq=0.05, amplitude=CQ_AMPLITUDE,
+                      server_form="f32", serial_form="f64")
 
 
-def serving_solute_run(prec):
-    """Solvation jobs run to a gradient tolerance (max |dE/dxi| <= 1e-5):
-    SERVING_SOLUTE["jobs"] requests with Poisson arrivals at rate_per_s,
-    grids drawn from {32^3 / 20 A, 48x64x80 / 24x30x36 A, 64^3 / 30 A}, mmax
-    from {1, 3} (mrso 2), each with a seeded synthetic solute of 5-40 LJ +
-    charge sites, SPC/E water, isotropic c(q) = -3e-6 exp(-q^2).  The server
-    (per-job potential and L-BFGS state resident on the device, one batched
-    evaluation per step for same-shape jobs) against the same jobs solved one
-    at a time by the single-field minimiser (potential + minimisation timed,
-    handle creation not)."""
+def _pct(v, q):
+    v = sorted(v)
+    return v[min(len(v) - 1, int(q * len(v)))]
+
+
+def serving_solute_run(jobs_n=None):
+    """The solvation request stream: SERVING_SOLUTE["jobs"] requests with
+    Poisson arrivals at rate_per_s, grids drawn with equal weight from {32^3
+    / 20 A, 48x64x80 / 24x30x36 A, 64^3 / 30 A, 96^3 / 40 A}, mmax from {1,
+    3} (mrso 2), each with a seeded synthetic solute of 5-40 LJ + charge
+    sites in SPC/E water, isotropic c(q) = -3e-6 exp(-q^2), minimised to max
+    |dE/dxi| <= 1e-5.
+
+    The server runs the mixed form (FP32 fields, per-job potential and
+    L-BFGS state resident on the device, same-shape jobs batched into one
+    evaluation and one L-BFGS launch per step, HBM admission budget 120 GB).
+    Against it: the same jobs solved one at a time in the plain FP64 form by
+    the single-field minimiser, each job's service time (potential +
+    minimisation) measured on the device side of a synchronize; their p50/p99
+    latencies replay the same arrivals through a first-in-first-out queue of
+    those service times."""
     import threading
 
     import numpy as np
@@ -720,6 +734,7 @@ def serving_solute_run(prec):
     import mini_mdft_gb300 as M
     from mini_mdft_gb300 import inputs as I
     cfg = SERVING_SOLUTE
+    n_jobs = jobs_n or cfg["jobs"]
     mrso, dq = cfg["mrso"], cfg["dq"]
     rho0, pref = I.solvent_constants(I.SPCE_N0, mrso)
     kT = I.kT()
@@ -727,7 +742,7 @@ def serving_solute_run(prec):
     rng = np.random.default_rng(7)
     weights = np.array([w for _, _, w in cfg["shapes"]])
     jobs = []
-    for i in range(cfg["jobs"]):
+    for i in range(n_jobs):
         si = int(rng.choice(len(cfg["shapes"]), p=weights / weights.sum()))
         mmax = int(rng.choice(cfg["mmax"]))
         n_sites = int(rng.integers(*cfg["sites"]))
@@ -739,13 +754,16 @@ def serving_solute_run(prec):
         nq = max(I.nq_for(n, box, dq) for n, box, _ in cfg["shapes"]) + 2
         tables[mmax] = I.isotropic_cq(mmax, mrso, nq, dq, amplitude=cfg["amplitude"])
     solutes = [I.synthetic_solute(ns, cfg["shapes"][si][1], seed=seed) for si, _, ns, seed in jobs]
-    srv = M.Server(precision=prec, max_batch=cfg["max_batch"])
+
+    # ---- the server, mixed form
+    srv = M.Server(precision=cfg["server_form"], max_batch=cfg["max_batch"],
+                   hbm_budget_bytes=cfg["hbm_budget_bytes"])
     sid = {}
     for mmax in cfg["mmax"]:
         idx, tab = tables[mmax]
         sid[mmax] = srv.add_solvent(mmax, mrso, idx, tab, dq, rho0, pref)
         srv.set_solvent_model(sid[mmax], I.SPCE_SITES, kT, vmax)
-    for si, (n, box, _) in enumerate(cfg["shapes"]):  # warm-up: plans, arenas, graphs
+    for n, box, _ in cfg["shapes"]:  # warm-up: plans, arenas, graphs
         for mmax in cfg["mmax"]:
             srv.wait_solute(srv.submit_solute(sid[mmax], n, box, solutes[0][:2], max_iter=3, gtol=0.0))
     ids = [None] * len(jobs)
@@ -762,57 +780,83 @@ def serving_solute_run(prec):
     th = threading.Thread(target=submitter, args=(t0,))
     th.start()
     th.join()
-    lats, iters, status = [], 0, {}
+    lats, iters, status, e_srv = [], 0, {}, []
     for k in range(len(jobs)):
         _, trace, st, lat = srv.wait_solute(ids[k])
         lats.append(lat)
         iters += len(trace) - 1
         status[st] = status.get(st, 0) + 1
+        e_srv.append(float(trace[-1, 0]))
     wall = time.perf_counter() - t0
     stats = srv.stats()
     srv.close()
-    # the same jobs one at a time with the single-field minimiser
+    del srv
+    torch.cuda.empty_cache()
+
+    # ---- the same jobs one at a time, plain FP64, single-field minimiser
+    form = cfg["serial_form"]
     plans = {}
     for si, (n, box, _) in enumerate(cfg["shapes"]):
         for mmax in cfg["mmax"]:
             idx, tab = tables[mmax]
             sg, ag = M.SpatialGrid(n, box), M.AngularGrid(mmax, mrso)
-            plans[(si, mmax)] = (sg, ag, M.OrientationProjectionTransform(sg, ag, precision=prec),
-                                 M.Convolution.from_table(idx, tab, dq, sg, ag, precision=prec))
+            plans[(si, mmax)] = (sg, ag, M.OrientationProjectionTransform(sg, ag, precision=form),
+                                 M.Convolution.from_table(idx, tab, dq, sg, ag, precision=form))
     for (si, mmax), (sg, ag, opt, conv) in plans.items():  # warm-up, as for the server
         vext = M.solute_vext(sg, ag, I.SPCE_SITES, solutes[0][:2], vmax)
         M.Solver(opt, conv, vext, kT=kT, rho0=rho0, prefactor=pref, history=5).minimize(torch.ones_like(vext),
                                                                                            max_iter=3, gtol=0.0)
-    seq = 0.0
+    service, e_ser, iters_ser = [], [], 0
     for k, (si, mmax, _, _) in enumerate(jobs):
         sg, ag, opt, conv = plans[(si, mmax)]
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         vext = M.solute_vext(sg, ag, I.SPCE_SITES, solutes[k], vmax)
         torch.cuda.synchronize()
-        seq += time.perf_counter() - t1
+        s = time.perf_counter() - t1
         solver = M.Solver(opt, conv, vext, kT=kT, rho0=rho0, prefactor=pref, history=5)
         xi = torch.ones_like(vext)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        solver.minimize(xi, max_iter=cfg["max_iter"], gtol=cfg["gtol"])
+        trace = solver.minimize(xi, max_iter=cfg["max_iter"], gtol=cfg["gtol"])
         torch.cuda.synchronize()
-        seq += time.perf_counter() - t1
+        service.append(s + time.perf_counter() - t1)
+        e_ser.append(float(trace[-1, 0]))
+        iters_ser += len(trace) - 1
         del solver, vext, xi
-    lats.sort()
+    del plans
+    torch.cuda.empty_cache()
+    free, done, ser_lats = 0.0, 0.0, []
+    for k in range(len(jobs)):  # FIFO replay of the arrivals through the measured service times
+        start = max(arrivals[k], free)
+        free = start + service[k]
+        ser_lats.append(free - arrivals[k])
+    ser_span = free  # first arrival to last completion
+    rel = [abs(a - b) / abs(b) for a, b in zip(e_srv, e_ser)]
     names = {0: "gtol", 1: "flat", 2: "max_iter", 3: "no_decrease"}
+    shape_names = ["32^3/20 A", "48x64x80/24x30x36 A", "64^3/30 A", "96^3/40 A"]
     return {
         "metric": "served solute solves/s", "value": len(jobs) / wall, "unit": "solves/s",
-        "p50_ms": 1e3 * lats[len(lats) // 2], "p99_ms": 1e3 * lats[min(len(lats) - 1, int(0.99 * len(lats)))],
-        "jobs": len(jobs), "iterations": iters, "form": prec,
+        "p50_ms": 1e3 * _pct(lats, 0.5), "p99_ms": 1e3 * _pct(lats, 0.99),
+        "jobs": len(jobs), "iterations": iters, "form": cfg["server_form"],
         "ended_by": {names[k]: v for k, v in sorted(status.items())},
-        "workload": "%d solvation jobs, Poisson arrivals at %.0f/s; grids 32^3/20 A (60 %%), 48x64x80/24x30x36 A, "
-                    "64^3/30 A (20 %% each); mmax 1 or 3, mrso 2; 5-40 site synthetic solutes in SPC/E water; "
-                    "isotropic c(q) = -3e-6 exp(-q^2); L-BFGS to max |dE/dxi| <= %g (at most %d iterations); "
-                    "max_batch %d"
-                    % (len(jobs), cfg["rate_per_s"], cfg["gtol"], cfg["max_iter"], cfg["max_batch"]),
+        "workload": "%d solvation requests, Poisson arrivals at %.0f/s (last arrival at %.2f s); grids %s with "
+                    "equal weight (%s jobs); mmax 1 or 3, mrso 2; 5-40 site synthetic solutes in SPC/E water; "
+                    "isotropic c(q) = -3e-6 exp(-q^2); L-BFGS (history 5) to max |dE/dxi| <= %g (at most %d "
+                    "iterations); max_batch %d, HBM admission budget %d GB"
+                    % (len(jobs), cfg["rate_per_s"], arrivals[-1], ", ".join(shape_names),
+                       "/".join(str(sum(1 for j in jobs if j[0] == s)) for s in range(len(shape_names))),
+                       cfg["gtol"], cfg["max_iter"], cfg["max_batch"], cfg["hbm_budget_bytes"] // 10 ** 9),
+        "wall_s": wall, "peak_bytes": stats["peak_bytes"],
         "graph_steps": stats["graph_steps"], "direct_steps": stats["direct_steps"],
-        "sequential_solves_per_s": len(jobs) / seq,
+        "serial": {"form": form, "solves_per_s": len(jobs) / ser_span, "busy_solves_per_s": len(jobs) / sum(service),
+                   "p50_ms": 1e3 * _pct(ser_lats, 0.5), "p99_ms": 1e3 * _pct(ser_lats, 0.99),
+                   "iterations": iters_ser,
+                   "how": "one job at a time, single-field minimiser, plain FP64; service time = potential + "
+                          "minimisation between synchronizes; latencies and solves/s from a FIFO replay of the "
+                          "same arrivals through those service times"},
+        "speedup_vs_serial": (len(jobs) / wall) / (len(jobs) / ser_span),
+        "final_energy_rel_diff_vs_serial": {"max": max(rel), "median": _pct(rel, 0.5)},
     }
 
 
@@ -924,6 +968,11 @@ def run_ours(args):
     if args.mode == "energy":
         if rank == 0:
             print(json.dumps(energy_launches()), flush=True)
+        return
+    if args.mode == "serving":
+        if rank == 0:
+            print(json.dumps({"serving": serving_run("f64df"),
+                              "serving_solute": serving_solute_run(args.serving_jobs)}), flush=True)
         return
     forms = ("f64", "f64df", "f32")
     P = {f: make_problem(f) for f in forms}
@@ -1063,7 +1112,7 @@ def run_ours(args):
     if rank == 0 and not args.no_minimizer:
         out["minimizer"] = minimizer_run(head)
     if rank == 0 and not args.no_serving:
-        out["serving_solute"] = serving_solute_run(head)
+        out["serving_solute"] = serving_solute_run(args.serving_jobs)
     if rank == 0 and not args.no_large_solve:
         out["large_solve"] = large_solve_run()
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:

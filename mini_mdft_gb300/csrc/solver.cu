@@ -383,13 +383,20 @@ namespace {
 
 // Dekker's division (1971): the quotient of the leading floats, corrected once
 // from the remainder formed with an exact product.
+// The correction r / b.hi (about 2^-24 of the quotient) only has to be good
+// to a few ulps of its own: the approximate division (error 2^-46 of the
+// quotient at most) instead of a correctly rounded one.
 __device__ __forceinline__ DF df_div(DF a, DF b) {
   const float q1 = a.hi / b.hi;
   const float p = q1 * b.hi;
   const float pe = fmaf(q1, b.hi, -p);  // q1 b.hi = p + pe exactly
   const float r = (((a.hi - p) - pe) + a.lo) - q1 * b.lo;
-  return df_fast_two_sum(q1, r / b.hi);
+  return df_fast_two_sum(q1, __fdividef(r, b.hi));
 }
+
+// a field value as a double-float pair: exact for both storage types
+__device__ __forceinline__ DF eg_df(float a) { return DF(a, 0.f); }
+__device__ __forceinline__ DF eg_df(double a) { return df_from_double_bits(a); }
 
 // ln(x^2) and x^2 - 1 for 2^-20 <= |x| < 2^21 from one FMA: |x| = mx 2^ex with
 // mx in [1, 2); u = mx^2 = m 2^k with m in [1/sqrt 2, sqrt 2) (k = 0, 1, 2 by mx
@@ -449,7 +456,7 @@ __device__ __noinline__ Terms64 terms_f64(double x, double wo, double v, double 
 }
 
 template <typename TV>
-__global__ void __launch_bounds__(kRedThreads) eg_kernel(const EgArgs A) {
+__global__ void __launch_bounds__(kRedThreads, 4) eg_kernel(const EgArgs A) {
   extern __shared__ double ws[];  // w as double (no), then as double-float pairs (no)
   float2* wf = reinterpret_cast<float2*>(ws + A.no);
   for (int i = threadIdx.x; i < A.no; i += blockDim.x) {
@@ -462,6 +469,9 @@ __global__ void __launch_bounds__(kRedThreads) eg_kernel(const EgArgs A) {
   const TV* vx = static_cast<const TV*>(A.vexc);
   const double c_id = A.kT * A.rho0 * A.dv, c_ext = A.rho0 * A.dv, c_exc = A.prefactor * A.rho0;
   const DF kT(A.kh, A.kl), cext(A.ch, A.cl), cexc2(A.xh, A.xl), one(1.f, 0.f);
+  // preconditioner constants (the preconditioner only scales search
+  // directions: float precision and approximate division are enough)
+  const float ikT = 1.f / A.kh, c2k = 2.f * A.ch * A.kh;
   // sums of w (xi^2 ln xi^2 - xi^2 + 1), w xi^2 vext and w vexc (xi^2 - 1):
   // double-float Dot2 accumulators, and plain FP64 sums for the FP64 elements
   Acc<DF> a_id, a_ext, a_exc;
@@ -474,23 +484,37 @@ __global__ void __launch_bounds__(kRedThreads) eg_kernel(const EgArgs A) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   int o = (int)(i % A.no);
   const int ostep = (int)(stride % A.no);
+  // the next element's loads are issued before this element's arithmetic,
+  // so that each thread keeps a load of every input in flight meanwhile
+  double xn = 0.0, ven = 0.0;
+  TV vn = TV(0);
+  if (i < A.n) {
+    xn = A.xi[i];
+    vn = vx[i];
+    ven = A.vext ? A.vext[i] : 0.0;
+  }
   for (; i < A.n; i += stride) {
-    const double x = A.xi[i], v = (double)vx[i];
-    const double ve = A.vext ? A.vext[i] : 0.0;
+    const double x = xn, ve = ven;
+    const TV vv = vn;
+    if (i + stride < A.n) {
+      xn = A.xi[i + stride];
+      vn = vx[i + stride];
+      ven = A.vext ? A.vext[i + stride] : 0.0;
+    }
     const unsigned ebits = (unsigned)(bits_of(x) >> 52) & 0x7ffu;
     double gi;
     if (ebits - 1003u <= 40u) {  // 2^-20 <= |x| < 2^21
       const LnSq q = df_ln_sq(x, A);
       const float2 w2 = wf[o];
-      const DF wd(w2.x, w2.y), vd = to_compute<DF>(v), ved = df_from_double_bits(ve);
+      const DF wd(w2.x, w2.y), vd = eg_df(vv), ved = df_from_double_bits(ve);
       acc_mac(a_id, wd, q.L + q.t * (q.L - one));  // (1 + t) L - t
       acc_mac(a_ext, wd, (q.t + one) * ved);
       acc_mac(a_exc, wd, vd * q.t);
       const DF inner = cext * (kT * q.L + ved) + cexc2 * vd;
       gi = df_to_double(twice(df_from_double_bits(x) * wd) * inner);
-      if (A.hinv) A.hinv[i] = 1.f / (2.f * wd.hi * cext.hi * kT.hi * fmaxf(q.L.hi + 2.f + ved.hi / kT.hi, 1.f));
+      if (A.hinv) A.hinv[i] = __fdividef(1.f, wd.hi * c2k * fmaxf(q.L.hi + 2.f + ved.hi * ikT, 1.f));
     } else {
-      const Terms64 tt = terms_f64(x, ws[o], v, ve, A);
+      const Terms64 tt = terms_f64(x, ws[o], (double)vv, ve, A);
       d_id += tt.id;
       d_ext += tt.ext;
       d_exc += tt.exc;
@@ -530,7 +554,9 @@ __global__ void __launch_bounds__(kRedThreads) eg_kernel(const EgArgs A) {
 // is always handled by one CTA (the same in every round), its threads' sums
 // combined in a fixed order, and a field's chunk sums added in chunk order:
 // the result depends on neither the grid nor the other fields of the batch.
-constexpr int kLbChunks = 256;  // = threads per CTA: the final sum takes one chunk per thread
+constexpr int kLbChunks = 1024;  // per field: enough items to keep every CTA of the grid busy
+constexpr int kLbPerThread = kLbChunks / kRedThreads;  // chunks each thread adds in the final sum
+static_assert(kLbChunks % kRedThreads == 0, "the final sum gives each thread whole chunks");
 constexpr int kLbMaxSlots = 16;
 constexpr int kLbMaxOps = 192;
 constexpr long long kLbSpin = 1LL << 24;  // polls of the grid barrier (x 64 ns sleep): ~1 s
@@ -547,6 +573,12 @@ struct LbBatch {
   LbSlot slot[kLbMaxSlots];
   LbOp op[kLbMaxOps];
 };
+
+// elements per chunk: a multiple of 4, so that every chunk starts 16-byte
+// aligned in FP32 and FP64 arrays whose base is
+__host__ __device__ __forceinline__ long long lb_chunk_len(long long n) {
+  return ((n + kLbChunks - 1) / kLbChunks + 3) & ~3LL;
+}
 
 __device__ __forceinline__ DF as_df(float a) { return DF(a, 0.f); }
 __device__ __forceinline__ DF as_df(double a) { return df_from_double_bits(a); }
@@ -619,6 +651,231 @@ __device__ __forceinline__ int lb_dots(const LbOp& op) {
   return op.type == kOpPair ? 2 : (op.type == kOpPass && op.out >= 0 ? 1 : 0);
 }
 
+// ---- vector access: 4 consecutive elements from 16-byte aligned storage ----
+__device__ __forceinline__ void ld4(const float* p, long long i, float (&o)[4]) {
+  const float4 v = *reinterpret_cast<const float4*>(p + i);
+  o[0] = v.x;
+  o[1] = v.y;
+  o[2] = v.z;
+  o[3] = v.w;
+}
+__device__ __forceinline__ void ld4(const double* p, long long i, double (&o)[4]) {
+  const double2 a = *reinterpret_cast<const double2*>(p + i), b = *reinterpret_cast<const double2*>(p + i + 2);
+  o[0] = a.x;
+  o[1] = a.y;
+  o[2] = b.x;
+  o[3] = b.y;
+}
+__device__ __forceinline__ void st4(float* p, long long i, const float (&o)[4]) {
+  *reinterpret_cast<float4*>(p + i) = make_float4(o[0], o[1], o[2], o[3]);
+}
+__device__ __forceinline__ void st4(double* p, long long i, const double (&o)[4]) {
+  *reinterpret_cast<double2*>(p + i) = make_double2(o[0], o[1]);
+  *reinterpret_cast<double2*>(p + i + 2) = make_double2(o[2], o[3]);
+}
+// a float or double vector as floats (doubles rounded to nearest)
+__device__ __forceinline__ void ldu4(const void* p, int is64, long long i, float (&o)[4]) {
+  if (is64) {
+    double t[4];
+    ld4(static_cast<const double*>(p), i, t);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) o[q] = as_f(t[q]);
+  } else {
+    ld4(static_cast<const float*>(p), i, o);
+  }
+}
+// a float or double vector as double-float values (doubles split exactly)
+__device__ __forceinline__ void ldv4(const void* p, int is64, long long i, DF (&o)[4]) {
+  if (is64) {
+    double t[4];
+    ld4(static_cast<const double*>(p), i, t);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) o[q] = as_df(t[q]);
+  } else {
+    float t[4];
+    ld4(static_cast<const float*>(p), i, t);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) o[q] = as_df(t[q]);
+  }
+}
+__device__ __forceinline__ bool al16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+// The element work of one op over elements [i0, i1) of one field, the CTA's
+// threads striding by kRedThreads: with every array 16-byte aligned and i0 a
+// multiple of 4, thread t takes the 4-element groups t, t + 256, ... (two
+// groups' loads in flight per step), the elements past the last whole group
+// one by one; otherwise every element one by one.  The op's fields are read
+// into registers first (the kernel's parameter space would otherwise be
+// re-read around every store).  Dots accumulate into a0 (and a1).
+__device__ void lb_elements(const LbOp& opr, const LbSlot& slr, long long i0, long long i1, Acc<DF>& a0,
+                            Acc<DF>& a1) {
+  const int tid = threadIdx.x;
+  const int type = opr.type;
+  if (type == kOpPass) {
+    const double* S = slr.S;
+    double cc = opr.c0;
+    if (opr.i1 >= 0) cc += opr.c1 * __ldcg(S + opr.i1);
+    if (opr.i2 >= 0) cc += opr.c2 * __ldcg(S + opr.i2);
+    const double a = opr.ja >= 0 ? __ldcg(S + opr.ja) : opr.a0;
+    const float cf = (float)cc, af = (float)a, hf = opr.jh >= 0 ? (float)__ldcg(S + opr.jh) : 1.f;
+    const bool rx = a != 0.0, dot = opr.out >= 0;
+    float* __restrict__ x = opr.f0;
+    const void* u = opr.u;
+    const void* v = opr.v;
+    const float* __restrict__ h = opr.h;
+    const int u64 = opr.u64, v64 = opr.v64;
+    long long i = i0 + tid;
+    if (al16(x) && al16(u) && al16(v) && al16(h)) {
+      const long long g1 = i1 >> 2;  // whole groups end
+      long long g = (i0 >> 2) + tid;
+      for (; g < g1; g += 2 * kRedThreads) {
+        const bool two = g + kRedThreads < g1;
+        float xo[2][4], uo[2][4], ho[2][4];
+        DF vo[2][4];
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+          if (k == 1 && !two) break;
+          const long long e = (g + k * kRedThreads) << 2;
+          if (rx) {
+            ld4(x, e, xo[k]);
+          } else {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) xo[k][q] = 0.f;
+          }
+          ldu4(u, u64, e, uo[k]);
+          if (h) {
+            ld4(h, e, ho[k]);
+          } else {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) ho[k][q] = 1.f;
+          }
+          if (dot) ldv4(v, v64, e, vo[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+          if (k == 1 && !two) break;
+          float xv[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            xv[q] = (h ? hf * ho[k][q] : 1.f) * fmaf(cf, uo[k][q], af * xo[k][q]);
+            if (dot) acc_mac(a0, vo[k][q], as_df(xv[q]));
+          }
+          st4(x, (g + k * kRedThreads) << 2, xv);
+        }
+      }
+      i = max(i0, g1 << 2) + tid;  // the tail past the last whole group (none in an empty chunk)
+    }
+    for (; i < i1; i += kRedThreads) {
+      const float xv = (h ? hf * h[i] : 1.f) * fmaf(cf, ldu(u, u64, i), rx ? af * x[i] : 0.f);
+      x[i] = xv;
+      if (dot) acc_mac(a0, ldv(v, v64, i), as_df(xv));
+    }
+  } else if (type == kOpPair) {
+    const float tf = (float)opr.t;
+    float* __restrict__ hs = opr.f0;
+    float* __restrict__ hy = opr.f1;
+    const float* __restrict__ h = opr.h;
+    double* __restrict__ gg = slr.g;
+    double* __restrict__ xx = slr.x;
+    const double* __restrict__ gt = slr.gt;
+    const double* __restrict__ xt = slr.xt;
+    const float* __restrict__ d = slr.d;
+    long long i = i0 + tid;
+    if (al16(hs) && al16(hy) && al16(h) && al16(gg) && al16(xx) && al16(gt) && al16(xt) && al16(d)) {
+      const long long g1 = i1 >> 2;
+      long long g = (i0 >> 2) + tid;
+      for (; g < g1; g += kRedThreads) {
+        const long long e = g << 2;
+        double gn[4], go[4], xn[4];
+        float dv[4], hv[4];
+        ld4(gt, e, gn);
+        ld4(gg, e, go);
+        ld4(d, e, dv);
+        ld4(xt, e, xn);
+        if (h) ld4(h, e, hv);
+        float sv[4], yv[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          sv[q] = tf * dv[q];
+          yv[q] = (df_from_double_bits(gn[q]) - df_from_double_bits(go[q])).hi;
+          acc_mac(a0, as_df(sv[q]), as_df(yv[q]));
+          acc_mac(a1, as_df(h ? hv[q] * yv[q] : yv[q]), as_df(yv[q]));
+        }
+        st4(hs, e, sv);
+        st4(hy, e, yv);
+        st4(gg, e, gn);  // the accepted point
+        st4(xx, e, xn);
+      }
+      i = max(i0, g1 << 2) + tid;
+    }
+    for (; i < i1; i += kRedThreads) {
+      const double gn = gt[i], go = gg[i];
+      const float sv = tf * d[i];
+      const float yv = (df_from_double_bits(gn) - df_from_double_bits(go)).hi;
+      hs[i] = sv;
+      hy[i] = yv;
+      acc_mac(a0, as_df(sv), as_df(yv));
+      acc_mac(a1, as_df(h ? h[i] * yv : yv), as_df(yv));
+      gg[i] = gn;
+      xx[i] = xt[i];
+    }
+  } else if (type == kOpCopy) {
+    double* __restrict__ gg = slr.g;
+    double* __restrict__ xx = slr.x;
+    const double* __restrict__ gt = slr.gt;
+    const double* __restrict__ xt = slr.xt;
+    long long i = i0 + tid;
+    if (al16(gg) && al16(xx) && al16(gt) && al16(xt)) {
+      const long long g1 = i1 >> 2;
+      long long g = (i0 >> 2) + tid;
+      for (; g < g1; g += kRedThreads) {
+        const long long e = g << 2;
+        double a[4], b[4];
+        ld4(gt, e, a);
+        ld4(xt, e, b);
+        st4(gg, e, a);
+        st4(xx, e, b);
+      }
+      i = max(i0, g1 << 2) + tid;
+    }
+    for (; i < i1; i += kRedThreads) {
+      gg[i] = gt[i];
+      xx[i] = xt[i];
+    }
+  } else {  // kOpStep: one FP64 FMA per element, d widened exactly from its bits
+    const double t = opr.t;
+    double* __restrict__ xt = slr.xt;
+    const double* __restrict__ xx = slr.x;
+    const float* __restrict__ d = slr.d;
+    long long i = i0 + tid;
+    if (al16(xt) && al16(xx) && al16(d)) {
+      const long long g1 = i1 >> 2;
+      long long g = (i0 >> 2) + tid;
+      for (; g < g1; g += 2 * kRedThreads) {
+        const bool two = g + kRedThreads < g1;
+        double xo[2][4];
+        float dv[2][4];
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+          if (k == 1 && !two) break;
+          ld4(xx, (g + k * kRedThreads) << 2, xo[k]);
+          ld4(d, (g + k * kRedThreads) << 2, dv[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+          if (k == 1 && !two) break;
+          double o[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) o[q] = fma(t, f2d_bits(dv[k][q]), xo[k][q]);
+          st4(xt, (g + k * kRedThreads) << 2, o);
+        }
+      }
+      i = max(i0, g1 << 2) + tid;
+    }
+    for (; i < i1; i += kRedThreads) xt[i] = fma(t, f2d_bits(d[i]), xx[i]);
+  }
+}
+
 __global__ void __launch_bounds__(kRedThreads) lbfgs_batch_kernel(const __grid_constant__ LbBatch B,
                                                                    float2* __restrict__ part, unsigned* bar,
                                                                    int* err, int* flag) {
@@ -635,67 +892,13 @@ __global__ void __launch_bounds__(kRedThreads) lbfgs_batch_kernel(const __grid_c
       const LbSlot& sl = B.slot[j];
       if (r >= sl.nops) continue;
       const LbOp& op = B.op[sl.op0 + r];
-      const long long len = (sl.n + kLbChunks - 1) / kLbChunks;
-      const long long i0 = (long long)c * len, i1 = min(sl.n, i0 + len);
+      const long long len = lb_chunk_len(sl.n);
+      const long long i0 = min(sl.n, (long long)c * len), i1 = min(sl.n, i0 + len);
       Acc<DF> a0, a1;
       acc_zero(a0);
       acc_zero(a1);
-      const double* S = sl.S;
-      if (op.type == kOpPass) {
-        double cc = op.c0;
-        if (op.i1 >= 0) cc += op.c1 * __ldcg(S + op.i1);
-        if (op.i2 >= 0) cc += op.c2 * __ldcg(S + op.i2);
-        const double a = op.ja >= 0 ? __ldcg(S + op.ja) : op.a0;
-        const float cf = (float)cc, af = (float)a, hf = op.jh >= 0 ? (float)__ldcg(S + op.jh) : 1.f;
-        const bool rx = a != 0.0, dot = op.out >= 0;
-        float* __restrict__ x = op.f0;
-        long long i = i0 + tid;
-        for (; i + 3 * kRedThreads < i1; i += 4 * kRedThreads) {  // four elements' loads in flight
-          float xo[4], uo[4], ho[4];
-          DF vo[4];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const long long e = i + q * kRedThreads;
-            xo[q] = rx ? x[e] : 0.f;
-            uo[q] = ldu(op.u, op.u64, e);
-            ho[q] = op.h ? hf * op.h[e] : 1.f;
-            if (dot) vo[q] = ldv(op.v, op.v64, e);
-          }
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const float xv = ho[q] * fmaf(cf, uo[q], af * xo[q]);
-            x[i + q * kRedThreads] = xv;
-            if (dot) acc_mac(a0, vo[q], as_df(xv));
-          }
-        }
-        for (; i < i1; i += kRedThreads) {
-          const float xv = (op.h ? hf * op.h[i] : 1.f) * fmaf(cf, ldu(op.u, op.u64, i), rx ? af * x[i] : 0.f);
-          x[i] = xv;
-          if (dot) acc_mac(a0, ldv(op.v, op.v64, i), as_df(xv));
-        }
-      } else if (op.type == kOpPair) {
-        const float tf = (float)op.t;
-        for (long long i = i0 + tid; i < i1; i += kRedThreads) {
-          const double gn = sl.gt[i], go = sl.g[i];
-          const float sv = tf * sl.d[i];
-          const float yv = (df_from_double_bits(gn) - df_from_double_bits(go)).hi;
-          op.f0[i] = sv;
-          op.f1[i] = yv;
-          acc_mac(a0, as_df(sv), as_df(yv));
-          acc_mac(a1, as_df(op.h ? op.h[i] * yv : yv), as_df(yv));
-          sl.g[i] = gn;  // the accepted point
-          sl.x[i] = sl.xt[i];
-        }
-      } else if (op.type == kOpCopy) {
-        for (long long i = i0 + tid; i < i1; i += kRedThreads) {
-          sl.g[i] = sl.gt[i];
-          sl.x[i] = sl.xt[i];
-        }
-      } else {  // kOpStep: one FP64 FMA per element, d widened exactly from its bits
-        for (long long i = i0 + tid; i < i1; i += kRedThreads) sl.xt[i] = fma(op.t, f2d_bits(sl.d[i]), sl.x[i]);
-      }
-      const int nd = lb_dots(op);
-      if (nd) {
+      lb_elements(op, sl, i0, i1, a0, a1);
+      if (lb_dots(op)) {
         DF v[2] = {acc_get(a0), acc_get(a1)};
         lb_block_sum<2>(v);
         if (tid == 0) {
@@ -709,15 +912,21 @@ __global__ void __launch_bounds__(kRedThreads) lbfgs_batch_kernel(const __grid_c
       break;
     }
     if (!any_dot) continue;
-    // ---- sums: field j's chunk sums in chunk order, one CTA per field ----
+    // ---- sums: field j's chunk sums in chunk order, one CTA per field; thread
+    // t adds chunks kLbPerThread t .. kLbPerThread (t + 1) - 1 in order ----
     for (int j = blockIdx.x; j < B.nslots; j += gridDim.x) {
       const LbSlot& sl = B.slot[j];
       if (r >= sl.nops) continue;
       const LbOp& op = B.op[sl.op0 + r];
       if (!lb_dots(op)) continue;
-      const float2 q0 = __ldcg(&part[((long long)j * kLbChunks + tid) * 2]);
-      const float2 q1 = __ldcg(&part[((long long)j * kLbChunks + tid) * 2 + 1]);
-      DF v[2] = {DF(q0.x, q0.y), DF(q1.x, q1.y)};
+      DF v[2] = {DF(0.f, 0.f), DF(0.f, 0.f)};
+#pragma unroll
+      for (int q = 0; q < kLbPerThread; ++q) {
+        const long long c = (long long)j * kLbChunks + tid * kLbPerThread + q;
+        const float2 q0 = __ldcg(&part[c * 2]), q1 = __ldcg(&part[c * 2 + 1]);
+        v[0] = v[0] + DF(q0.x, q0.y);
+        v[1] = v[1] + DF(q1.x, q1.y);
+      }
       lb_block_sum<2>(v);
       if (tid == 0) {
         double* S = sl.S;
