@@ -486,6 +486,62 @@ def energy_launches():
     return {"mode": "energy", "iterations": len(trace) - 1, "energy_end": float(trace[-1, 0])}
 
 
+def delta_f_call_times(reps=30):
+    """mdft_get_delta_f against mdft_get_delta_f_noalloc on the headline
+    fields (64^3 / mmax 3: 2^18 points x 84 orientations, FP64 fields in the
+    double-float form, seed 0), called straight through the C ABI: host
+    microseconds inside each call, and device microseconds between CUDA
+    events recorded on the stream just before and just after each call
+    (launch gaps, the scratch allocation and the completion-counter reset
+    included).  The allocation-free call's interval is its counter reset and
+    the energy kernel alone, so the difference is what the stream-ordered
+    scratch allocation costs."""
+    import ctypes as C
+
+    import torch
+
+    import mini_mdft_gb300 as M
+    from mini_mdft_gb300 import inputs as I
+    L = M.lib()
+    n, mmax, mrso = WORKLOAD["n"], WORKLOAD["mmax"], WORKLOAD["mrso"]
+    ag = M.AngularGrid(mmax, mrso)
+    N = n[0] * n[1] * n[2]
+    rho0, pref = I.solvent_constants(I.SPCE_N0, mrso)
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    xi = torch.rand((N, ag.m_no), generator=gen, device="cuda", dtype=torch.float64) * 0.2 + 0.9
+    vexc = torch.rand(xi.shape, generator=gen, device="cuda", dtype=torch.float64)
+    w = torch.from_numpy(ag.m_w).cuda()
+    df = torch.empty_like(xi)
+    ff = torch.zeros(1, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    args = [C.c_void_p(t.data_ptr()) for t in (xi, vexc, w, df, ff)]
+    out = {}
+    for name in ("mdft_get_delta_f", "mdft_get_delta_f_noalloc"):
+        fn = getattr(L, name)
+        for _ in range(5):
+            assert fn(*args, N, ag.m_no, rho0, pref, 2, sp) == 0
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        host = 0.0
+        for a, b in ev:
+            a.record(stream)
+            t0 = time.perf_counter()
+            rc = fn(*args, N, ag.m_no, rho0, pref, 2, sp)
+            host += time.perf_counter() - t0
+            b.record(stream)
+            assert rc == 0
+            stream.synchronize()  # one call at a time, as a solver's loop makes them
+        dev = sorted(a.elapsed_time(b) * 1e3 for a, b in ev)
+        out[name] = {"host_us_per_call": host / reps * 1e6, "device_us_median": dev[len(dev) // 2],
+                     "device_us_min": dev[0]}
+    a, b = out["mdft_get_delta_f"], out["mdft_get_delta_f_noalloc"]
+    out["allocation_cost_us"] = a["device_us_median"] - b["device_us_median"]
+    out["workload"] = ("64^3 points x 84 orientations, FP64 fields, double-float form; %d calls each, one at a time "
+                       "(synchronised between calls)" % reps)
+    return out
+
+
 def minimizer_run(prec):
     """One minimiser run on the headline workload (64^3 / 30 A / mmax 3 /
     mrso 2): a 12-site synthetic solute (sites uniform in the central 10 A
@@ -653,30 +709,30 @@ def serving_run(prec):
     wall = time.perf_counter() - t0
     st = srv.stats()
     srv.close()
-    # the same jobs one at a time, operator API on the caller's stream
-    # (host fields page-locked like the server's, device buffers made once)
+    # the same jobs one at a time, operator API on the caller's stream: the
+    # same host arrays in and a host array out per job, as the server takes
+    # and returns them (device buffers made once per shape)
     plans = {}
     for n, box, _ in SERVING["shapes"]:
         sg, ag = M.SpatialGrid(n, box), M.AngularGrid(mmax, mrso)
-        host = torch.from_numpy(fields[n]).pin_memory()
-        dev = torch.empty_like(host, device="cuda")
+        dev = torch.empty(fields[n].shape, dtype=torch.from_numpy(fields[n]).dtype, device="cuda")
         p = torch.zeros((ag.m_np,) + tuple(n), dtype=torch.complex64 if prec == "f32" else torch.complex128,
                         device="cuda")
         plans[n] = (M.OrientationProjectionTransform(sg, ag, precision=prec),
                     M.Convolution.from_table(idx, tab, dq, sg, ag, precision=prec),
-                    torch.from_numpy(ag.m_w), host, dev, p, torch.empty_like(dev), torch.empty_like(dev),
-                    torch.empty_like(host).pin_memory())
+                    torch.from_numpy(ag.m_w), dev, p, torch.empty_like(dev), torch.empty_like(dev))
+
     def one_at_a_time(job_list):
         for n, box, k in job_list:
-            opt, conv, w, host, xi, p, vexc, df, out = plans[n]
-            xi.copy_(host, non_blocking=True)
+            opt, conv, w, xi, p, vexc, df = plans[n]
+            xi.copy_(torch.from_numpy(fields[n]))
             for _ in range(k):
                 opt.angl2proj_from_xi(xi, rho0, p)
                 conv.execute(p)
                 opt.proj2angl(p, vexc)
                 M.get_delta_f(xi, vexc, w, df, rho0, pref)
                 xi -= SERVING["step"] * df
-            out.copy_(xi)
+            xi.cpu().numpy()
 
     one_at_a_time([(n, box, 2) for n, box, _ in SERVING["shapes"]])  # warm-up, as for the server
     torch.cuda.synchronize()
@@ -700,9 +756,10 @@ def serving_run(prec):
 
 SERVING_SOLUTE = dict(shapes=[((32, 32, 32), (20.0, 20.0, 20.0), 0.25), ((48, 64, 80), (24.0, 30.0, 36.0), 0.25),
                               ((64, 64, 64), (30.0, 30.0, 30.0), 0.25), ((96, 96, 96), (40.0, 40.0, 40.0), 0.25)],
-                      mmax=(1, 3), mrso=2, sites=(5, 41), jobs=256, rate_per_s=40.0, gtol=1e-5, max_iter=300,
-                      max_batch=8, hbm_budget_bytes=120 * 10 ** 9, dq=0.05, amplitude=CQ_AMPLITUDE,
-                      server_form="f32", serial_form="f64")
+                      mmax=(1, 3), mrso=2, sites=(5, 41), jobs=256, default_jobs=64, rate_per_s=40.0, gtol=1e-5,
+                      max_iter=300, max_batch=8, hbm_budget_bytes=120 * 10 ** 9, dq=0.05, amplitude=CQ_AMPLITUDE,
+                      plain_sample=4)
+_END = {0: "gtol", 1: "flat", 2: "max_iter", 3: "no_decrease"}
 
 
 def _pct(v, q):
@@ -710,59 +767,51 @@ def _pct(v, q):
     return v[min(len(v) - 1, int(q * len(v)))]
 
 
-def serving_solute_run(jobs_n=None):
-    """The solvation request stream: SERVING_SOLUTE["jobs"] requests with
-    Poisson arrivals at rate_per_s, grids drawn with equal weight from {32^3
-    / 20 A, 48x64x80 / 24x30x36 A, 64^3 / 30 A, 96^3 / 40 A}, mmax from {1,
-    3} (mrso 2), each with a seeded synthetic solute of 5-40 LJ + charge
-    sites in SPC/E water, isotropic c(q) = -3e-6 exp(-q^2), minimised to max
-    |dE/dxi| <= 1e-5.
-
-    The server runs the mixed form (FP32 fields, per-job potential and
-    L-BFGS state resident on the device, same-shape jobs batched into one
-    evaluation and one L-BFGS launch per step, HBM admission budget 120 GB).
-    Against it: the same jobs solved one at a time in the plain FP64 form by
-    the single-field minimiser, each job's service time (potential +
-    minimisation) measured on the device side of a synchronize; their p50/p99
-    latencies replay the same arrivals through a first-in-first-out queue of
-    those service times."""
-    import threading
-
+def _stream(n_jobs):
+    """The seeded request stream: (jobs, arrivals, solutes, c(q) tables);
+    the first n requests of any longer stream are the same."""
     import numpy as np
-    import torch
 
-    import mini_mdft_gb300 as M
     from mini_mdft_gb300 import inputs as I
     cfg = SERVING_SOLUTE
-    n_jobs = jobs_n or cfg["jobs"]
-    mrso, dq = cfg["mrso"], cfg["dq"]
-    rho0, pref = I.solvent_constants(I.SPCE_N0, mrso)
-    kT = I.kT()
-    vmax = 100 * kT
     rng = np.random.default_rng(7)
     weights = np.array([w for _, _, w in cfg["shapes"]])
     jobs = []
-    for i in range(n_jobs):
+    for i in range(cfg["jobs"]):
         si = int(rng.choice(len(cfg["shapes"]), p=weights / weights.sum()))
         mmax = int(rng.choice(cfg["mmax"]))
         n_sites = int(rng.integers(*cfg["sites"]))
         jobs.append((si, mmax, n_sites, 100 + i))
     arrivals = np.cumsum(rng.exponential(1.0 / cfg["rate_per_s"], len(jobs)))
     arrivals -= arrivals[0]
+    jobs, arrivals = jobs[:n_jobs], arrivals[:n_jobs]
     tables = {}
     for mmax in cfg["mmax"]:
-        nq = max(I.nq_for(n, box, dq) for n, box, _ in cfg["shapes"]) + 2
-        tables[mmax] = I.isotropic_cq(mmax, mrso, nq, dq, amplitude=cfg["amplitude"])
+        nq = max(I.nq_for(n, box, cfg["dq"]) for n, box, _ in cfg["shapes"]) + 2
+        tables[mmax] = I.isotropic_cq(mmax, cfg["mrso"], nq, cfg["dq"], amplitude=cfg["amplitude"])
     solutes = [I.synthetic_solute(ns, cfg["shapes"][si][1], seed=seed) for si, _, ns, seed in jobs]
+    return jobs, arrivals, solutes, tables
 
-    # ---- the server, mixed form
-    srv = M.Server(precision=cfg["server_form"], max_batch=cfg["max_batch"],
-                   hbm_budget_bytes=cfg["hbm_budget_bytes"])
+
+def _serve_stream(form, jobs, arrivals, solutes, tables):
+    """The job server in one form on the stream, requests submitted at their
+    arrival times from a second thread; latency = submit to result."""
+    import threading
+
+    import torch
+
+    import mini_mdft_gb300 as M
+    from mini_mdft_gb300 import inputs as I
+    cfg = SERVING_SOLUTE
+    mrso, dq = cfg["mrso"], cfg["dq"]
+    rho0, pref = I.solvent_constants(I.SPCE_N0, mrso)
+    kT = I.kT()
+    srv = M.Server(precision=form, max_batch=cfg["max_batch"], hbm_budget_bytes=cfg["hbm_budget_bytes"])
     sid = {}
     for mmax in cfg["mmax"]:
         idx, tab = tables[mmax]
         sid[mmax] = srv.add_solvent(mmax, mrso, idx, tab, dq, rho0, pref)
-        srv.set_solvent_model(sid[mmax], I.SPCE_SITES, kT, vmax)
+        srv.set_solvent_model(sid[mmax], I.SPCE_SITES, kT, 100 * kT)
     for n, box, _ in cfg["shapes"]:  # warm-up: plans, arenas, graphs
         for mmax in cfg["mmax"]:
             srv.wait_solute(srv.submit_solute(sid[mmax], n, box, solutes[0][:2], max_iter=3, gtol=0.0))
@@ -780,21 +829,42 @@ def serving_solute_run(jobs_n=None):
     th = threading.Thread(target=submitter, args=(t0,))
     th.start()
     th.join()
-    lats, iters, status, e_srv = [], 0, {}, []
+    lats, iters, status, energies, gmax = [], 0, {}, [], []
     for k in range(len(jobs)):
         _, trace, st, lat = srv.wait_solute(ids[k])
         lats.append(lat)
         iters += len(trace) - 1
         status[st] = status.get(st, 0) + 1
-        e_srv.append(float(trace[-1, 0]))
+        energies.append(float(trace[-1, 0]))
+        gmax.append(float(trace[-1, 4]))
     wall = time.perf_counter() - t0
     stats = srv.stats()
     srv.close()
     del srv
     torch.cuda.empty_cache()
+    return {"form": form, "solves_per_s": len(jobs) / wall, "p50_ms": 1e3 * _pct(lats, 0.5),
+            "p99_ms": 1e3 * _pct(lats, 0.99), "wall_s": wall, "iterations": iters,
+            "ended_by": {_END[k]: v for k, v in sorted(status.items())},
+            "final_max_abs_gradient": {"median": _pct(gmax, 0.5), "max": max(gmax)},
+            "peak_bytes": stats["peak_bytes"], "graph_steps": stats["graph_steps"],
+            "direct_steps": stats["direct_steps"]}, energies
 
-    # ---- the same jobs one at a time, plain FP64, single-field minimiser
-    form = cfg["serial_form"]
+
+def _serial_stream(form, jobs, arrivals, solutes, tables, every=1):
+    """The same jobs (every `every`-th one) one at a time through the
+    single-field minimiser: each job's service time (potential +
+    minimisation between synchronizes); solves/s and p50/p99 from a
+    first-in-first-out replay of the arrivals through those service times
+    (with every > 1 only the busy rate is stated)."""
+    import torch
+
+    import mini_mdft_gb300 as M
+    from mini_mdft_gb300 import inputs as I
+    cfg = SERVING_SOLUTE
+    mrso, dq = cfg["mrso"], cfg["dq"]
+    rho0, pref = I.solvent_constants(I.SPCE_N0, mrso)
+    kT = I.kT()
+    vmax = 100 * kT
     plans = {}
     for si, (n, box, _) in enumerate(cfg["shapes"]):
         for mmax in cfg["mmax"]:
@@ -806,8 +876,10 @@ def serving_solute_run(jobs_n=None):
         vext = M.solute_vext(sg, ag, I.SPCE_SITES, solutes[0][:2], vmax)
         M.Solver(opt, conv, vext, kT=kT, rho0=rho0, prefactor=pref, history=5).minimize(torch.ones_like(vext),
                                                                                            max_iter=3, gtol=0.0)
-    service, e_ser, iters_ser = [], [], 0
-    for k, (si, mmax, _, _) in enumerate(jobs):
+    picked = list(range(0, len(jobs), every))
+    service, energies, iters, status, gmax = [], {}, 0, {}, []
+    for k in picked:
+        si, mmax, _, _ = jobs[k]
         sg, ag, opt, conv = plans[(si, mmax)]
         torch.cuda.synchronize()
         t1 = time.perf_counter()
@@ -821,42 +893,82 @@ def serving_solute_run(jobs_n=None):
         trace = solver.minimize(xi, max_iter=cfg["max_iter"], gtol=cfg["gtol"])
         torch.cuda.synchronize()
         service.append(s + time.perf_counter() - t1)
-        e_ser.append(float(trace[-1, 0]))
-        iters_ser += len(trace) - 1
+        st = solver.status()
+        status[st] = status.get(st, 0) + 1
+        energies[k] = float(trace[-1, 0])
+        gmax.append(float(trace[-1, 4]))
+        iters += len(trace) - 1
         del solver, vext, xi
     del plans
     torch.cuda.empty_cache()
-    free, done, ser_lats = 0.0, 0.0, []
-    for k in range(len(jobs)):  # FIFO replay of the arrivals through the measured service times
-        start = max(arrivals[k], free)
-        free = start + service[k]
-        ser_lats.append(free - arrivals[k])
-    ser_span = free  # first arrival to last completion
-    rel = [abs(a - b) / abs(b) for a, b in zip(e_srv, e_ser)]
-    names = {0: "gtol", 1: "flat", 2: "max_iter", 3: "no_decrease"}
+    out = {"form": form, "jobs": len(picked), "busy_solves_per_s": len(picked) / sum(service), "iterations": iters,
+           "ended_by": {_END[k]: v for k, v in sorted(status.items())},
+           "final_max_abs_gradient": {"median": _pct(gmax, 0.5), "max": max(gmax)}}
+    if every == 1:
+        free, lats = 0.0, []
+        for k in range(len(jobs)):
+            start = max(arrivals[k], free)
+            free = start + service[k]
+            lats.append(free - arrivals[k])
+        out.update(solves_per_s=len(jobs) / free, p50_ms=1e3 * _pct(lats, 0.5), p99_ms=1e3 * _pct(lats, 0.99))
+    return out, energies
+
+
+def serving_solute_run(jobs_n=None):
+    """The solvation request stream (config: SERVING_SOLUTE): requests with
+    Poisson arrivals at rate_per_s, grids drawn with equal weight from {32^3
+    / 20 A, 48x64x80 / 24x30x36 A, 64^3 / 30 A, 96^3 / 40 A}, mmax from {1,
+    3} (mrso 2), each with a seeded synthetic solute of 5-40 LJ + charge
+    sites in SPC/E water, isotropic c(q) = -3e-6 exp(-q^2), minimised with
+    L-BFGS (history 5) to max |dE/dxi| <= 1e-5 (at most 300 iterations).
+    The first default_jobs requests of the 256-request stream by default.
+
+    Arms, each on the same requests:
+      * the server in the FP64-accurate form (FP64 fields, double-float
+        arithmetic; the headline "value");
+      * the server in the mixed form (FP32 fields and FP32 transforms,
+        double-float sums and FP64 minimiser state);
+      * serial: one job at a time through the single-field minimiser in the
+        FP64-accurate form, latencies from a FIFO replay of the arrivals;
+      * serial plain FP64 (FP64 arithmetic throughout), on every
+        plain_sample-th request: its busy solves/s.
+    The server keeps each job's potential and L-BFGS state on the device,
+    evaluates same-shape jobs as one batch and runs their L-BFGS steps in
+    one batched launch sequence per step, and admits groups within an HBM
+    budget of 120 GB."""
+    cfg = SERVING_SOLUTE
+    n_jobs = jobs_n or cfg["default_jobs"]
+    jobs, arrivals, solutes, tables = _stream(n_jobs)
+    srv_df, e_df = _serve_stream("f64df", jobs, arrivals, solutes, tables)
+    srv_mix, e_mix = _serve_stream("f32", jobs, arrivals, solutes, tables)
+    ser, e_ser = _serial_stream("f64df", jobs, arrivals, solutes, tables)
+    plain, e_plain = _serial_stream("f64", jobs, arrivals, solutes, tables, every=cfg["plain_sample"])
+
+    def rel(a, b):
+        r = [abs(x - y) / abs(y) for x, y in zip(a, b)]
+        return {"max": max(r), "median": _pct(r, 0.5)}
     shape_names = ["32^3/20 A", "48x64x80/24x30x36 A", "64^3/30 A", "96^3/40 A"]
+    e_ser_list = [e_ser[k] for k in range(len(jobs))]
     return {
-        "metric": "served solute solves/s", "value": len(jobs) / wall, "unit": "solves/s",
-        "p50_ms": 1e3 * _pct(lats, 0.5), "p99_ms": 1e3 * _pct(lats, 0.99),
-        "jobs": len(jobs), "iterations": iters, "form": cfg["server_form"],
-        "ended_by": {names[k]: v for k, v in sorted(status.items())},
-        "workload": "%d solvation requests, Poisson arrivals at %.0f/s (last arrival at %.2f s); grids %s with "
-                    "equal weight (%s jobs); mmax 1 or 3, mrso 2; 5-40 site synthetic solutes in SPC/E water; "
-                    "isotropic c(q) = -3e-6 exp(-q^2); L-BFGS (history 5) to max |dE/dxi| <= %g (at most %d "
-                    "iterations); max_batch %d, HBM admission budget %d GB"
-                    % (len(jobs), cfg["rate_per_s"], arrivals[-1], ", ".join(shape_names),
+        "metric": "served solute solves/s", "value": srv_df["solves_per_s"], "unit": "solves/s",
+        "p50_ms": srv_df["p50_ms"], "p99_ms": srv_df["p99_ms"], "jobs": len(jobs), "form": "f64df",
+        "workload": "%d solvation requests (the first %d of the seeded 256-request stream), Poisson arrivals at "
+                    "%.0f/s (last at %.2f s); grids %s with equal weight (%s requests); mmax 1 or 3, mrso 2; "
+                    "5-40 site synthetic solutes in SPC/E water; isotropic c(q) = -3e-6 exp(-q^2); L-BFGS "
+                    "(history 5) to max |dE/dxi| <= %g (at most %d iterations); max_batch %d, HBM admission "
+                    "budget %d GB"
+                    % (len(jobs), len(jobs), cfg["rate_per_s"], arrivals[-1], ", ".join(shape_names),
                        "/".join(str(sum(1 for j in jobs if j[0] == s)) for s in range(len(shape_names))),
                        cfg["gtol"], cfg["max_iter"], cfg["max_batch"], cfg["hbm_budget_bytes"] // 10 ** 9),
-        "wall_s": wall, "peak_bytes": stats["peak_bytes"],
-        "graph_steps": stats["graph_steps"], "direct_steps": stats["direct_steps"],
-        "serial": {"form": form, "solves_per_s": len(jobs) / ser_span, "busy_solves_per_s": len(jobs) / sum(service),
-                   "p50_ms": 1e3 * _pct(ser_lats, 0.5), "p99_ms": 1e3 * _pct(ser_lats, 0.99),
-                   "iterations": iters_ser,
-                   "how": "one job at a time, single-field minimiser, plain FP64; service time = potential + "
-                          "minimisation between synchronizes; latencies and solves/s from a FIFO replay of the "
-                          "same arrivals through those service times"},
-        "speedup_vs_serial": (len(jobs) / wall) / (len(jobs) / ser_span),
-        "final_energy_rel_diff_vs_serial": {"max": max(rel), "median": _pct(rel, 0.5)},
+        "server_f64df": srv_df, "server_mixed": srv_mix, "serial_f64df": ser,
+        "serial_plain_f64_sample": plain,
+        "speedup_server_f64df_vs_serial_f64df": srv_df["solves_per_s"] / ser["solves_per_s"],
+        "speedup_server_mixed_vs_serial_f64df": srv_mix["solves_per_s"] / ser["solves_per_s"],
+        "speedup_server_mixed_vs_serial_plain_f64_busy": srv_mix["solves_per_s"] / plain["busy_solves_per_s"],
+        "final_energy_rel_diff": {"server_f64df_vs_serial": rel(e_df, e_ser_list),
+                                  "server_mixed_vs_serial": rel(e_mix, e_ser_list),
+                                  "serial_plain_vs_serial": rel([e_plain[k] for k in sorted(e_plain)],
+                                                                [e_ser[k] for k in sorted(e_plain)])},
     }
 
 
@@ -1111,6 +1223,7 @@ def run_ours(args):
         out["serving"] = serving_run(head)
     if rank == 0 and not args.no_minimizer:
         out["minimizer"] = minimizer_run(head)
+        out["get_delta_f_calls"] = delta_f_call_times()
     if rank == 0 and not args.no_serving:
         out["serving_solute"] = serving_solute_run(args.serving_jobs)
     if rank == 0 and not args.no_large_solve:

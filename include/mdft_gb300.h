@@ -208,11 +208,18 @@ int mdft_get_delta_rho(const void* xi, void* delta_rho, size_t n, double rho0,
  * first).  The sum over points is deterministic on a given GPU (a fixed
  * reduction tree with compensated partial sums; its shape follows the
  * device's SM count and the kernel's occupancy).  Uses a stream-ordered
- * temporary of 16 bytes per 32 points, plus 16. */
+ * temporary of 16 bytes per 32 points, plus 16, from the library's own pool
+ * (mdft_scratch_pool). */
 int mdft_get_delta_f(const void* xi, const void* vexc, const double* w,
                      void* delta_f, double* ff_dev, size_t nxyz, int no,
                      double rho0, double prefactor, int precision,
                      void* stream);
+/* The stream-ordered memory pool (a cudaMemPool_t) on the current device
+ * that the library's allocating entry points take their temporaries from,
+ * created at the first use; it keeps up to 64 MiB mapped between calls, so
+ * calls made after a synchronize do not map their scratch again.  No
+ * counterpart in the reference. */
+int mdft_scratch_pool(void** pool);
 
 /* get_delta_f for callers that cannot allocate device memory while they run
  * (an application that gives the whole GPU to its own pool allocator up
@@ -354,6 +361,10 @@ int mdft_solver_energy(mdft_solver_t s, const double* xi, double* grad, double* 
  * iteration i; iterations (may be NULL): iterations taken. */
 int mdft_solver_minimize(mdft_solver_t s, double* xi, int max_iter, double gtol, double ftol,
                          double* trace, int* iterations, void* stream);
+/* How the last mdft_solver_minimize ended: 0 max |dE/dxi| <= gtol, 1 |Delta E|
+ * <= ftol max(1, |E|), 2 max_iter reached, 3 no step along the search
+ * direction lowered E (after 40 halvings), -1 never run. */
+int mdft_solver_status(mdft_solver_t s, int* status);
 int mdft_solver_destroy(mdft_solver_t s);
 
 #ifdef __cplusplus

@@ -59,6 +59,7 @@ SIGNATURES = {
     "mdft_get_delta_rho": (i32, [vp, vp, sz, f64, i32, vp]),
     "mdft_get_delta_f": (i32, [vp, vp, vp, vp, vp, sz, i32, f64, f64, i32, vp]),
     "mdft_get_delta_f_noalloc": (i32, [vp, vp, vp, vp, vp, sz, i32, f64, f64, i32, vp]),
+    "mdft_scratch_pool": (i32, [C.POINTER(vp)]),
     "mdft_wait_timeouts": (i32, [ip]),
     "mdft_wait_selftest": (i32, [i32, vp]),
     "mdft_grid_barrier_selftest": (i32, [i32, vp]),
@@ -77,6 +78,7 @@ SIGNATURES = {
     "mdft_solver_create": (i32, [C.POINTER(vp), vp, vp, vp, f64, f64, f64, i32]),
     "mdft_solver_energy": (i32, [vp, vp, vp, dp, vp]),
     "mdft_solver_minimize": (i32, [vp, vp, i32, f64, f64, dp, ip, vp]),
+    "mdft_solver_status": (i32, [vp, ip]),
     "mdft_solver_destroy": (i32, [vp]),
 }
 

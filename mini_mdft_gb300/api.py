@@ -575,6 +575,16 @@ class Solver:
                                          _np_d(trace), C.byref(it), _stream()))
         return trace[: it.value + 1]
 
+    STATUS = {0: "gtol", 1: "flat", 2: "max_iter", 3: "no_decrease", -1: "not_run"}
+
+    def status(self):
+        """How the last minimize ended (mdft_solver_status): 0 gtol reached,
+        1 E flat (ftol), 2 max_iter, 3 no decrease along the direction, -1
+        never run."""
+        st = C.c_int()
+        check(lib().mdft_solver_status(self.h, C.byref(st)))
+        return st.value
+
 
 def luc_read(path, np_luc, qmax):
     """IO::LucData: (luc_index (5, np_luc) int32, table (np_luc, nq) complex128,

@@ -10,6 +10,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -470,12 +471,49 @@ void check_device(int dev) {
 }
 
 // Stream-ordered scratch for the energy partials.
+// The library's own stream-ordered memory pool on the current device, for
+// the temporaries of its allocating entry points.  It keeps up to
+// kScratchKeep bytes mapped between calls: the device's default pool hands
+// its memory back to the driver at every synchronisation (unless its owner
+// raised the release threshold), so each call made after a synchronize --
+// a solver reads its energy back every iteration -- would map its scratch
+// afresh, about 100 us of host time per call.  A handle found invalid (the
+// context torn down and created again) is replaced.
+constexpr uint64_t kScratchKeep = uint64_t(64) << 20;
+std::mutex g_pool_mu;
+std::map<int, cudaMemPool_t> g_pools;
+
+cudaMemPool_t scratch_pool() {
+  int dev = 0;
+  mdft::cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  auto it = g_pools.find(dev);
+  if (it != g_pools.end()) {
+    uint64_t v = 0;
+    if (cudaMemPoolGetAttribute(it->second, cudaMemPoolAttrReleaseThreshold, &v) == cudaSuccess) return it->second;
+    cudaGetLastError();
+    g_pools.erase(it);
+  }
+  cudaMemPoolProps props{};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = dev;
+  cudaMemPool_t pool = nullptr;
+  mdft::cuda_check(cudaMemPoolCreate(&pool, &props), "cudaMemPoolCreate");
+  uint64_t keep = kScratchKeep;
+  mdft::cuda_check(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep),
+                   "cudaMemPoolSetAttribute");
+  g_pools[dev] = pool;
+  return pool;
+}
+
 struct Scratch {
   void* p = nullptr;
   cudaStream_t s;
   Scratch(size_t bytes, cudaStream_t st) : s(st) {
-    cudaError_t e = cudaMallocAsync(&p, bytes, s);
-    if (e != cudaSuccess) throw Error(MDFT_ERR_NOMEM, std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
+    cudaError_t e = cudaMallocFromPoolAsync(&p, bytes, scratch_pool(), s);
+    if (e != cudaSuccess)
+      throw Error(MDFT_ERR_NOMEM, std::string("cudaMallocFromPoolAsync: ") + cudaGetErrorString(e));
   }
   ~Scratch() {
     if (p) cudaFreeAsync(p, s);
@@ -487,6 +525,13 @@ struct Scratch {
 extern "C" {
 
 int mdft_abi_version(void) { return MDFT_GB300_ABI_VERSION; }
+
+int mdft_scratch_pool(void** pool) {
+  return guarded([&] {
+    throw_if(!pool, "NULL argument");
+    *pool = scratch_pool();
+  });
+}
 
 const char* mdft_last_error(void) { return g_last_error.c_str(); }
 

@@ -8,7 +8,9 @@
 // them in a fixed order, so ff is deterministic and independent of
 // scheduling.
 #include <algorithm>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <string>
 
 #include "common.cuh"
@@ -210,14 +212,30 @@ void launch_delta_rho(const T* xi, T* dr, size_t n, double rho0, cudaStream_t s)
 // this kernel), each with an equal run of grid points, and no more CTAs than
 // the scratch has partial slots (one per kEnergyPoints points).  The grid
 // depends only on the device and the problem, so ff does too.
+// SMs x resident CTAs of one delta_f kernel instance at a shared-memory size,
+// per device: queried once and cached (a query per call costs microseconds
+// of host time on every get_delta_f)
 template <typename T, bool F64>
-unsigned delta_f_grid(size_t nxyz, size_t nb, size_t smem, size_t* chunk) {
-  int dev = 0, sms = 0, per_sm = 0;
+size_t delta_f_wave(size_t smem) {
+  static std::mutex mu;
+  static std::map<std::pair<int, size_t>, size_t> cache;
+  int dev = 0;
   cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find({dev, smem});
+  if (it != cache.end()) return it->second;
+  int sms = 0, per_sm = 0;
   cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
   cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, delta_f_kernel<T, F64>, kEnergyThreads, smem),
              "cudaOccupancyMaxActiveBlocksPerMultiprocessor(delta_f)");
   const size_t wave = (size_t)std::max(1, sms) * (size_t)std::max(1, per_sm);
+  cache[{dev, smem}] = wave;
+  return wave;
+}
+
+template <typename T, bool F64>
+unsigned delta_f_grid(size_t nxyz, size_t nb, size_t smem, size_t* chunk) {
+  const size_t wave = delta_f_wave<T, F64>(smem);
   const size_t want = std::min(nb, wave);
   *chunk = (nxyz + want - 1) / want;
   return (unsigned)((nxyz + *chunk - 1) / *chunk);  // CTAs with a non-empty run

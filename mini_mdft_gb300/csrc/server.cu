@@ -13,8 +13,9 @@
 //     the group advances all its active jobs (compacted into the first k
 //     slots) with one set of batched launches per step;
 //   * each group step is replayed from a CUDA graph captured for its active
-//     count k (the first step at a given k runs directly, which also checks
-//     the launches, and a failed capture falls back to direct launches);
+//     count k; the graphs of every k are captured when the group is made (a
+//     count whose capture fails runs directly, and is captured again after
+//     its first direct step);
 //   * a group is created only while the device memory of all groups stays
 //     within the server's budget; groups without jobs are released, least
 //     recently used first, when a new one does not fit;
@@ -182,7 +183,10 @@ struct Group {
   DevPtr xt, x, g, gt, vext, d, hs, hy, hinv, S, red;
   double* tails = nullptr;  // page-locked: 8 doubles per slot read back each step
   std::vector<mdft::Lbfgs> lb;
-  mdft::LbRunner lbr;  // one persistent launch per step runs every slot's L-BFGS operations
+  // every slot's L-BFGS operations of a step in one batch, one launch per
+  // round (not the persistent cooperative launch: a group's launches share
+  // the GPU with the other groups' streams)
+  mdft::LbRunner lbr;
   int queued = 1;      // fixed-step groups: steps queued by the last launch
   mdft::EgConst eg{};
   Solvent model;
@@ -232,6 +236,7 @@ struct mdft_server_s {
   void admit();
   Group* group_for(const Job& j);
   void step(Group& g);
+  void precapture(Group& g);
   void enqueue_step(Group& g, int k);
   void bind_slot(Group& g, int slot);
   void complete_step(Group& g);
@@ -297,7 +302,7 @@ Group* mdft_server_s::group_for(const Job& j) {
                    : (5 * f64b + f64b / 2 * (2 + 2 * kHistory) + fb * (g->elem == 4 ? 2 : 1) +
                       (size_t)g->np * g->N * 2 * g->elem) *
                              g->B +
-                         mdft::reduction_scratch_bytes() + 8 * g->no;
+                         mdft::reduction_scratch_bytes() * g->B + 8 * g->no;
   // a rough bound on the plans before building them: the R(q) table and
   // pair data dominate (about 1 KB per grid point at mmax <= 6)
   const size_t plan_guess = (size_t)g->N * 1024;
@@ -347,9 +352,10 @@ Group* mdft_server_s::group_for(const Job& j) {
     g->hs.alloc(f64b / 2 * kHistory * g->B, "server arena");
     g->hy.alloc(f64b / 2 * kHistory * g->B, "server arena");
     g->S.alloc(sizeof(double) * mdft::Lbfgs::nscalars(kHistory) * g->B, "server arena");
-    g->red.alloc(mdft::reduction_scratch_bytes(), "server arena");
-    ck(cudaMemset(g->red.p, 0, mdft::reduction_scratch_bytes()), "scratch reset");
+    g->red.alloc(mdft::reduction_scratch_bytes() * g->B, "server arena");  // one per slot
+    ck(cudaMemset(g->red.p, 0, mdft::reduction_scratch_bytes() * g->B), "scratch reset");
     ck(cudaHostAlloc((void**)&g->tails, sizeof(double) * 8 * g->B, cudaHostAllocDefault), "page-locked tails");
+    g->lbr.rounds = true;
     g->lb.resize(g->B);
     g->model = sv;
     g->eg = mdft::EgConst{sv.kT, sv.rho0, (j.len[0] / j.n[0]) * (j.len[1] / j.n[1]) * (j.len[2] / j.n[2]),
@@ -364,6 +370,7 @@ Group* mdft_server_s::group_for(const Job& j) {
   g->bytes = free0 > free1 ? free0 - free1 : arena;
   in_use += g->bytes;
   if (in_use > peak.load()) peak.store(in_use);
+  precapture(*g);
   Group* raw = g.get();
   groups.emplace(key, std::move(g));
   n_groups.store((int)groups.size());
@@ -448,16 +455,15 @@ void enqueue_solve_step(Group& g, int k) {
   mdft::detail::angl2proj_fields(g.opt, xin, true, g.rho0, g.p.p, k, s);
   mdft::detail::execute_fields(g.conv, g.p.p, k, s);
   mdft::detail::proj2angl_fields(g.opt, g.p.p, g.vexc.p, k, s);
+  // every slot's energy, gradient and preconditioner in one launch, then the
+  // slots' scalar tails (8 doubles each, one scalar block apart) in one copy
   const int ns = mdft::Lbfgs::nscalars(kHistory);
-  for (int j = 0; j < k; ++j) {
-    double* S = g.S.as<double>() + (size_t)ns * j;
-    mdft::energy_grad(g.eg, g.xt.as<double>() + n * j, g.vexc.as<unsigned char>() + n * g.elem * j, g.elem == 4,
-                      g.vext.as<double>() + n * j, g.w.as<double>(), g.gt.as<double>() + n * j, (long long)n, g.no,
-                      S + mdft::Lbfgs::energy_at(kHistory), g.red.p, g.hinv.as<float>() + n * j, s);
-    ck(cudaMemcpyAsync(g.tails + 8 * j, S + mdft::Lbfgs::tail_at(kHistory), 8 * sizeof(double),
-                       cudaMemcpyDeviceToHost, s),
-       "minimiser tail read-back");
-  }
+  mdft::energy_grad(g.eg, g.xt.as<double>(), g.vexc.p, g.elem == 4, g.vext.as<double>(), g.w.as<double>(),
+                    g.gt.as<double>(), (long long)n, g.no, g.S.as<double>() + mdft::Lbfgs::energy_at(kHistory),
+                    g.red.p, g.hinv.as<float>(), s, k, ns);
+  ck(cudaMemcpy2DAsync(g.tails, 8 * sizeof(double), g.S.as<double>() + mdft::Lbfgs::tail_at(kHistory),
+                       sizeof(double) * ns, 8 * sizeof(double), k, cudaMemcpyDeviceToHost, s),
+     "minimiser tail read-back");
 }
 
 void mdft_server_s::enqueue_step(Group& g, int k) {
@@ -499,6 +505,29 @@ void mdft_server_s::enqueue_step(Group& g, int k) {
     descent_kernel<float><<<nb, 256, 0, s>>>(g.xi.as<float>(), g.df.as<float>(), g.alpha.as<double>(), per_field,
                                              n);
   mdft::launch_check("server descent kernel launch");
+}
+
+// Captures the step graph of every active count 1..B of a new group, so that
+// no capture or instantiation lands in a running job's step; a count whose
+// capture fails runs directly (first step) and is tried again in step().
+void mdft_server_s::precapture(Group& g) {
+  for (int k = 1; k <= g.B; ++k) {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool ok = cudaStreamBeginCapture(g.stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+      try {
+        enqueue_step(g, k);
+      } catch (const Error&) {
+        ok = false;
+      }
+      ok = (cudaStreamEndCapture(g.stream, &graph) == cudaSuccess) && ok && graph;
+      ok = ok && cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+      if (graph) cudaGraphDestroy(graph);
+    }
+    cudaGetLastError();
+    if (ok) g.graphs[k] = exec;
+  }
 }
 
 void mdft_server_s::step(Group& g) {

@@ -372,8 +372,11 @@ struct EgArgs {
   float ln2h, ln2l;
   float ah[10], al[10];          // 1 / (2k + 1), k = 0..9
   double* out;  // [E_total, E_id, E_ext, E_exc, max |g|]
-  double* part;
-  unsigned* counter;
+  // reduction scratch of field 0: (CTAs, 7) doubles, then at counter_off
+  // the completion counter; field f's at f scratch_stride bytes further
+  void* scratch;
+  size_t counter_off, scratch_stride;
+  long long out_stride;  // doubles between the fields' out blocks
   // 1 / D with D = 2 rho0 dv w kT max(ln xi^2 + 2 + vext/kT, 1): the local
   // terms' curvature d^2/dxi^2 (E_id + E_ext), floored at half its value at
   // their minimum -- the minimiser's diagonal preconditioner (may be null)
@@ -466,7 +469,14 @@ __global__ void __launch_bounds__(kRedThreads, 4) eg_kernel(const EgArgs A) {
     wf[i] = make_float2(d.hi, d.lo);
   }
   __syncthreads();
-  const TV* vx = static_cast<const TV*>(A.vexc);
+  // field blockIdx.y of a batch: its arrays start at y n, its outputs and
+  // scratch at their strides
+  const long long fo = (long long)blockIdx.y * A.n;
+  const double* __restrict__ xi = A.xi + fo;
+  const TV* __restrict__ vx = static_cast<const TV*>(A.vexc) + fo;
+  const double* __restrict__ vext = A.vext ? A.vext + fo : nullptr;
+  double* __restrict__ gout = A.g + fo;
+  float* __restrict__ hinv = A.hinv ? A.hinv + fo : nullptr;
   const double c_id = A.kT * A.rho0 * A.dv, c_ext = A.rho0 * A.dv, c_exc = A.prefactor * A.rho0;
   const DF kT(A.kh, A.kl), cext(A.ch, A.cl), cexc2(A.xh, A.xl), one(1.f, 0.f);
   // preconditioner constants (the preconditioner only scales search
@@ -489,17 +499,17 @@ __global__ void __launch_bounds__(kRedThreads, 4) eg_kernel(const EgArgs A) {
   double xn = 0.0, ven = 0.0;
   TV vn = TV(0);
   if (i < A.n) {
-    xn = A.xi[i];
+    xn = xi[i];
     vn = vx[i];
-    ven = A.vext ? A.vext[i] : 0.0;
+    ven = vext ? vext[i] : 0.0;
   }
   for (; i < A.n; i += stride) {
     const double x = xn, ve = ven;
     const TV vv = vn;
     if (i + stride < A.n) {
-      xn = A.xi[i + stride];
+      xn = xi[i + stride];
       vn = vx[i + stride];
-      ven = A.vext ? A.vext[i + stride] : 0.0;
+      ven = vext ? vext[i + stride] : 0.0;
     }
     const unsigned ebits = (unsigned)(bits_of(x) >> 52) & 0x7ffu;
     double gi;
@@ -512,16 +522,16 @@ __global__ void __launch_bounds__(kRedThreads, 4) eg_kernel(const EgArgs A) {
       acc_mac(a_exc, wd, vd * q.t);
       const DF inner = cext * (kT * q.L + ved) + cexc2 * vd;
       gi = df_to_double(twice(df_from_double_bits(x) * wd) * inner);
-      if (A.hinv) A.hinv[i] = __fdividef(1.f, wd.hi * c2k * fmaxf(q.L.hi + 2.f + ved.hi * ikT, 1.f));
+      if (hinv) hinv[i] = __fdividef(1.f, wd.hi * c2k * fmaxf(q.L.hi + 2.f + ved.hi * ikT, 1.f));
     } else {
       const Terms64 tt = terms_f64(x, ws[o], (double)vv, ve, A);
       d_id += tt.id;
       d_ext += tt.ext;
       d_exc += tt.exc;
       gi = tt.g;
-      if (A.hinv) A.hinv[i] = tt.hinv;
+      if (hinv) hinv[i] = tt.hinv;
     }
-    A.g[i] = gi;
+    gout[i] = gi;
     const unsigned long long gb = bits_of(gi) & 0x7fffffffffffffffull;
     gmax = gb > gmax ? gb : gmax;
     o += ostep;
@@ -532,8 +542,9 @@ __global__ void __launch_bounds__(kRedThreads, 4) eg_kernel(const EgArgs A) {
   r.s[1] = dd_plus(Dd{c_ext * df_to_double(acc_get(a_ext)), 0.0}, c_ext * d_ext);
   r.s[2] = dd_plus(Dd{c_exc * df_to_double(acc_get(a_exc)), 0.0}, c_exc * d_exc);
   r.mx = double_of(gmax);
-  double* out = A.out;
-  grid_reduce<3>(r, A.part, A.counter, [out](const Red<3>& tt) {
+  double* out = A.out + (long long)blockIdx.y * A.out_stride;
+  unsigned char* scr = static_cast<unsigned char*>(A.scratch) + (size_t)blockIdx.y * A.scratch_stride;
+  grid_reduce<3>(r, reinterpret_cast<double*>(scr), reinterpret_cast<unsigned*>(scr + A.counter_off), [out](const Red<3>& tt) {
     const double id = tt.s[0].hi + tt.s[0].lo, ext = tt.s[1].hi + tt.s[1].lo, exc = tt.s[2].hi + tt.s[2].lo;
     const Dd tot = dd_plus(dd_plus(tt.s[0], tt.s[1]), tt.s[2]);
     out[0] = tot.hi + tot.lo;
@@ -876,80 +887,117 @@ __device__ void lb_elements(const LbOp& opr, const LbSlot& slr, long long i0, lo
   }
 }
 
+// element work of item `it` (chunk c of field j) in round r; its chunk sums
+// go to part[it]
+__device__ __forceinline__ void lb_item(const LbBatch& B, int r, long long it, float2* __restrict__ part) {
+  const int j = (int)(it / kLbChunks), c = (int)(it % kLbChunks);
+  const LbSlot& sl = B.slot[j];
+  if (r >= sl.nops) return;
+  const LbOp& op = B.op[sl.op0 + r];
+  const long long len = lb_chunk_len(sl.n);
+  const long long i0 = min(sl.n, (long long)c * len), i1 = min(sl.n, i0 + len);
+  Acc<DF> a0, a1;
+  acc_zero(a0);
+  acc_zero(a1);
+  lb_elements(op, sl, i0, i1, a0, a1);
+  if (lb_dots(op)) {
+    DF v[2] = {acc_get(a0), acc_get(a1)};
+    lb_block_sum<2>(v);
+    if (threadIdx.x == 0) {
+      part[it * 2] = make_float2(v[0].hi, v[0].lo);
+      part[it * 2 + 1] = make_float2(v[1].hi, v[1].lo);
+    }
+  }
+}
+
+// field j's sums of round r from its chunk sums, in chunk order (thread t
+// adds chunks kLbPerThread t .. kLbPerThread (t + 1) - 1, then the block sum),
+// and the scalars they set
+__device__ __forceinline__ void lb_field_sums(const LbBatch& B, int r, int j, const float2* __restrict__ part) {
+  const int tid = threadIdx.x;
+  const LbSlot& sl = B.slot[j];
+  if (r >= sl.nops) return;
+  const LbOp& op = B.op[sl.op0 + r];
+  if (!lb_dots(op)) return;
+  DF v[2] = {DF(0.f, 0.f), DF(0.f, 0.f)};
+#pragma unroll
+  for (int q = 0; q < kLbPerThread; ++q) {
+    const long long c = (long long)j * kLbChunks + tid * kLbPerThread + q;
+    const float2 q0 = __ldcg(&part[c * 2]), q1 = __ldcg(&part[c * 2 + 1]);
+    v[0] = v[0] + DF(q0.x, q0.y);
+    v[1] = v[1] + DF(q1.x, q1.y);
+  }
+  lb_block_sum<2>(v);
+  if (tid == 0) {
+    double* S = sl.S;
+    const double t0 = df_to_double(v[0]), t1 = df_to_double(v[1]);
+    if (op.type == kOpPass) {
+      const double scale = (op.js1 >= 0 ? S[op.js1] : op.sc0) * (op.js2 >= 0 ? S[op.js2] : 1.0);
+      S[op.out] = scale * t0;
+    } else {
+      S[op.out] = t0;
+      S[op.out + 1] = t1;
+      const bool good = t1 > 0.0 && t0 > 1e-12 * t1;
+      S[op.i1] = good ? 1.0 / t0 : 0.0;
+      if (good) S[op.i2] = t0 / t1;
+    }
+    __threadfence();
+  }
+}
+
+__device__ __forceinline__ bool lb_round_dots(const LbBatch& B, int r) {
+  for (int j = 0; j < B.nslots; ++j)
+    if (r < B.slot[j].nops && lb_dots(B.op[B.slot[j].op0 + r])) return true;
+  return false;
+}
+
+// Persistent form: every round of every field in one cooperative launch, the
+// rounds and their sums separated by the bounded grid barrier.
 __global__ void __launch_bounds__(kRedThreads) lbfgs_batch_kernel(const __grid_constant__ LbBatch B,
                                                                    float2* __restrict__ part, unsigned* bar,
                                                                    int* err, int* flag) {
-  const int tid = threadIdx.x;
   const long long items = (long long)B.nslots * kLbChunks;
   bool ok = true;
   for (int r = 0; r < B.maxops && ok; ++r) {
-    bool any_dot = false;
-    for (int j = 0; j < B.nslots; ++j)
-      if (r < B.slot[j].nops && lb_dots(B.op[B.slot[j].op0 + r])) any_dot = true;
-    // ---- element phase: chunk c of field j, every element once ----
-    for (long long it = blockIdx.x; it < items; it += gridDim.x) {
-      const int j = (int)(it / kLbChunks), c = (int)(it % kLbChunks);
-      const LbSlot& sl = B.slot[j];
-      if (r >= sl.nops) continue;
-      const LbOp& op = B.op[sl.op0 + r];
-      const long long len = lb_chunk_len(sl.n);
-      const long long i0 = min(sl.n, (long long)c * len), i1 = min(sl.n, i0 + len);
-      Acc<DF> a0, a1;
-      acc_zero(a0);
-      acc_zero(a1);
-      lb_elements(op, sl, i0, i1, a0, a1);
-      if (lb_dots(op)) {
-        DF v[2] = {acc_get(a0), acc_get(a1)};
-        lb_block_sum<2>(v);
-        if (tid == 0) {
-          part[(it)*2] = make_float2(v[0].hi, v[0].lo);
-          part[(it)*2 + 1] = make_float2(v[1].hi, v[1].lo);
-        }
-      }
-    }
+    for (long long it = blockIdx.x; it < items; it += gridDim.x) lb_item(B, r, it, part);
     if (!lb_grid_sync(bar, gridDim.x)) {
       ok = false;
       break;
     }
-    if (!any_dot) continue;
-    // ---- sums: field j's chunk sums in chunk order, one CTA per field; thread
-    // t adds chunks kLbPerThread t .. kLbPerThread (t + 1) - 1 in order ----
-    for (int j = blockIdx.x; j < B.nslots; j += gridDim.x) {
-      const LbSlot& sl = B.slot[j];
-      if (r >= sl.nops) continue;
-      const LbOp& op = B.op[sl.op0 + r];
-      if (!lb_dots(op)) continue;
-      DF v[2] = {DF(0.f, 0.f), DF(0.f, 0.f)};
-#pragma unroll
-      for (int q = 0; q < kLbPerThread; ++q) {
-        const long long c = (long long)j * kLbChunks + tid * kLbPerThread + q;
-        const float2 q0 = __ldcg(&part[c * 2]), q1 = __ldcg(&part[c * 2 + 1]);
-        v[0] = v[0] + DF(q0.x, q0.y);
-        v[1] = v[1] + DF(q1.x, q1.y);
-      }
-      lb_block_sum<2>(v);
-      if (tid == 0) {
-        double* S = sl.S;
-        const double t0 = df_to_double(v[0]), t1 = df_to_double(v[1]);
-        if (op.type == kOpPass) {
-          const double scale = (op.js1 >= 0 ? S[op.js1] : op.sc0) * (op.js2 >= 0 ? S[op.js2] : 1.0);
-          S[op.out] = scale * t0;
-        } else {
-          S[op.out] = t0;
-          S[op.out + 1] = t1;
-          const bool good = t1 > 0.0 && t0 > 1e-12 * t1;
-          S[op.i1] = good ? 1.0 / t0 : 0.0;
-          if (good) S[op.i2] = t0 / t1;
-        }
-        __threadfence();
-      }
-    }
+    if (!lb_round_dots(B, r)) continue;
+    for (int j = blockIdx.x; j < B.nslots; j += gridDim.x) lb_field_sums(B, r, j, part);
     if (!lb_grid_sync(bar, gridDim.x)) {
       ok = false;
       break;
     }
   }
-  if (!ok && blockIdx.x == 0 && tid == 0) note_wait_timeout(err, flag);
+  if (!ok && blockIdx.x == 0 && threadIdx.x == 0) note_wait_timeout(err, flag);
+}
+
+// Round form: one ordinary launch per round, the op program in device memory.
+// The last CTA to finish the round's element work (completion counter) adds
+// every field's sums, exactly as the persistent form does, and clears the
+// counter; the next round's launch then reads them.  No CTA waits for
+// another, so the launch needs no co-residency and shares the GPU with other
+// streams' kernels.
+__global__ void __launch_bounds__(kRedThreads) lbfgs_round_kernel(const LbBatch* __restrict__ Bp, int r,
+                                                                   float2* __restrict__ part,
+                                                                   unsigned* __restrict__ counter) {
+  const LbBatch& B = *Bp;
+  const long long items = (long long)B.nslots * kLbChunks;
+  for (long long it = blockIdx.x; it < items; it += gridDim.x) lb_item(B, r, it, part);
+  if (!lb_round_dots(B, r)) return;
+  __shared__ bool last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  for (int j = 0; j < B.nslots; ++j) lb_field_sums(B, r, j, part);
+  if (threadIdx.x == 0) *counter = 0u;
 }
 
 __global__ void __launch_bounds__(kRedThreads) grid_barrier_selftest_kernel(unsigned* bar, unsigned missing,
@@ -1125,7 +1173,8 @@ void vext_compute(const Grid& g, const double* sv_sites, int n_solvent, const do
 
 void energy_grad(const EgConst& c, const double* xi, const void* vexc, bool vexc_f32, const double* vext,
                  const double* w, double* grad, long long n, int no, double* out, void* scratch, float* hinv,
-                 cudaStream_t s) {
+                 cudaStream_t s, int nf, long long out_stride) {
+  throw_if(nf < 1 || nf > 65535, "internal: energy batch size", 4);
   EgArgs A{};
   A.hinv = hinv;
   A.xi = xi;
@@ -1149,14 +1198,19 @@ void energy_grad(const EgConst& c, const double* xi, const void* vexc, bool vexc
   split(0.693147180559945309417232121458176568L, A.ln2h, A.ln2l);
   for (int k = 0; k < 10; ++k) split(1.0L / (2 * k + 1), A.ah[k], A.al[k]);
   A.out = out;
-  A.part = static_cast<double*>(scratch);
-  A.counter = reinterpret_cast<unsigned*>(static_cast<double*>(scratch) + kRedBlocks * 7);
+  A.out_stride = out_stride;
+  A.scratch = scratch;
+  A.counter_off = sizeof(double) * kRedBlocks * 7;
+  A.scratch_stride = reduction_scratch_bytes();
   const size_t smem = (sizeof(double) + sizeof(float2)) * (size_t)no;
   throw_if(smem > 48 * 1024, "too many orientations for the energy kernel", MDFT_ERR_UNSUPPORTED);
+  // the grid of each field depends on n only: a field's sums are the same
+  // alone and in a batch
+  const dim3 grid(red_blocks(n, 152 * 4), nf);
   if (vexc_f32)
-    eg_kernel<float><<<red_blocks(n, 152 * 4), kRedThreads, smem, s>>>(A);
+    eg_kernel<float><<<grid, kRedThreads, smem, s>>>(A);
   else
-    eg_kernel<double><<<red_blocks(n, 152 * 4), kRedThreads, smem, s>>>(A);
+    eg_kernel<double><<<grid, kRedThreads, smem, s>>>(A);
   launch_ok("energy kernel launch");
 }
 
@@ -1326,21 +1380,42 @@ void LbRunner::init() {
   cuda_check(cudaMemset(buf.ptr, 0, part + 64), "L-BFGS batch state reset");
   int dev = 0, nsm = 0, per = 0, coop = 0;
   cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "SM count");
+  if (rounds) {
+    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lbfgs_round_kernel, kRedThreads, 0),
+               "L-BFGS round occupancy");
+    throw_if(per < 1, "internal: the L-BFGS round kernel does not fit an SM", 4);
+    prog.alloc(sizeof(LbBatch));
+    blocks = nsm * per;  // one wave
+    return;
+  }
   cuda_check(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev), "cooperative launch attribute");
   throw_if(!coop, "the device does not support cooperative launches", 4);
-  cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev), "SM count");
   cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lbfgs_batch_kernel, kRedThreads, 0),
              "L-BFGS batch occupancy");
   throw_if(per < 1, "internal: the L-BFGS batch kernel does not fit an SM", 4);
-  // two CTAs per SM at most: enough loads in flight, and room left for the
-  // other groups' kernels while the batch waits at its barriers
+  // two CTAs per SM at most: enough loads in flight with the vector loads
   blocks = nsm * std::min(per, 2);
 }
 
 namespace {
-void lb_launch(const LbBatch& B, LbRunner& r, cudaStream_t s) {
+void lb_launch(LbBatch& B, int nop, LbRunner& r, cudaStream_t s) {
   const size_t part = sizeof(float2) * 2 * (size_t)kLbMaxSlots * kLbChunks;
   unsigned* bar = reinterpret_cast<unsigned*>(static_cast<unsigned char*>(r.buf.ptr) + part);
+  if (r.rounds) {
+    // the program's used part; from pageable memory, so B may change as soon
+    // as the call returns
+    const size_t bytes = offsetof(LbBatch, op) + sizeof(LbOp) * (size_t)nop;
+    cuda_check(cudaMemcpyAsync(r.prog.ptr, &B, bytes, cudaMemcpyHostToDevice, s), "L-BFGS program upload");
+    const long long items = (long long)B.nslots * kLbChunks;
+    const unsigned grid = (unsigned)std::min<long long>(items, r.blocks);
+    float2* pp = static_cast<float2*>(r.buf.ptr);
+    clear_stale_error();
+    for (int k = 0; k < B.maxops; ++k)
+      lbfgs_round_kernel<<<grid, kRedThreads, 0, s>>>(static_cast<const LbBatch*>(r.prog.ptr), k, pp, bar);
+    launch_ok("L-BFGS round launch");
+    return;
+  }
   cuda_check(cudaMemsetAsync(bar, 0, 16, s), "grid barrier reset");
   const WaitStatus& w = device_wait_status();
   float2* pp = static_cast<float2*>(r.buf.ptr);
@@ -1361,7 +1436,7 @@ void lbfgs_run(Lbfgs* const* lbs, int k, LbRunner& r, cudaStream_t s) {
   B.maxops = 0;
   int nop = 0;
   auto flush = [&] {
-    if (B.nslots) lb_launch(B, r, s);
+    if (B.nslots) lb_launch(B, nop, r, s);
     B.nslots = 0;
     B.maxops = 0;
     nop = 0;
@@ -1564,6 +1639,13 @@ int mdft_solver_minimize(mdft_solver_t h, double* xi, int max_iter, double gtol,
     const std::vector<double>& tr = h->lb.trace();
     if (trace) std::memcpy(trace, tr.data(), sizeof(double) * std::min(tr.size(), (size_t)5 * (max_iter + 1)));
     if (iterations) *iterations = h->lb.iterations();
+  });
+}
+
+int mdft_solver_status(mdft_solver_t h, int* status) {
+  return solver_guard([&] {
+    throw_if(!h || !status, "NULL argument");
+    *status = (int)h->lb.status();
   });
 }
 

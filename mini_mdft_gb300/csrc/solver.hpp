@@ -22,11 +22,14 @@ void vext_compute(const Grid& g, const double* solvent_sites, int n_solvent, con
 // E and dE/dxi at xi: gradient to grad, [E_total, E_id, E_ext, E_exc,
 // max |g|] to out (device), and (hinv not null) the inverse of the local
 // terms' curvature, floored, as the minimiser's diagonal preconditioner.  vexc is double, or float when vexc_f32; vext
-// may be null.  part / counter: reduction scratch (reduction_scratch_bytes,
-// the counter zero, left zero).
+// may be null.  scratch: reduction scratch (reduction_scratch_bytes, zeroed
+// once, left zeroed).  nf > 1: nf fields in one launch, field f's arrays at
+// f n elements, its out block at f out_stride doubles, its scratch at f
+// reduction_scratch_bytes() bytes; each field's sums are the ones it gets
+// alone.
 void energy_grad(const EgConst& c, const double* xi, const void* vexc, bool vexc_f32, const double* vext,
                  const double* w, double* grad, long long n, int no, double* out, void* scratch, float* hinv,
-                 cudaStream_t s);
+                 cudaStream_t s, int nf = 1, long long out_stride = 0);
 size_t reduction_scratch_bytes();
 
 // xi (double) -> float copy of n values
@@ -58,8 +61,15 @@ struct LbOp {
 // Device state of a batch launch: the partial sums and the grid barrier.
 class Lbfgs;
 struct LbRunner {
-  DevBuf buf;  // partial sums, then the barrier words (count, generation, abort)
+  DevBuf buf;   // partial sums, then the barrier words (count, generation, abort)
+  DevBuf prog;  // round form: the op program in device memory
   int blocks = 0;
+  // false: one persistent cooperative launch per run (the bounded grid
+  // barrier between rounds); true: one ordinary launch per round, for callers
+  // whose launches share the GPU with other streams' work (a cooperative
+  // launch waits until every SM has room for its CTAs).  Same sums, same
+  // order: both forms give identical results.
+  bool rounds = false;
   void init();  // on the current device, outside stream capture
 };
 // Runs the queued operations of k fields' minimisers (on_eval since their

@@ -87,6 +87,9 @@ def test_solver_argument_checks(L):
     it = C.c_int()
     assert L.mdft_solver_minimize(None, FAKE, 1, 0.0, 0.0, _dp(trace), C.byref(it), None) == 1
     assert "NULL argument" in _err(L)
+    st = C.c_int(7)
+    assert L.mdft_solver_status(None, C.byref(st)) == 1
+    assert "NULL argument" in _err(L) and st.value == 7
     assert L.mdft_solver_destroy(None) == 0
 
 

@@ -133,10 +133,18 @@ def test_minimizer_reaches_boltzmann_density_without_excess(gpu_lib):
     xi = torch.ones_like(vext)
     solver = M.Solver(opt, conv, vext, kT=kT, rho0=rho0, prefactor=pref)
     # near max |g| ~ 1e-7 the energy decrease of a step (~1e-12) reaches the
-    # rounding of E (~2e3 here, spacing 4.5e-13) and the run stops there;
-    # 1e-6 bounds |ln xi - ln xi_B| by ~1e-4
+    # rounding of E (~2e3 here, spacing 4.5e-13), so the run may stop there
+    # before gtol; 1e-6 bounds |ln xi - ln xi_B| by ~1e-4
+    assert solver.status() == -1  # never run
     trace = solver.minimize(xi, max_iter=300, gtol=1e-10)
     assert trace[-1, 4] <= 1e-6
+    # it ends at gtol or at the rounding floor, not at the iteration cap
+    assert M.Solver.STATUS[solver.status()] in ("gtol", "flat", "no_decrease")
+    if solver.status() == 0:
+        assert trace[-1, 4] <= 1e-10
+    assert len(trace) - 1 < 300
+    solver.minimize(xi, max_iter=1, gtol=0.0)
+    assert M.Solver.STATUS[solver.status()] in ("max_iter", "flat", "no_decrease")
     assert np.all(np.diff(trace[:, 0]) <= 0)
     # E depends on xi^2 only (rho = rho0 xi^2): a step may cross to -xi
     xb = torch.exp(-vext / (2 * kT))

@@ -3,7 +3,8 @@ cannot allocate device memory during their solve (e.g. an application whose
 pool allocator owns the whole GPU, or a loop that must not pay for an
 allocation call).  Its scratch is a fixed array inside the library, so it
 must give what mdft_get_delta_f gives, call after call, and draw nothing from
-the device's stream-ordered memory pool (the pool mdft_get_delta_f takes its
+a stream-ordered memory pool: neither the device's default pool nor the
+library's own (mdft_scratch_pool, the pool mdft_get_delta_f takes its
 temporary from).
 
 Collected last (file name) so that a run stopping at the first failure has
@@ -33,15 +34,18 @@ def _run(L, fn, xi, vexc, w, df, ff, prec, stream):
 
 
 class _PoolWatermark:
-    """High-water mark of the current device's stream-ordered memory pool
-    (the one cudaMallocAsync draws from), read through the driver API."""
+    """High-water mark of a stream-ordered memory pool, read through the
+    driver API: the current device's default pool (the one cudaMallocAsync
+    draws from), or the given one."""
 
-    def __init__(self):
+    def __init__(self, pool=None):
         self.cu = C.CDLL("libcuda.so.1")
-        dev = C.c_int(0)
-        assert self.cu.cuCtxGetDevice(C.byref(dev)) == 0
-        self.pool = C.c_void_p(0)
-        assert self.cu.cuDeviceGetMemPool(C.byref(self.pool), dev) == 0
+        if pool is None:
+            dev = C.c_int(0)
+            assert self.cu.cuCtxGetDevice(C.byref(dev)) == 0
+            pool = C.c_void_p(0)
+            assert self.cu.cuDeviceGetMemPool(C.byref(pool), dev) == 0
+        self.pool = pool
 
     def reset(self):
         zero = C.c_uint64(0)
@@ -57,8 +61,9 @@ class _PoolWatermark:
 def test_noalloc_matches_allocating_entry_point_twice(gpu_lib, prec):
     """FP64 (0), FP32 (1) and double-float on FP64 fields (2): two calls in a
     row through the fixed scratch give the allocating call's df bit for bit
-    and its ff; the pool's high-water mark stays zero across them, and a
-    positive control shows the allocating call does move it."""
+    and its ff; the high-water marks of the default pool and of the
+    library's pool stay zero across them, and a positive control shows the
+    allocating call does move the library pool's."""
     import torch
     L = gpu_lib.lib()
     dt = torch.float32 if prec == 1 else torch.float64
@@ -68,25 +73,29 @@ def test_noalloc_matches_allocating_entry_point_twice(gpu_lib, prec):
     vexc = torch.from_numpy(rng.uniform(-1.0, 1.0, shape)).to("cuda", dt)
     w = torch.from_numpy(rng.uniform(0.0, 1.0, 84)).to("cuda", torch.float64)
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
-    pool = _PoolWatermark()
+    lp = C.c_void_p()
+    assert L.mdft_scratch_pool(C.byref(lp)) == 0 and lp.value
+    pools = (_PoolWatermark(), _PoolWatermark(lp))
 
     df_ref = torch.zeros_like(xi)
     ff_ref = torch.zeros(1, dtype=torch.float64, device="cuda")
     torch.cuda.synchronize()
-    pool.reset()
+    for pool in pools:
+        pool.reset()
     assert _run(L, L.mdft_get_delta_f, xi, vexc, w, df_ref, ff_ref, prec, stream) == 0
     torch.cuda.synchronize()
-    assert pool.high() > 0  # the allocating entry point draws its temporary from the pool
+    assert pools[1].high() > 0  # the allocating entry point draws its temporary from the library's pool
 
     for _ in range(2):  # two calls in a row share the fixed scratch
         df = torch.full_like(xi, 7.0)
         ff = torch.full((1,), 7.0, dtype=torch.float64, device="cuda")
         torch.cuda.synchronize()
-        pool.reset()
+        for pool in pools:
+            pool.reset()
         assert _run(L, L.mdft_get_delta_f_noalloc, xi, vexc, w, df, ff, prec, stream) == 0, \
             L.mdft_last_error()
         torch.cuda.synchronize()
-        assert pool.high() == 0
+        assert all(pool.high() == 0 for pool in pools)
         assert torch.equal(df, df_ref)
         a, b = float(ff.item()), float(ff_ref.item())
         assert abs(a - b) <= 1e-12 * abs(b)
