@@ -17,6 +17,8 @@
 //     per point so that the per-thread rows are read bank-conflict-free.
 // S is the storage type of the fields, C the arithmetic type.
 #pragma once
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace mdft {
@@ -84,9 +86,25 @@ __device__ __forceinline__ Cx<C> ldtw(const void* t, int i) {
   return static_cast<const Cx<C>*>(t)[i];
 }
 
-// FP32: at most 128 registers so that two 256-thread CTAs share an SM
+// Double-float at mmax >= 4: the per-(point, theta) DFT stages would keep a
+// whole (phi, psi) row of complex double-float values in registers (up to
+// 255 per thread, one CTA per SM); they are split instead into a psi stage
+// and a phi stage, one thread per row or column, passing the values through
+// shared memory in place.  Every output is formed by the same operations in
+// the same order, so results do not change.
+template <typename C, int MMAX>
+constexpr bool split_dft() {
+  return std::is_same<C, DF>::value && MMAX >= 4;
+}
+// CTAs per SM the kernels are compiled for (launch bounds): FP32 and the
+// split stages keep within 128 registers so that two CTAs share an SM
+template <typename C, int MMAX>
+constexpr int ang_min_blocks() {
+  return (sizeof(C) == 4 || split_dft<C, MMAX>()) ? 2 : 1;
+}
+
 template <typename S, typename C, int MMAX, int MRSO, bool FROM_XI>
-__global__ void __launch_bounds__(A2P_THREADS, sizeof(C) == 4 ? 2 : 1)
+__global__ void __launch_bounds__(A2P_THREADS, (ang_min_blocks<C, MMAX>()))
 angl2proj_fast_kernel(const AngPlan P, const S* __restrict__ o, Cx<S>* __restrict__ p, C rho0) {
   using Sh = Shape<MMAX, MRSO>;
   constexpr int PTS = pts_per_cta<C, MMAX, MRSO>();
@@ -128,6 +146,92 @@ angl2proj_fast_kernel(const AngPlan P, const S* __restrict__ o, Cx<S>* __restric
   }
   __syncthreads();
 
+  if constexpr (split_dft<C, MMAX>()) {
+    // psi DFT, one thread per (point, theta, phi row): Y(f, kpsi) into the
+    // Z tile at [theta][kpsi][f][point]
+    for (int w = tid; w < NT * NPHI * PTS; w += blockDim.x) {
+      const int tf = w / PTS, q = w - tf * PTS;
+      if (q >= cnt) continue;
+      const int th = tf / NPHI, f = tf - th * NPHI;
+      const C* r = ot + q * LDO + th * NPHI * NPSI + f * NPSI;
+      Cx<C>* zy = Zs + ((size_t)th * (K + 1) * NPHI + f) * PTS + q;
+      C s0 = r[0];
+#pragma unroll
+      for (int j = 1; j < NPSI; ++j) s0 = s0 + r[j];
+      zy[0] = mkc<C>(s0, C(0));
+#pragma unroll
+      for (int k = 1; k <= K; ++k) {
+        Acc<C> re, im;
+        acc_set(re, r[0]);
+        acc_zero(im);
+#pragma unroll
+        for (int j = 1; j <= HPSI; ++j) {
+          const Cx<C> t = ldtw<C>(P.tw_psi, (k * j) % NPSI);
+          acc_mac(re, r[j] + r[NPSI - j], t.re);
+          acc_mac(im, r[j] - r[NPSI - j], t.im);
+        }
+        zy[(size_t)k * NPHI * PTS] = mkc<C>(acc_get(re), acc_get(im));
+      }
+    }
+    __syncthreads();
+    // phi DFT, one thread per (point, theta, kpsi): reads its column Y(., kpsi)
+    // and writes the outputs over the same slots
+    for (int w = tid; w < NT * (K + 1) * PTS; w += blockDim.x) {
+      const int tk = w / PTS, q = w - tk * PTS;
+      if (q >= cnt) continue;
+      const int th = tk / (K + 1), kp = tk - th * (K + 1);
+      Cx<C>* zk = Zs + (size_t)(th * (K + 1) + kp) * NPHI * PTS + q;
+      Cx<C> Yc[NPHI];
+#pragma unroll
+      for (int f = 0; f < NPHI; ++f) Yc[f] = zk[(size_t)f * PTS];
+      if (kp == 0) {  // real input, X(n-k) = conj(X(k))
+        C s0 = Yc[0].re;
+#pragma unroll
+        for (int j = 1; j < NPHI; ++j) s0 = s0 + Yc[j].re;
+        zk[(0 + MMAX) * PTS] = mkc<C>(s0, C(0));
+#pragma unroll
+        for (int k = 1; k <= HPHI; ++k) {
+          Acc<C> are, aim;
+          acc_set(are, Yc[0].re);
+          acc_zero(aim);
+#pragma unroll
+          for (int j = 1; j <= HPHI; ++j) {
+            const Cx<C> t = ldtw<C>(P.tw_phi, (k * j) % NPHI);
+            acc_mac(are, Yc[j].re + Yc[NPHI - j].re, t.re);
+            acc_mac(aim, Yc[j].re - Yc[NPHI - j].re, t.im);
+          }
+          const C re = acc_get(are), im = acc_get(aim);
+          zk[(k + MMAX) * PTS] = mkc<C>(re, -im);
+          zk[(-k + MMAX) * PTS] = mkc<C>(re, im);
+        }
+      } else {  // complex input, pair k with n - k
+        Cx<C> s0 = Yc[0];
+#pragma unroll
+        for (int j = 1; j < NPHI; ++j) s0 = s0 + Yc[j];
+        zk[(0 + MMAX) * PTS] = conj(s0);
+#pragma unroll
+        for (int k = 1; k <= HPHI; ++k) {
+          Acc<C> pr, pi, qr, qi;
+          acc_set(pr, Yc[0].re);
+          acc_set(pi, Yc[0].im);
+          acc_zero(qr);
+          acc_zero(qi);
+#pragma unroll
+          for (int j = 1; j <= HPHI; ++j) {
+            const Cx<C> t = ldtw<C>(P.tw_phi, (k * j) % NPHI);
+            const Cx<C> A = Yc[j] + Yc[NPHI - j], B = Yc[j] - Yc[NPHI - j];
+            acc_mac(pr, A.re, t.re);
+            acc_mac(pi, A.im, t.re);
+            acc_mac(qr, B.re, t.im);
+            acc_mac(qi, B.im, t.im);
+          }
+          const Cx<C> Pk = mkc<C>(acc_get(pr), acc_get(pi)), Qk = mkc<C>(acc_get(qr), acc_get(qi));
+          zk[(k + MMAX) * PTS] = conj(mkc<C>(Pk.re - Qk.im, Pk.im + Qk.re));
+          zk[(-k + MMAX) * PTS] = conj(mkc<C>(Pk.re + Qk.im, Pk.im - Qk.re));
+        }
+      }
+    }
+  } else {
   // psi and phi DFTs, one thread per (point, theta)
   for (int w = tid; w < NT * PTS; w += blockDim.x) {
     const int th = w / PTS, q = w - th * PTS;
@@ -212,6 +316,7 @@ angl2proj_fast_kernel(const AngPlan P, const S* __restrict__ o, Cx<S>* __restric
       }
     }
   }
+  }
   __syncthreads();
 
   // theta contraction, one thread per (point, projection)
@@ -236,7 +341,7 @@ angl2proj_fast_kernel(const AngPlan P, const S* __restrict__ o, Cx<S>* __restric
 }
 
 template <typename S, typename C, int MMAX, int MRSO>
-__global__ void __launch_bounds__(A2P_THREADS, sizeof(C) == 4 ? 2 : 1)
+__global__ void __launch_bounds__(A2P_THREADS, (ang_min_blocks<C, MMAX>()))
 proj2angl_fast_kernel(const AngPlan P, const Cx<S>* __restrict__ p, S* __restrict__ o) {
   using Sh = Shape<MMAX, MRSO>;
   constexpr int PTS = pts_per_cta<C, MMAX, MRSO>();
@@ -270,6 +375,110 @@ proj2angl_fast_kernel(const AngPlan P, const Cx<S>* __restrict__ p, S* __restric
   __syncthreads();
 
   const C* coef = static_cast<const C*>(P.coef_p2a);
+  if constexpr (split_dft<C, MMAX>()) {
+    constexpr int HPHI2 = (NPHI - 1) / 2;
+    // synthesis over m and inverse phi DFT, one thread per (point, theta,
+    // kpsi); U(f, kpsi) goes into the o tile at the slots its psi row will
+    // occupy: (f, j = 0) holds the real U(f, 0), (f, 2 kpsi - 1) and
+    // (f, 2 kpsi) the real and imaginary parts of U(f, kpsi)
+    for (int w = tid; w < NT * (K + 1) * PTS; w += blockDim.x) {
+      const int tk = w / PTS, q = w - tk * PTS;
+      if (q >= cnt) continue;
+      const int th = tk / (K + 1), kp = tk - th * (K + 1);
+      Cx<C> oh[NPHI];
+#pragma unroll
+      for (int mup = -MMAX; mup <= MMAX; ++mup) {
+        Acc<C> sre, sim;
+        acc_zero(sre);
+        acc_zero(sim);
+        const int a = mup < 0 ? -mup : mup, b = MRSO * kp;
+        const int m0 = a > b ? a : b;
+#pragma unroll
+        for (int m = m0; m <= MMAX; ++m) {
+          const int ip = Sh::ip(m, mup, kp);
+          const Cx<C> v = Ps[ip * PTS + q];
+          const C c = coef[th * NP + ip];
+          acc_mac(sre, v.re, c);
+          acc_mac(sim, v.im, c);
+        }
+        const int kf = mup >= 0 ? mup : mup + NPHI;
+        oh[kf] = conj(mkc<C>(acc_get(sre), acc_get(sim)));
+      }
+      C* row = ot + q * LDO + th * NPHI * NPSI;
+      if (kp == 0) {  // only the real part is used (C2R)
+        C s0 = oh[0].re;
+#pragma unroll
+        for (int k = 1; k < NPHI; ++k) s0 = s0 + oh[k].re;
+        row[0] = s0;
+#pragma unroll
+        for (int f = 1; f <= HPHI2; ++f) {
+          Acc<C> aa, ab;
+          acc_set(aa, oh[0].re);
+          acc_zero(ab);
+#pragma unroll
+          for (int k = 1; k <= HPHI2; ++k) {
+            const Cx<C> t = ldtw<C>(P.tw_phi, (k * f) % NPHI);
+            acc_mac(aa, oh[k].re + oh[NPHI - k].re, t.re);
+            acc_mac(ab, oh[k].im - oh[NPHI - k].im, t.im);
+          }
+          const C ca = acc_get(aa), cb = acc_get(ab);
+          row[f * NPSI] = ca + cb;
+          row[(NPHI - f) * NPSI] = ca - cb;
+        }
+      } else {
+        Cx<C> s0 = oh[0];
+#pragma unroll
+        for (int k = 1; k < NPHI; ++k) s0 = s0 + oh[k];
+        row[2 * kp - 1] = s0.re;
+        row[2 * kp] = s0.im;
+#pragma unroll
+        for (int f = 1; f <= HPHI2; ++f) {
+          Acc<C> pr, pi, qr, qi;
+          acc_set(pr, oh[0].re);
+          acc_set(pi, oh[0].im);
+          acc_zero(qr);
+          acc_zero(qi);
+#pragma unroll
+          for (int k = 1; k <= HPHI2; ++k) {
+            const Cx<C> t = ldtw<C>(P.tw_phi, (k * f) % NPHI);
+            const Cx<C> A = oh[k] + oh[NPHI - k], B = oh[k] - oh[NPHI - k];
+            acc_mac(pr, A.re, t.re);
+            acc_mac(pi, A.im, t.re);
+            acc_mac(qr, B.re, t.im);
+            acc_mac(qi, B.im, t.im);
+          }
+          const Cx<C> Pf = mkc<C>(acc_get(pr), acc_get(pi)), Qf = mkc<C>(acc_get(qr), acc_get(qi));
+          row[f * NPSI + 2 * kp - 1] = Pf.re + Qf.im;
+          row[f * NPSI + 2 * kp] = Pf.im - Qf.re;
+          row[(NPHI - f) * NPSI + 2 * kp - 1] = Pf.re - Qf.im;
+          row[(NPHI - f) * NPSI + 2 * kp] = Pf.im + Qf.re;
+        }
+      }
+    }
+    __syncthreads();
+    // C2R along psi, one thread per (point, theta, phi row): reads its row's
+    // U values and writes the orientations over the same slots
+    for (int w = tid; w < NT * NPHI * PTS; w += blockDim.x) {
+      const int tf = w / PTS, q = w - tf * PTS;
+      if (q >= cnt) continue;
+      C* r = ot + q * LDO + tf * NPSI;  // (theta, f) = tf: row tf of the point
+      C u[NPSI];
+#pragma unroll
+      for (int j = 0; j < NPSI; ++j) u[j] = r[j];
+#pragma unroll
+      for (int j = 0; j < NPSI; ++j) {
+        Acc<C> v;
+        acc_set(v, u[0]);
+#pragma unroll
+        for (int kp = 1; kp <= K; ++kp) {
+          const Cx<C> e = ldtw<C>(P.tw_psi, (kp * j) % NPSI);
+          acc_mac(v, twice(u[2 * kp - 1]), e.re);
+          acc_mac(v, twice(u[2 * kp]), e.im);
+        }
+        r[j] = acc_get(v);
+      }
+    }
+  } else {
   for (int w = tid; w < NT * PTS; w += blockDim.x) {
     const int th = w / PTS, q = w - th * PTS;
     if (q >= cnt) continue;
@@ -368,6 +577,7 @@ proj2angl_fast_kernel(const AngPlan P, const Cx<S>* __restrict__ p, S* __restric
         out[f * NPSI + j] = acc_get(v);
       }
     }
+  }
   }
   __syncthreads();
   S* dst = o + pt0 * NO;
