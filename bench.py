@@ -44,6 +44,8 @@ METRIC = "conv applies/s @64^3 mmax3"
 # headline
 WORKLOAD_96 = dict(n=(96, 96, 96), box=(40.0, 40.0, 40.0), mmax=4, mrso=2, dq=0.01)
 WORKLOAD_128 = dict(n=(128, 128, 128), box=(50.0, 50.0, 50.0), mmax=5, mrso=2, dq=0.01)
+# the mmax-5 kernel instances on a grid small enough for full ncu captures
+WORKLOAD_32M5 = dict(n=(32, 32, 32), box=(20.0, 20.0, 20.0), mmax=5, mrso=2, dq=0.01)
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -60,6 +62,9 @@ def parse_args():
                     help="skip the 128^3 / mmax 5 solve and per-kernel table")
     ap.add_argument("--no-96", action="store_true",
                     help="skip the 96^3 / mmax 4 per-kernel table and accuracy check")
+    ap.add_argument("--steps-workload", choices=["64", "96", "128", "32m5"], default="64",
+                    help="workload of --mode steps: the headline 64^3 / mmax 3 (default), 96^3 / mmax 4, "
+                         "128^3 / mmax 5, or 32^3 / 20 A / mmax 5 (the mmax-5 kernels on a small grid)")
     ap.add_argument("--serving-jobs", type=int, default=None,
                     help="requests in the solute serving stream (default 256)")
     ap.add_argument("--mode", choices=["full", "steps", "energy", "serving"], default="full",
@@ -120,15 +125,20 @@ def kernel_name(stage, form):
     return k[form] if isinstance(k, dict) else k
 
 
-def per_kernel_table(st, form, s, hbm_peak):
+def per_kernel_table(st, form, s, hbm_peak, traffic_of=None):
     """One entry per launch of the round trip: algorithmic bytes, CUDA-event
-    time, achieved GB/s and fraction of the measured HBM bandwidth."""
+    time, achieved GB/s and fraction of the measured HBM bandwidth; with
+    traffic_of (the headline workload) also the DRAM bytes of the committed
+    ncu capture for that launch."""
     ab = algorithmic_bytes(s, 4 if form == "f32" else 8)
     rows = []
     for k in STAGES:
         t = st[k]
-        rows.append({"launch": k, "kernel": kernel_name(k, form), "algorithmic_bytes": ab[k],
-                     "ms": t * 1e3, "achieved_gbs": ab[k] / t / 1e9, "frac": ab[k] / t / 1e9 / hbm_peak})
+        row = {"launch": k, "kernel": kernel_name(k, form), "algorithmic_bytes": ab[k],
+               "ms": t * 1e3, "achieved_gbs": ab[k] / t / 1e9, "frac": ab[k] / t / 1e9 / hbm_peak}
+        if traffic_of is not None:
+            row["traffic_ncu"] = traffic_of(form, k)[0]
+        rows.append(row)
     return rows
 
 
@@ -1087,7 +1097,11 @@ def run_ours(args):
                               "serving_solute": serving_solute_run(args.serving_jobs)}), flush=True)
         return
     forms = ("f64", "f64df", "f32")
-    P = {f: make_problem(f) for f in forms}
+    if args.mode == "steps":
+        wl = {"64": WORKLOAD, "96": WORKLOAD_96, "128": WORKLOAD_128, "32m5": WORKLOAD_32M5}[args.steps_workload]
+        P = {f: make_problem(f, wl) for f in forms}
+    else:
+        P = {f: make_problem(f) for f in forms}
     if args.mode == "steps":
         for f in forms:
             for _ in range(W):
@@ -1158,7 +1172,7 @@ def run_ours(args):
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
     ab = algorithmic_bytes(s, 8)
     # the dominant single launch of the headline form's round trip
-    table = {f: per_kernel_table(st[f], f, s, hbm_peak) for f in forms}
+    table = {f: per_kernel_table(st[f], f, s, hbm_peak, profiled_traffic) for f in forms}
     dom = max(table[head], key=lambda r: r["ms"])
     traffic, traffic_cmd = profiled_traffic(head, dom["launch"])
     kernels_per_step = 1 + 3 + 1 + 3 + 1
