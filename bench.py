@@ -87,7 +87,7 @@ def sizes(wl=None):
     nt, nphi, npsi, no, np_ = I.angular_counts(wl["mmax"], wl["mrso"])
     n = wl["n"]
     N = n[0] * n[1] * n[2]
-    return dict(N=N, ntheta=nt, nphi=nphi, npsi=npsi, no=no, np=np_,
+    return dict(N=N, ntheta=nt, nphi=nphi, npsi=npsi, no=no, np=np_, mmax=wl["mmax"],
                 np_new=I.np_new_count(wl["mmax"], wl["mrso"]))
 
 
@@ -120,7 +120,12 @@ KERNEL_OF_STAGE = {
 }
 
 
-def kernel_name(stage, form):
+def kernel_name(stage, form, mmax=3):
+    """The kernel a launch runs: the split forms' k-space step is one warp
+    per pair from np >= 50 (double-float) / 80 (FP32) projections, i.e.
+    mmax >= 4 / 5 at mrso 2."""
+    if stage == "oz" and ((form == "f64df" and mmax >= 4) or (form == "f32" and mmax >= 5)):
+        return "oz_warp_kernel"
     k = KERNEL_OF_STAGE[stage]
     return k[form] if isinstance(k, dict) else k
 
@@ -134,7 +139,7 @@ def per_kernel_table(st, form, s, hbm_peak, traffic_of=None):
     rows = []
     for k in STAGES:
         t = st[k]
-        row = {"launch": k, "kernel": kernel_name(k, form), "algorithmic_bytes": ab[k],
+        row = {"launch": k, "kernel": kernel_name(k, form, s.get("mmax", 3)), "algorithmic_bytes": ab[k],
                "ms": t * 1e3, "achieved_gbs": ab[k] / t / 1e9, "frac": ab[k] / t / 1e9 / hbm_peak}
         if traffic_of is not None:
             row["traffic_ncu"] = traffic_of(form, k)[0]

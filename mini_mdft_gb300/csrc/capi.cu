@@ -207,7 +207,10 @@ void conv_build(mdft_conv_s* h, const mdft::LucTable& t) {
   std::vector<int4> pr(h->npairs);
   for (int i = 0; i < h->npairs; ++i)
     pr[i] = make_int4(h->pair_list[3 * i], h->pair_list[3 * i + 1], h->pair_list[3 * i + 2], 0);
-  constexpr bool by_q = std::is_same<T, float>::value;
+  // (the warp-per-pair kernel of large angular grids reads a pair's
+  // projections across the lanes, so it keeps the linear order, in which
+  // neighbouring warps share the sectors of the field they read)
+  const bool by_q = std::is_same<T, float>::value && g.np < mdft::oz_warp_min_np<T>();
   auto q2 = [&](const int4& a) { return g.kx[a.x] * g.kx[a.x] + g.ky[a.y] * g.ky[a.y] + g.kz[a.z] * g.kz[a.z]; };
   std::sort(pr.begin(), pr.end(), [&](const int4& a, const int4& b) {
     if (by_q) {

@@ -543,6 +543,16 @@ void launch_fft_axis(const FftAxis& a, void* data, int sign, cudaStream_t s);
 // ---------------------------------------------------------------------------
 // Fused (q,-q) rotation + Ornstein-Zernike + rotation back.
 // ---------------------------------------------------------------------------
+// projections from which the split forms' k-space step runs one warp per
+// pair (oz_warp_kernel) instead of one lane per pair side, by measurement on
+// one GB300: double-float from mmax 4 (np 55 at mrso 2: 5.64 -> 5.08 ms at
+// 96^3; mmax 5, 39.9 -> 21.9 ms at 128^3), FP32 from mmax 5 (10.1 -> 9.0 ms
+// at 128^3; at mmax 4 the lane kernel is faster, 1.46 against 2.18 ms)
+template <typename C>
+constexpr int oz_warp_min_np() {
+  return sizeof(C) == 4 ? 80 : 50;
+}
+
 struct OzPlan {
   int nx, ny, nz, np, mmax, mrso, K, np_new, nq, npairs;
   long long N;
@@ -574,6 +584,9 @@ struct OzPlan {
   size_t smem;
   // Lane-per-pair path: per-pair geometry computed once at plan creation.
   int lane_path;           // 1: oz_lane_kernel, 0: warp-per-pair fallback
+  // lane path of the split forms on large angular grids: one warp per pair
+  // (oz_warp_kernel) over the same tables, instead of a lane per pair side
+  int warp_pairs;
   long long npairs_pad;    // npairs rounded up to a multiple of 32
   int nR;                  // entries per pair in rtab (see oz_build_rtab)
   const int4* pinfo;       // (npairs_pad) lq, lmq, iq, singular (padding: zeros)

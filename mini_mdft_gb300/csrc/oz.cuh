@@ -920,6 +920,189 @@ oz_lane1_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
 #undef RT
 }
 
+
+// ---------------------------------------------------------------------------
+// Warp-per-pair path for large angular grids (split forms, np >=
+// oz_warp_min_np).
+//
+// The lane kernel keeps every lane's np rotated projections in its own
+// shared column, np x 16 bytes per thread in double-float: at mmax 5 (np 88)
+// an SM then holds 4 warps (double-float) or 8 (FP32).  Here one warp owns
+// one (q, -q) pair and spreads its projections over the lanes, so the
+// shared state is per warp (the pair's inputs, rotated projections and
+// R(q) entries, ~7 KB in double-float at mmax 5) and an SM holds 32 warps.
+// Each output is the same sum, in the same order, as in the lane kernel:
+// lane t takes projections t, t + 32, ... of both sides in every stage,
+// sharing the R(q) entries (rotations) and the c(|q|) coefficients (OZ)
+// between the two sides.
+// ---------------------------------------------------------------------------
+template <typename C>
+__host__ __device__ constexpr size_t warp_pair_smem(int np, int nR) {
+  return ((size_t)4 * np * sizeof(Cx<C>) + (size_t)nR * sizeof(C) + 15) & ~size_t(15);
+}
+
+template <typename S, typename C, int MMAX>
+__global__ void __launch_bounds__(256)
+oz_warp_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const long long pair = (long long)blockIdx.x * P.warps_per_cta + wib;
+  if (pair >= P.npairs) return;  // whole warp exits together
+  const int np = P.np, mrso = P.mrso;
+  unsigned char* base = sm + (size_t)wib * warp_pair_smem<C>(np, P.nR);
+  Cx<C>* G0 = reinterpret_cast<Cx<C>*>(base);  // q side: inputs, then OZ outputs
+  Cx<C>* G1 = G0 + np;                          // -q side
+  Cx<C>* D0 = G1 + np;                          // rotated to the q frame
+  Cx<C>* D1 = D0 + np;
+  C* rt = reinterpret_cast<C*>(D1 + np);  // the pair's R(q) entries
+  // projection index arithmetic in registers (no per-thread array that a
+  // runtime m would index through local memory): byte m of bpack is the
+  // first projection of degree m (< 256 for mmax <= 6), nibble m of wpack
+  // the count m / mrso + 1 of its mu2 values
+  unsigned long long bpack = 0, wpack = 0;
+  {
+    int b = 0;
+#pragma unroll
+    for (int m = 0; m <= MMAX; ++m) {
+      bpack |= (unsigned long long)b << (8 * m);
+      wpack |= (unsigned long long)(m / mrso + 1) << (4 * m);
+      b += (2 * m + 1) * (m / mrso + 1);
+    }
+  }
+  auto pbase = [&](int m) { return (int)((bpack >> (8 * m)) & 0xffu); };
+  auto pw = [&](int m) { return (int)((wpack >> (4 * m)) & 0xfu); };
+  auto ipx = [&](int m, int mup, int mu2) { return pbase(m) + (mup + m) * pw(m) + mu2; };
+  // (m, mup, mu2) of projection ip
+  auto decode = [&](int ip, int& m, int& mup, int& mu2) {
+    m = 0;
+#pragma unroll
+    for (int l = 1; l <= MMAX; ++l)
+      if (ip >= pbase(l)) m = l;
+    const int w = pw(m), r = ip - pbase(m);
+    mup = r / w - m;
+    mu2 = r - (r / w) * w;
+  };
+  const int4 info = P.pinfo[pair];
+  const long long N = P.pstride;
+  const long long lq = info.x + (long long)blockIdx.y * P.N, lmq = info.y + (long long)blockIdx.y * P.N;
+  {
+    const C* Rt = static_cast<const C*>(P.rtab) + (pair >> 5) * (long long)P.nR * 32 + (pair & 31);
+    for (int e = lane; e < P.nR; e += 32) rt[e] = Rt[(long long)e * 32];
+  }
+#define RH(l, m, j) rt[hoff(l) + ((m) + (l)) * ((l) + 1) + (j)]
+#define WPOW(k) mkc<C>(rt[hoff(MMAX + 1) + 2 * ((k)-1)], rt[hoff(MMAX + 1) + 2 * ((k)-1) + 1])
+  __syncwarp();
+  // inputs of both sides, times w^(a - m) as the lane kernel applies it
+  for (int ip = lane; ip < np; ip += 32) {
+    int m, mup, mu2;
+    decode(ip, m, mup, mu2);
+    const Cx<S> u = p[(long long)ip * N + lq], v = p[(long long)ip * N + lmq];
+    Cx<C> a = mkc<C>(to_compute<C>(u.re), to_compute<C>(u.im));
+    Cx<C> b = mkc<C>(to_compute<C>(v.re), to_compute<C>(v.im));
+    if (mup != 0) {
+      const int t = mup > 0 ? mup : -mup;
+      const Cx<C> wt = mup > 0 ? WPOW(t) : conj(WPOW(t));
+      a = cx_mul(a, wt);
+      b = cx_mul(b, wt);
+    }
+    G0[ip] = a;
+    G1[ip] = b;
+  }
+  __syncwarp();
+  // rotation to the q frame (MDFT_Convolution.hpp:427-443)
+  for (int ip = lane; ip < np; ip += 32) {
+    int m, k, mu2;
+    decode(ip, m, k, mu2);
+    const int j = k < 0 ? -k : k;
+    const int b0 = ipx(m, -m, mu2), bs = pw(m);  // g_b at b0 + b bs
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const Cx<C>* g = s ? G1 : G0;
+      const bool direct = k == 0 || (s == 0 ? k > 0 : k < 0);
+      CAcc<C> x;
+      cacc_zero(x);
+      for (int b = 0; b <= 2 * m; ++b) {
+        const C h = RH(m, b - m, j);
+        if (direct)
+          cacc_mac_r(x, g[b0 + b * bs], h);
+        else
+          cacc_mac_r(x, g[b0 + (2 * m - b) * bs], ((m + b) & 1) ? -h : h);
+      }
+      Cx<C> v = cacc_get(x);
+      if (!direct && (j & 1)) v = mkc<C>(-v.re, -v.im);
+      if (s == 1 && (m & 1)) v = mkc<C>(-v.re, -v.im);
+      (s ? D1 : D0)[ip] = v;
+    }
+  }
+  __syncwarp();
+  // OZ with c(|q|) (:449-496) and the chop (:514-517); outputs over G
+  const bool singular = info.w != 0;
+  const C alpha = static_cast<const C*>(P.palpha)[pair];
+  const C beta = C(1) - alpha;
+  const bool pre = P.ceff != nullptr;
+  const Cx<C>* clo = static_cast<const Cx<C>*>(pre ? P.ceff : P.ctab) + (size_t)info.z * P.np_new;
+  const Cx<C>* chi = clo + P.np_new;
+  for (int ip = lane; ip < np; ip += 32) {
+    int m, k, mu2;
+    decode(ip, m, k, mu2);
+    const int ak = k < 0 ? -k : k;
+    CAcc<C> s0, s1;
+    cacc_zero(s0);
+    cacc_zero(s1);
+    int ia = P.ia_start[ip];
+    for (int n = ak; n <= MMAX; ++n) {
+      const int nn = pw(n) - 1;
+      for (int u = 0; u <= 2 * nn; ++u, ++ia) {
+        const Cx<C> c = pre ? clo[ia]
+                            : mkc<C>(alpha * chi[ia].re + beta * clo[ia].re, alpha * chi[ia].im + beta * clo[ia].im);
+        const int nu2 = u - nn;
+        if (nu2 < 0) {
+          const int jj = ipx(n, k, -nu2);
+          cacc_mac(s0, c, D0[jj]);
+          cacc_mac(s1, c, D1[jj]);
+        } else {
+          const int jj = ipx(n, k, nu2);
+          cacc_macc(s0, c, D1[jj]);
+          cacc_macc(s1, c, D0[jj]);
+        }
+      }
+    }
+    G0[ip] = chop(cacc_get(s0));
+    G1[ip] = chop(cacc_get(s1));
+  }
+  __syncwarp();
+  // rotation back with conj R (:518-536) and the stores (:538-541): the -q
+  // store wins at self-paired points, -q conjugated at singular mid-k points
+  const bool store0 = info.x != info.y;
+  for (int ip = lane; ip < np; ip += 32) {
+    int m, a, mu2;
+    decode(ip, m, a, mu2);
+    a += m;  // 0 .. 2m
+    const int k0 = ipx(m, -m, mu2), ks = pw(m);  // G(m, k) at k0 + (k + m) ks
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const Cx<C>* g = s ? G1 : G0;
+      CAcc<C> acc;
+      cacc_zero(acc);
+      for (int k = -m; k <= m; ++k) {
+        const int ak = k < 0 ? -k : k;
+        const bool direct = s ? (k <= 0) : (k >= 0);
+        const bool neg = (((a - m) & 1) != 0) != ((k & 1) != 0);
+        const C hd = RH(m, a - m, ak), hm = RH(m, m - a, ak);
+        cacc_mac_r(acc, g[k0 + (k + m) * ks], direct ? hd : (neg ? -hm : hm));
+      }
+      Cx<C> v = cacc_get(acc);
+      if (a > m) v = cx_mul(v, conj(WPOW(a - m)));
+      if (a < m) v = cx_mul(v, WPOW(m - a));
+      if (s == 1 && (m & 1)) v = mkc<C>(-v.re, -v.im);
+      if (s == 1 && singular) v = conj(v);
+      if (s == 1 || store0) p[(long long)ip * N + (s ? lmq : lq)] = mkc<S>(to_storage<S>(v.re), to_storage<S>(v.im));
+    }
+  }
+#undef RH
+#undef WPOW
+}
+
 constexpr int kLaneMaxMmax = 6;
 
 template <typename C>
@@ -939,6 +1122,10 @@ size_t lane_smem_per_warp(int np) {
 template <typename S, typename C, int K>
 void lane_attr_one(const OzPlan& P) {
   if constexpr (split_pairs<C>()) {
+    if (P.warp_pairs) {
+      allow_max_smem(oz_warp_kernel<S, C, K>, P.smem, "oz smem attribute");
+      return;
+    }
     if constexpr (std::is_same<S, C>::value) {
       if (P.mrso == 2) {
         oz_lane_r2_attr<C, K>(P.smem);
@@ -966,6 +1153,10 @@ void lane_attr_all(const OzPlan& P) {
 template <typename S, typename C, int K>
 void lane_launch_one(const OzPlan& P, Cx<S>* p, dim3 grid, dim3 block, cudaStream_t s) {
   if constexpr (split_pairs<C>()) {
+    if (P.warp_pairs) {
+      oz_warp_kernel<S, C, K><<<grid, block, P.smem, s>>>(P, p);
+      return;
+    }
     if constexpr (std::is_same<S, C>::value) {
       if (P.mrso == 2) {
         oz_lane_r2_launch<C, K>(P, p, grid, block, s);
@@ -985,6 +1176,17 @@ void oz_plan_finish(OzPlan& P) {
   // Lane path when one warp's shared columns fit with room for a few warps
   // per SM; otherwise the warp-per-pair kernel (R computed on the fly).
   const size_t per_warp = lane_smem_per_warp<C>(P.np);
+  P.warp_pairs = 0;
+  if (split_pairs<C>() && P.np >= oz_warp_min_np<C>() && P.mmax <= kLaneMaxMmax && P.N < (1LL << 31)) {
+    // the lane kernel's per-thread columns would leave few warps per SM:
+    // one warp per pair, 8 pairs per CTA, over the same tables
+    P.lane_path = 1;
+    P.warp_pairs = 1;
+    P.warps_per_cta = 8;
+    P.smem = warp_pair_smem<C>(P.np, hoff(P.mmax + 1) + 2 * P.mmax) * P.warps_per_cta;
+    lane_attr_all<S, C>(P);
+    return;
+  }
   P.lane_path = (P.mmax <= kLaneMaxMmax && per_warp <= 64 * 1024 && P.N < (1LL << 31)) ? 1 : 0;
   if (P.lane_path) {
     P.warps_per_cta = lane_warps(per_warp, split_pairs<C>());
@@ -1036,7 +1238,7 @@ void launch_oz(const OzPlan& P, Cx<S>* p, cudaStream_t s) {
   if (P.npairs == 0) return;
   clear_stale_error();
   if (P.lane_path) {
-    const int per_warp_pairs = split_pairs<C>() ? 16 : 32;
+    const int per_warp_pairs = P.warp_pairs ? 1 : (split_pairs<C>() ? 16 : 32);
     const long long ngrp = (P.npairs + per_warp_pairs - 1) / per_warp_pairs;
     const long long nb = (ngrp + P.warps_per_cta - 1) / P.warps_per_cta;
     throw_if(nb > 0x7fffffffLL, "too many k-space pairs", 4);
