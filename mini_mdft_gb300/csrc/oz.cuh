@@ -945,10 +945,23 @@ template <typename S, typename C, int MMAX>
 __global__ void __launch_bounds__(256)
 oz_warp_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
   extern __shared__ __align__(16) unsigned char sm[];
+  // the OZ stage's order of the projections: by |k| from MMAX down, so that
+  // the lanes of one round have sums of similar length
+  __shared__ short oz_order[256];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int np = P.np, mrso = P.mrso;
+  for (int ip = threadIdx.x; ip < np; ip += blockDim.x) {  // rank of ip in that order
+    const int a = abs(__ldg(P.ip_mup + ip));
+    int r = 0;
+    for (int q = 0; q < np; ++q) {
+      const int b = abs(__ldg(P.ip_mup + q));
+      r += (b > a || (b == a && q < ip)) ? 1 : 0;
+    }
+    oz_order[r] = (short)ip;
+  }
+  __syncthreads();
   const long long pair = (long long)blockIdx.x * P.warps_per_cta + wib;
   if (pair >= P.npairs) return;  // whole warp exits together
-  const int np = P.np, mrso = P.mrso;
   unsigned char* base = sm + (size_t)wib * warp_pair_smem<C>(np, P.nR);
   Cx<C>* G0 = reinterpret_cast<Cx<C>*>(base);  // q side: inputs, then OZ outputs
   Cx<C>* G1 = G0 + np;                          // -q side
@@ -1021,12 +1034,12 @@ oz_warp_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
       const bool direct = k == 0 || (s == 0 ? k > 0 : k < 0);
       CAcc<C> x;
       cacc_zero(x);
+      // direct: sum_b g_b h_b; mirrored: sum_b (-1)^(m+b) g_{2m-b} h_b (selects,
+      // not branches: neighbouring lanes take either)
       for (int b = 0; b <= 2 * m; ++b) {
         const C h = RH(m, b - m, j);
-        if (direct)
-          cacc_mac_r(x, g[b0 + b * bs], h);
-        else
-          cacc_mac_r(x, g[b0 + (2 * m - b) * bs], ((m + b) & 1) ? -h : h);
+        const int bb = direct ? b : 2 * m - b;
+        cacc_mac_r(x, g[b0 + bb * bs], (!direct && ((m + b) & 1)) ? -h : h);
       }
       Cx<C> v = cacc_get(x);
       if (!direct && (j & 1)) v = mkc<C>(-v.re, -v.im);
@@ -1042,7 +1055,8 @@ oz_warp_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
   const bool pre = P.ceff != nullptr;
   const Cx<C>* clo = static_cast<const Cx<C>*>(pre ? P.ceff : P.ctab) + (size_t)info.z * P.np_new;
   const Cx<C>* chi = clo + P.np_new;
-  for (int ip = lane; ip < np; ip += 32) {
+  for (int r = lane; r < np; r += 32) {
+    const int ip = oz_order[r];
     int m, k, mu2;
     decode(ip, m, k, mu2);
     const int ak = k < 0 ? -k : k;
@@ -1055,16 +1069,14 @@ oz_warp_kernel(const OzPlan P, Cx<S>* __restrict__ p) {
       for (int u = 0; u <= 2 * nn; ++u, ++ia) {
         const Cx<C> c = pre ? clo[ia]
                             : mkc<C>(alpha * chi[ia].re + beta * clo[ia].re, alpha * chi[ia].im + beta * clo[ia].im);
+        // nu2 < 0: own column at -nu2; nu2 >= 0: the other side's at nu2,
+        // conjugated (c conj(D) = the same products as cacc_macc)
         const int nu2 = u - nn;
-        if (nu2 < 0) {
-          const int jj = ipx(n, k, -nu2);
-          cacc_mac(s0, c, D0[jj]);
-          cacc_mac(s1, c, D1[jj]);
-        } else {
-          const int jj = ipx(n, k, nu2);
-          cacc_macc(s0, c, D1[jj]);
-          cacc_macc(s1, c, D0[jj]);
-        }
+        const bool own = nu2 < 0;
+        const int jj = ipx(n, k, own ? -nu2 : nu2);
+        const Cx<C> d0 = own ? D0[jj] : conj(D1[jj]), d1 = own ? D1[jj] : conj(D0[jj]);
+        cacc_mac(s0, c, d0);
+        cacc_mac(s1, c, d1);
       }
     }
     G0[ip] = chop(cacc_get(s0));
