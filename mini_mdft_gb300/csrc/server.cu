@@ -181,7 +181,7 @@ struct Group {
   // solute groups: per slot the minimiser's fields (xt contiguous: the batched
   // evaluation reads the k trial points as one array) and scalar blocks
   DevPtr xt, x, g, gt, vext, d, hs, hy, hinv, S, red;
-  double* tails = nullptr;  // page-locked: 8 doubles per slot read back each step
+  double* tails = nullptr;  // page-locked: Lbfgs::kTail doubles per slot read back each step
   std::vector<mdft::Lbfgs> lb;
   // every slot's L-BFGS operations of a step in one batch, one launch per
   // round (not the persistent cooperative launch: a group's launches share
@@ -354,7 +354,8 @@ Group* mdft_server_s::group_for(const Job& j) {
     g->S.alloc(sizeof(double) * mdft::Lbfgs::nscalars(kHistory) * g->B, "server arena");
     g->red.alloc(mdft::reduction_scratch_bytes() * g->B, "server arena");  // one per slot
     ck(cudaMemset(g->red.p, 0, mdft::reduction_scratch_bytes() * g->B), "scratch reset");
-    ck(cudaHostAlloc((void**)&g->tails, sizeof(double) * 8 * g->B, cudaHostAllocDefault), "page-locked tails");
+    ck(cudaHostAlloc((void**)&g->tails, sizeof(double) * mdft::Lbfgs::kTail * g->B, cudaHostAllocDefault),
+       "page-locked tails");
     g->lbr.rounds = true;
     g->lb.resize(g->B);
     g->model = sv;
@@ -410,7 +411,8 @@ void mdft_server_s::admit() {
                            j->solute.data(), (int)j->solute.size() / 6, g->model.vmax,
                            g->vext.as<double>() + (size_t)n * slot, g->stream);
         bind_slot(*g, slot);
-        g->lb[slot].start(j->gtol, 0.0, j->max_iter, g->stream);
+        // the FP32 form's energies are noisy at ~1e-7: accept by the slope too
+        g->lb[slot].start(j->gtol, 0.0, j->max_iter, g->stream, g->elem == 4 ? 1e-6 : 0.0);
       }
       ck(cudaStreamSynchronize(g->stream), "job admission");
     } catch (const Error& e) {
@@ -456,13 +458,15 @@ void enqueue_solve_step(Group& g, int k) {
   mdft::detail::execute_fields(g.conv, g.p.p, k, s);
   mdft::detail::proj2angl_fields(g.opt, g.p.p, g.vexc.p, k, s);
   // every slot's energy, gradient and preconditioner in one launch, then the
-  // slots' scalar tails (8 doubles each, one scalar block apart) in one copy
+  // slots' scalar tails (kTail doubles each, one scalar block apart) in one
+  // copy; the FP32 form also sums each slot's slope along its direction
   const int ns = mdft::Lbfgs::nscalars(kHistory);
   mdft::energy_grad(g.eg, g.xt.as<double>(), g.vexc.p, g.elem == 4, g.vext.as<double>(), g.w.as<double>(),
                     g.gt.as<double>(), (long long)n, g.no, g.S.as<double>() + mdft::Lbfgs::energy_at(kHistory),
-                    g.red.p, g.hinv.as<float>(), s, k, ns);
-  ck(cudaMemcpy2DAsync(g.tails, 8 * sizeof(double), g.S.as<double>() + mdft::Lbfgs::tail_at(kHistory),
-                       sizeof(double) * ns, 8 * sizeof(double), k, cudaMemcpyDeviceToHost, s),
+                    g.red.p, g.hinv.as<float>(), s, k, ns, g.elem == 4 ? g.d.as<float>() : nullptr);
+  constexpr size_t tb = sizeof(double) * mdft::Lbfgs::kTail;
+  ck(cudaMemcpy2DAsync(g.tails, tb, g.S.as<double>() + mdft::Lbfgs::tail_at(kHistory), sizeof(double) * ns, tb, k,
+                       cudaMemcpyDeviceToHost, s),
      "minimiser tail read-back");
 }
 
@@ -732,7 +736,7 @@ void mdft_server_s::complete_step(Group& g) {
     std::vector<int> ended;
     std::vector<mdft::Lbfgs*> run;
     for (int s = g.k - 1; s >= 0; --s) {
-      if (g.lb[s].on_eval(g.tails + 8 * s)) ended.push_back(s);
+      if (g.lb[s].on_eval(g.tails + mdft::Lbfgs::kTail * s)) ended.push_back(s);
       run.push_back(&g.lb[s]);
     }
     mdft::lbfgs_run(run.data(), (int)run.size(), g.lbr, g.stream);

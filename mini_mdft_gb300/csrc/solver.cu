@@ -372,11 +372,12 @@ struct EgArgs {
   float ln2h, ln2l;
   float ah[10], al[10];          // 1 / (2k + 1), k = 0..9
   double* out;  // [E_total, E_id, E_ext, E_exc, max |g|]
-  // reduction scratch of field 0: (CTAs, 7) doubles, then at counter_off
+  // reduction scratch of field 0: (CTAs, 9) doubles, then at counter_off
   // the completion counter; field f's at f scratch_stride bytes further
   void* scratch;
   size_t counter_off, scratch_stride;
   long long out_stride;  // doubles between the fields' out blocks
+  const float* dir;      // search direction (may be null): out[5] = g . dir
   // 1 / D with D = 2 rho0 dv w kT max(ln xi^2 + 2 + vext/kT, 1): the local
   // terms' curvature d^2/dxi^2 (E_id + E_ext), floored at half its value at
   // their minimum -- the minimiser's diagonal preconditioner (may be null)
@@ -484,10 +485,12 @@ __global__ void __launch_bounds__(kRedThreads, 4) eg_kernel(const EgArgs A) {
   const float ikT = 1.f / A.kh, c2k = 2.f * A.ch * A.kh;
   // sums of w (xi^2 ln xi^2 - xi^2 + 1), w xi^2 vext and w vexc (xi^2 - 1):
   // double-float Dot2 accumulators, and plain FP64 sums for the FP64 elements
-  Acc<DF> a_id, a_ext, a_exc;
+  Acc<DF> a_id, a_ext, a_exc, a_gd;
   acc_zero(a_id);
   acc_zero(a_ext);
   acc_zero(a_exc);
+  acc_zero(a_gd);  // g . dir (with a direction only)
+  const float* __restrict__ dir = A.dir ? A.dir + fo : nullptr;
   double d_id = 0.0, d_ext = 0.0, d_exc = 0.0;
   unsigned long long gmax = 0;  // bits of max |g| (non-negative doubles order as integers)
   const long long stride = (long long)gridDim.x * blockDim.x;
@@ -521,7 +524,9 @@ __global__ void __launch_bounds__(kRedThreads, 4) eg_kernel(const EgArgs A) {
       acc_mac(a_ext, wd, (q.t + one) * ved);
       acc_mac(a_exc, wd, vd * q.t);
       const DF inner = cext * (kT * q.L + ved) + cexc2 * vd;
-      gi = df_to_double(twice(df_from_double_bits(x) * wd) * inner);
+      const DF gdf = twice(df_from_double_bits(x) * wd) * inner;
+      gi = df_to_double(gdf);
+      if (dir) acc_mac(a_gd, gdf, DF(dir[i], 0.f));
       if (hinv) hinv[i] = __fdividef(1.f, wd.hi * c2k * fmaxf(q.L.hi + 2.f + ved.hi * ikT, 1.f));
     } else {
       const Terms64 tt = terms_f64(x, ws[o], (double)vv, ve, A);
@@ -530,6 +535,7 @@ __global__ void __launch_bounds__(kRedThreads, 4) eg_kernel(const EgArgs A) {
       d_exc += tt.exc;
       gi = tt.g;
       if (hinv) hinv[i] = tt.hinv;
+      if (dir) acc_mac(a_gd, df_from_double_bits(gi), DF(dir[i], 0.f));
     }
     gout[i] = gi;
     const unsigned long long gb = bits_of(gi) & 0x7fffffffffffffffull;
@@ -537,14 +543,16 @@ __global__ void __launch_bounds__(kRedThreads, 4) eg_kernel(const EgArgs A) {
     o += ostep;
     if (o >= A.no) o -= A.no;
   }
-  Red<3> r;
+  Red<4> r;
   r.s[0] = dd_plus(Dd{c_id * df_to_double(acc_get(a_id)), 0.0}, c_id * d_id);
   r.s[1] = dd_plus(Dd{c_ext * df_to_double(acc_get(a_ext)), 0.0}, c_ext * d_ext);
   r.s[2] = dd_plus(Dd{c_exc * df_to_double(acc_get(a_exc)), 0.0}, c_exc * d_exc);
+  r.s[3] = Dd{df_to_double(acc_get(a_gd)), 0.0};
   r.mx = double_of(gmax);
   double* out = A.out + (long long)blockIdx.y * A.out_stride;
   unsigned char* scr = static_cast<unsigned char*>(A.scratch) + (size_t)blockIdx.y * A.scratch_stride;
-  grid_reduce<3>(r, reinterpret_cast<double*>(scr), reinterpret_cast<unsigned*>(scr + A.counter_off), [out](const Red<3>& tt) {
+  const bool want_gd = dir != nullptr;
+  grid_reduce<4>(r, reinterpret_cast<double*>(scr), reinterpret_cast<unsigned*>(scr + A.counter_off), [out, want_gd](const Red<4>& tt) {
     const double id = tt.s[0].hi + tt.s[0].lo, ext = tt.s[1].hi + tt.s[1].lo, exc = tt.s[2].hi + tt.s[2].lo;
     const Dd tot = dd_plus(dd_plus(tt.s[0], tt.s[1]), tt.s[2]);
     out[0] = tot.hi + tot.lo;
@@ -552,6 +560,7 @@ __global__ void __launch_bounds__(kRedThreads, 4) eg_kernel(const EgArgs A) {
     out[2] = ext;
     out[3] = exc;
     out[4] = tt.mx;
+    if (want_gd) out[5] = tt.s[3].hi + tt.s[3].lo;
   });
 }
 
@@ -1071,7 +1080,7 @@ void launch_ok(const char* what) {
 }
 }  // namespace
 
-size_t reduction_scratch_bytes() { return sizeof(double) * kRedBlocks * 7 + 256; }
+size_t reduction_scratch_bytes() { return sizeof(double) * kRedBlocks * 9 + 256; }
 
 void to_float(float* y, const double* x, long long n, cudaStream_t s) {
   to_float_kernel<<<stream_blocks(n), 256, 0, s>>>(y, x, n);
@@ -1173,10 +1182,11 @@ void vext_compute(const Grid& g, const double* sv_sites, int n_solvent, const do
 
 void energy_grad(const EgConst& c, const double* xi, const void* vexc, bool vexc_f32, const double* vext,
                  const double* w, double* grad, long long n, int no, double* out, void* scratch, float* hinv,
-                 cudaStream_t s, int nf, long long out_stride) {
+                 cudaStream_t s, int nf, long long out_stride, const float* dir) {
   throw_if(nf < 1 || nf > 65535, "internal: energy batch size", 4);
   EgArgs A{};
   A.hinv = hinv;
+  A.dir = dir;
   A.xi = xi;
   A.vexc = vexc;
   A.vext = vext;
@@ -1200,7 +1210,7 @@ void energy_grad(const EgConst& c, const double* xi, const void* vexc, bool vexc
   A.out = out;
   A.out_stride = out_stride;
   A.scratch = scratch;
-  A.counter_off = sizeof(double) * kRedBlocks * 7;
+  A.counter_off = sizeof(double) * kRedBlocks * 9;  // the (CTAs, 2 x 4 + 1) partials of grid_reduce<4>
   A.scratch_stride = reduction_scratch_bytes();
   const size_t smem = (sizeof(double) + sizeof(float2)) * (size_t)no;
   throw_if(smem > 48 * 1024, "too many orientations for the energy kernel", MDFT_ERR_UNSUPPORTED);
@@ -1293,9 +1303,10 @@ void Lbfgs::step() {
   ops_.push_back(o);
 }
 
-void Lbfgs::start(double gtol, double ftol, int max_iter, cudaStream_t s) {
+void Lbfgs::start(double gtol, double ftol, int max_iter, cudaStream_t s, double e_noise) {
   gtol_ = gtol;
   ftol_ = ftol;
+  e_noise_ = e_noise;
   max_iter_ = max_iter;
   nh_ = head_ = ls_ = iter_ = 0;
   first_ = true;
@@ -1320,7 +1331,15 @@ bool Lbfgs::on_eval(const double* tail) {
       step();
       return false;
     }
-    if (!(std::isfinite(Et[0]) && Et[0] <= E_[0] + c1 * t_ * gdv)) {
+    // Armijo; or, with noisy energies, approximate Wolfe: E within the noise
+    // of the current value and the slope at the trial point risen to at most
+    // (1 - 2 delta) |g.d| (for a quadratic along d this is Armijo with
+    // c1 = delta, told by the slope, which the noise of E does not reach)
+    const double delta = 0.1, slope_t = tail[8];
+    const bool armijo = std::isfinite(Et[0]) && Et[0] <= E_[0] + c1 * t_ * gdv;
+    const bool approx = e_noise_ > 0.0 && std::isfinite(Et[0]) && std::isfinite(slope_t) &&
+                        Et[0] <= E_[0] + e_noise_ * std::fabs(E_[0]) && slope_t <= (1.0 - 2.0 * delta) * -gdv;
+    if (!(armijo || approx)) {
       t_ *= 0.5;
       if (++ls_ > max_ls) {  // no decrease along the direction: end at x
         status_ = kStalled;
@@ -1515,8 +1534,9 @@ int solver_guard(F&& f) {
   }
 }
 
-// E(x) and its gradient into g; the 5 terms to out (device)
-void evaluate(mdft_solver_s* h, const double* x, double* g, double* out, cudaStream_t s) {
+// E(x) and its gradient into g; the 5 terms to out (device), and with_slope
+// g . d (the minimiser's direction) to out[5]
+void evaluate(mdft_solver_s* h, const double* x, double* g, double* out, cudaStream_t s, bool with_slope = false) {
   const void* xin = x;
   if (h->prec == MDFT_F32) {
     mdft::to_float(h->xf.as<float>(), x, h->n, s);
@@ -1526,7 +1546,8 @@ void evaluate(mdft_solver_s* h, const double* x, double* g, double* out, cudaStr
   mdft::detail::execute_fields(h->conv, h->p.ptr, 1, s);
   mdft::detail::proj2angl_fields(h->opt, h->p.ptr, h->vexc.ptr, 1, s);
   mdft::energy_grad(h->c, x, h->vexc.ptr, h->prec == MDFT_F32, h->has_vext ? h->vext.as<double>() : nullptr,
-                    h->w.as<double>(), g, h->n, h->no, out, h->scratch.ptr, h->hinv.as<float>(), s);
+                    h->w.as<double>(), g, h->n, h->no, out, h->scratch.ptr, h->hinv.as<float>(), s, 1, 0,
+                    with_slope ? h->d.as<float>() : nullptr);
 }
 
 }  // namespace
@@ -1620,12 +1641,15 @@ int mdft_solver_minimize(mdft_solver_t h, double* xi, int max_iter, double gtol,
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const size_t fb = sizeof(double) * (size_t)h->n;
     cuda_check(cudaMemcpyAsync(h->xt.ptr, xi, fb, cudaMemcpyDeviceToDevice, s), "start copy");
-    h->lb.start(gtol, ftol, max_iter, s);
+    // the FP32 form's energies carry ~1e-7 relative noise (its transforms
+    // run in FP32): the line search then also accepts by the slope
+    const double e_noise = h->prec == MDFT_F32 ? 1e-6 : 0.0;
+    h->lb.start(gtol, ftol, max_iter, s, e_noise);
     const int m = h->m;
     double* Sd = h->S.as<double>();
-    double tail[8];
+    double tail[mdft::Lbfgs::kTail];
     for (;;) {
-      evaluate(h, h->xt.as<double>(), h->gt.as<double>(), Sd + mdft::Lbfgs::energy_at(m), s);
+      evaluate(h, h->xt.as<double>(), h->gt.as<double>(), Sd + mdft::Lbfgs::energy_at(m), s, e_noise > 0.0);
       cuda_check(cudaMemcpyAsync(tail, Sd + mdft::Lbfgs::tail_at(m), sizeof tail, cudaMemcpyDeviceToHost, s),
                  "tail read-back");
       cuda_check(cudaStreamSynchronize(s), "solver stream");

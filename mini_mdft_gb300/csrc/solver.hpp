@@ -26,10 +26,11 @@ void vext_compute(const Grid& g, const double* solvent_sites, int n_solvent, con
 // once, left zeroed).  nf > 1: nf fields in one launch, field f's arrays at
 // f n elements, its out block at f out_stride doubles, its scratch at f
 // reduction_scratch_bytes() bytes; each field's sums are the ones it gets
-// alone.
+// alone.  dir (FP32, may be null): also out[5] = grad . dir, the slope of E
+// along the search direction at xi.
 void energy_grad(const EgConst& c, const double* xi, const void* vexc, bool vexc_f32, const double* vext,
                  const double* w, double* grad, long long n, int no, double* out, void* scratch, float* hinv,
-                 cudaStream_t s, int nf = 1, long long out_stride = 0);
+                 cudaStream_t s, int nf = 1, long long out_stride = 0, const float* dir = nullptr);
 size_t reduction_scratch_bytes();
 
 // xi (double) -> float copy of n values
@@ -91,8 +92,8 @@ void grid_barrier_selftest(int missing, LbRunner& r, cudaStream_t s);
 // scalar block S, and a curvature pair with s.y <= 1e-12 y.y enters with
 // rho = 0 (it then drops out of the recursion), so the host never waits for
 // a dot product.  After each evaluation of E and its gradient at xt the
-// caller reads back the block's tail (tail_at(m), 8 doubles: g.d, s.y, y.y,
-// the 5 energy terms) and calls on_eval, which queues the vector operations
+// caller reads back the block's tail (tail_at(m), kTail doubles: g.d, s.y,
+// y.y, the 5 energy terms, the trial slope) and calls on_eval, which queues the vector operations
 // that form the next trial point in xt; lbfgs_run runs them.
 class Lbfgs {
  public:
@@ -109,14 +110,22 @@ class Lbfgs {
     void* scratch;
   };
   enum Status { kRunning = -1, kConverged = 0, kFlat = 1, kMaxIter = 2, kStalled = 3 };
-  static int nscalars(int m) { return 2 * m + 11; }
+  static int nscalars(int m) { return 2 * m + 12; }
   static int tail_at(int m) { return 2 * m + 3; }
-  static int energy_at(int m) { return 2 * m + 6; }
+  static int energy_at(int m) { return 2 * m + 6; }  // 5 terms, then the trial slope g(xt) . d
+  static constexpr int kTail = 9;                     // g.d, s.y, y.P.y, 5 terms, g(xt) . d
 
   // re-points the field's buffers (after a slot move the host state is kept)
   void bind(const Bufs& b, long long n, int m);
-  // a new run from the point in xt: resets the scalars and the history
-  void start(double gtol, double ftol, int max_iter, cudaStream_t s);
+  // a new run from the point in xt: resets the scalars and the history.
+  // e_noise > 0: the relative noise of E (an FP32 evaluation); a trial whose
+  // E is within e_noise |E| of the current one and whose slope along the
+  // direction has risen to at most (1 - 2 delta) |g.d| (approximate Wolfe,
+  // Hager and Zhang 2005, delta = 0.1) is accepted when the Armijo test
+  // cannot tell, so the run is not stopped by the noise; the evaluation must
+  // then write g(xt) . d (energy_grad with the direction)
+  void start(double gtol, double ftol, int max_iter, cudaStream_t s, double e_noise = 0.0);
+  double e_noise() const { return e_noise_; }
   // the evaluation at xt is done: accept or backtrack, and queue the
   // operations of the next trial point into xt; true when the run has ended.
   // The caller runs ops() (lbfgs_run) after every call: when the run ends at
@@ -146,7 +155,7 @@ class Lbfgs {
   int m_ = 5;
   int nh_ = 0, head_ = 0, ls_ = 0, iter_ = 0, max_iter_ = 0;
   bool first_ = true;
-  double gtol_ = 0, ftol_ = 0, t_ = 0;
+  double gtol_ = 0, ftol_ = 0, t_ = 0, e_noise_ = 0;
   double E_[5] = {0, 0, 0, 0, 0};
   Status status_ = kRunning;
   std::vector<double> trace_;

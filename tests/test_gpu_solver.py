@@ -191,9 +191,12 @@ def test_minimizer_with_solute_descends_and_forms_agree(gpu_lib):
         solver = M.Solver(opt, conv, vext, kT=kT, rho0=rho0, prefactor=pref, history=7)
         xi = torch.ones_like(vext)
         trace = solver.minimize(xi, max_iter=300, gtol=1e-9)
-        assert np.all(np.diff(trace[:, 0]) <= 1e-12 * np.abs(trace[:, 0]).max()), prec
-        # the FP32 convolution's energies carry ~1e-7 relative noise, below
-        # which the line search cannot see a decrease
+        # the FP32 convolution's energies carry ~1e-7 relative noise: there
+        # the line search also accepts a step by its slope (approximate
+        # Wolfe) when E is within 1e-6 |E| of the current value, so E may
+        # rise by that much; the FP64 forms descend monotonically
+        band = 1e-6 if prec == "f32" else 1e-12
+        assert np.all(np.diff(trace[:, 0]) <= band * np.abs(trace[:, 0]).max()), prec
         assert trace[-1, 4] <= (1e-2 if prec == "f32" else 1e-3) * trace[0, 4], prec
         assert torch.isfinite(xi).all()
         final[prec] = trace[-1]
