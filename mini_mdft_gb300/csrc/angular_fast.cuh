@@ -47,18 +47,42 @@ struct Shape {
   }
 };
 
+// Double-float at mmax >= 4: the per-(point, theta) DFT stages would keep a
+// whole (phi, psi) row of complex double-float values in registers (up to
+// 255 per thread, one CTA per SM); they are split instead into a psi stage
+// and a phi stage, one thread per row or column, passing the values through
+// shared memory in place.  Every output is formed by the same operations in
+// the same order, so results do not change.  These kernels run one CTA of
+// 512 threads per SM over twice the points of a 256-thread CTA: the stages'
+// work items (a few hundred per tile) then fill the threads' rounds.
+template <typename C, int MMAX>
+constexpr bool split_dft() {
+  return std::is_same<C, DF>::value && MMAX >= 4;
+}
 // threads per CTA of both kernels (the launches and the staging loops)
-constexpr int A2P_THREADS = 256;
+template <typename C, int MMAX>
+constexpr int ang_threads() {
+  return split_dft<C, MMAX>() ? 512 : 256;
+}
+// CTAs per SM the kernels are compiled for (launch bounds): 128 registers a
+// thread for FP32 (two 256-thread CTAs) and for the split stages (one
+// 512-thread CTA); the other double-float and FP64 kernels take what they need
+template <typename C, int MMAX>
+constexpr int ang_min_blocks() {
+  return sizeof(C) == 4 ? 2 : 1;
+}
 
-// points per CTA: keep the CTA's shared memory near 100 KB
+// points per CTA: keep the CTA's shared memory near 100 KB (two CTAs per SM),
+// or 200 KB for the one 512-thread CTA of the split stages
 template <typename C, int MMAX, int MRSO>
 constexpr int pts_per_cta() {
   using Sh = Shape<MMAX, MRSO>;
+  const long long budget = split_dft<C, MMAX>() ? 200 * 1024 : 104 * 1024;
   int pts = 128;
   while (pts > 16) {
     const long long bytes = (long long)pts * Sh::LDO * sizeof(C) +
                             (long long)Sh::NT * (Sh::K + 1) * Sh::NPHI * pts * sizeof(Cx<C>);
-    if (bytes <= 104 * 1024) break;
+    if (bytes <= budget) break;
     pts /= 2;
   }
   return pts;
@@ -86,25 +110,9 @@ __device__ __forceinline__ Cx<C> ldtw(const void* t, int i) {
   return static_cast<const Cx<C>*>(t)[i];
 }
 
-// Double-float at mmax >= 4: the per-(point, theta) DFT stages would keep a
-// whole (phi, psi) row of complex double-float values in registers (up to
-// 255 per thread, one CTA per SM); they are split instead into a psi stage
-// and a phi stage, one thread per row or column, passing the values through
-// shared memory in place.  Every output is formed by the same operations in
-// the same order, so results do not change.
-template <typename C, int MMAX>
-constexpr bool split_dft() {
-  return std::is_same<C, DF>::value && MMAX >= 4;
-}
-// CTAs per SM the kernels are compiled for (launch bounds): FP32 and the
-// split stages keep within 128 registers so that two CTAs share an SM
-template <typename C, int MMAX>
-constexpr int ang_min_blocks() {
-  return (sizeof(C) == 4 || split_dft<C, MMAX>()) ? 2 : 1;
-}
 
 template <typename S, typename C, int MMAX, int MRSO, bool FROM_XI>
-__global__ void __launch_bounds__(A2P_THREADS, (ang_min_blocks<C, MMAX>()))
+__global__ void __launch_bounds__((ang_threads<C, MMAX>()), (ang_min_blocks<C, MMAX>()))
 angl2proj_fast_kernel(const AngPlan P, const S* __restrict__ o, Cx<S>* __restrict__ p, C rho0) {
   using Sh = Shape<MMAX, MRSO>;
   constexpr int PTS = pts_per_cta<C, MMAX, MRSO>();
@@ -126,18 +134,19 @@ angl2proj_fast_kernel(const AngPlan P, const S* __restrict__ o, Cx<S>* __restric
   // a thread's loads are issued before the first shared store, so the tile
   // costs one memory round trip instead of one per element
   {
-    constexpr int IT = (PTS * NO + A2P_THREADS - 1) / A2P_THREADS;
+    constexpr int NTH = ang_threads<C, MMAX>();
+    constexpr int IT = (PTS * NO + NTH - 1) / NTH;
     const S* src = o + pt0 * NO;
     const int n = cnt * NO;
     S v[IT];
 #pragma unroll
     for (int r = 0; r < IT; ++r) {
-      const int i = tid + r * A2P_THREADS;
+      const int i = tid + r * NTH;
       if (i < n) v[r] = src[i];
     }
 #pragma unroll
     for (int r = 0; r < IT; ++r) {
-      const int i = tid + r * A2P_THREADS;
+      const int i = tid + r * NTH;
       if (i < n) {
         const int q = i / NO, j = i - q * NO;
         ot[q * LDO + j] = FROM_XI ? rho0 * to_compute<C>(xi_sq_minus_one(v[r])) : to_compute<C>(v[r]);
@@ -341,7 +350,7 @@ angl2proj_fast_kernel(const AngPlan P, const S* __restrict__ o, Cx<S>* __restric
 }
 
 template <typename S, typename C, int MMAX, int MRSO>
-__global__ void __launch_bounds__(A2P_THREADS, (ang_min_blocks<C, MMAX>()))
+__global__ void __launch_bounds__((ang_threads<C, MMAX>()), (ang_min_blocks<C, MMAX>()))
 proj2angl_fast_kernel(const AngPlan P, const Cx<S>* __restrict__ p, S* __restrict__ o) {
   using Sh = Shape<MMAX, MRSO>;
   constexpr int PTS = pts_per_cta<C, MMAX, MRSO>();
@@ -357,17 +366,18 @@ proj2angl_fast_kernel(const AngPlan P, const Cx<S>* __restrict__ p, S* __restric
 
   // stage p(ip, pt0 .. pt0 + cnt) as Ps[ip][point], loads batched as above
   {
-    constexpr int IT = (NP * PTS + A2P_THREADS - 1) / A2P_THREADS;
+    constexpr int NTH = ang_threads<C, MMAX>();
+    constexpr int IT = (NP * PTS + NTH - 1) / NTH;
     Cx<S> v[IT];
 #pragma unroll
     for (int r = 0; r < IT; ++r) {
-      const int w = tid + r * A2P_THREADS;
+      const int w = tid + r * NTH;
       const int ip = w / PTS, q = w - ip * PTS;
       if (w < NP * PTS && q < cnt) v[r] = p[(long long)ip * P.N + pt0 + q];
     }
 #pragma unroll
     for (int r = 0; r < IT; ++r) {
-      const int w = tid + r * A2P_THREADS;
+      const int w = tid + r * NTH;
       const int q = w - (w / PTS) * PTS;
       if (w < NP * PTS && q < cnt) Ps[w] = mkc<C>(to_compute<C>(v[r].re), to_compute<C>(v[r].im));
     }
@@ -607,9 +617,9 @@ void fast_a2p(const AngPlan& P, const S* o, Cx<S>* p, bool from_xi, double rho0,
   const long long nb = (P.N + PTS - 1) / PTS;
   throw_if(nb > 0x7fffffffLL, "grid too large", 4);
   if (from_xi)
-    angl2proj_fast_kernel<S, C, MMAX, MRSO, true><<<(unsigned)nb, A2P_THREADS, sm, s>>>(P, o, p, C(rho0));
+    angl2proj_fast_kernel<S, C, MMAX, MRSO, true><<<(unsigned)nb, ang_threads<C, MMAX>(), sm, s>>>(P, o, p, C(rho0));
   else
-    angl2proj_fast_kernel<S, C, MMAX, MRSO, false><<<(unsigned)nb, A2P_THREADS, sm, s>>>(P, o, p, C(rho0));
+    angl2proj_fast_kernel<S, C, MMAX, MRSO, false><<<(unsigned)nb, ang_threads<C, MMAX>(), sm, s>>>(P, o, p, C(rho0));
 }
 
 template <typename S, typename C, int MMAX, int MRSO>
@@ -620,7 +630,7 @@ void fast_p2a(const AngPlan& P, const Cx<S>* p, S* o, cudaStream_t s) {
                          (size_t)Sh::NP * PTS * sizeof(Cx<C>);
   const long long nb = (P.N + PTS - 1) / PTS;
   throw_if(nb > 0x7fffffffLL, "grid too large", 4);
-  proj2angl_fast_kernel<S, C, MMAX, MRSO><<<(unsigned)nb, A2P_THREADS, sm2, s>>>(P, p, o);
+  proj2angl_fast_kernel<S, C, MMAX, MRSO><<<(unsigned)nb, ang_threads<C, MMAX>(), sm2, s>>>(P, p, o);
 }
 
 }  // namespace
