@@ -166,15 +166,11 @@ __device__ void grid_reduce(Red<K> r, double* __restrict__ part, unsigned* __res
   }
 }
 
-// Sums of per-thread double-float values combined on the FP32 pipes: warps
-// by shuffles, warp 0 over the CTA's warps, one partial (K pairs) per CTA,
-// and in the last CTA to finish every thread over the partials, then the
-// warps again, in a fixed order.  The L-BFGS dot products are double-float
-// Dot2 sums per thread, so double-float combining keeps their precision;
-// combining them as double-doubles (grid_reduce) spends tens of
-// microseconds per launch on the narrow FP64 pipe.  part: >= K float pairs
-// per CTA (the (gridDim.x, 2K + 1) doubles of grid_reduce hold them);
-// counter: zero on entry, left zero.  fin gets the K sums as doubles.
+// Warp sums of per-thread double-float values on the FP32 pipes (shuffles
+// in a fixed order): the L-BFGS dot products are double-float Dot2 sums per
+// thread, so double-float combining keeps their precision, where combining
+// them as double-doubles would spend tens of microseconds per launch on the
+// narrow FP64 pipe.
 template <int K>
 __device__ __forceinline__ void df_warp_sum(DF (&v)[K]) {
 #pragma unroll
@@ -183,72 +179,9 @@ __device__ __forceinline__ void df_warp_sum(DF (&v)[K]) {
     for (int k = 0; k < K; ++k)
       v[k] = v[k] + DF(__shfl_down_sync(0xffffffffu, v[k].hi, off), __shfl_down_sync(0xffffffffu, v[k].lo, off));
 }
-template <int K, typename Fin>
-__device__ void grid_reduce_df(DF (&v)[K], double* __restrict__ part, unsigned* __restrict__ counter, Fin fin) {
-  __shared__ float2 sh[K][kRedThreads / 32];
-  __shared__ bool last;
-  float2* pf = reinterpret_cast<float2*>(part);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x / 32;
-  df_warp_sum<K>(v);
-  if (lane == 0) {
-#pragma unroll
-    for (int k = 0; k < K; ++k) sh[k][wid] = make_float2(v[k].hi, v[k].lo);
-  }
-  __syncthreads();
-  if (wid == 0) {
-    DF t[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const float2 q = lane < nw ? sh[k][lane] : make_float2(0.f, 0.f);
-      t[k] = DF(q.x, q.y);
-    }
-    df_warp_sum<K>(t);
-    if (lane == 0) {
-#pragma unroll
-      for (int k = 0; k < K; ++k) pf[(size_t)blockIdx.x * K + k] = make_float2(t[k].hi, t[k].lo);
-      __threadfence();
-      last = atomicAdd(counter, 1u) == gridDim.x - 1;
-    }
-  }
-  __syncthreads();  // also ends warp 0's reads of sh
-  if (!last) return;
-  __threadfence();
-  DF t[K];
-#pragma unroll
-  for (int k = 0; k < K; ++k) t[k] = DF(0.f, 0.f);
-  for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const float2 q = __ldcg(&pf[(size_t)b * K + k]);
-      t[k] = t[k] + DF(q.x, q.y);
-    }
-  }
-  df_warp_sum<K>(t);
-  if (lane == 0) {
-#pragma unroll
-    for (int k = 0; k < K; ++k) sh[k][wid] = make_float2(t[k].hi, t[k].lo);
-  }
-  __syncthreads();
-  if (wid == 0) {
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const float2 q = lane < nw ? sh[k][lane] : make_float2(0.f, 0.f);
-      t[k] = DF(q.x, q.y);
-    }
-    df_warp_sum<K>(t);
-    if (lane == 0) {
-      double r[K];
-#pragma unroll
-      for (int k = 0; k < K; ++k) r[k] = df_to_double(t[k]);
-      fin(r);
-      *counter = 0u;
-    }
-  }
-}
 
-// grid of a streaming reduction: at most `cap` CTAs (8 per SM for the
-// memory-bound passes, so that enough loads are in flight; 4 for the energy
-// kernel, whose registers allow 4)
+// grid of a streaming reduction: at most `cap` CTAs (the energy kernel
+// passes 4 per SM, the CTAs its registers allow)
 unsigned red_blocks(long long n, int cap = kRedBlocks) {
   const long long b = (n + kRedThreads - 1) / kRedThreads;
   return (unsigned)std::max(1LL, std::min<long long>(b, cap));
