@@ -13,9 +13,9 @@
 //     the group advances all its active jobs (compacted into the first k
 //     slots) with one set of batched launches per step;
 //   * each group step is replayed from a CUDA graph captured for its active
-//     count k; the graphs of every k are captured when the group is made (a
-//     count whose capture fails runs directly, and is captured again after
-//     its first direct step);
+//     count k; the graphs of k = 1..16 are captured when the group is made
+//     (a count whose capture fails, or a larger one, runs directly once and
+//     is captured after that first direct step);
 //   * a group is created only while the device memory of all groups stays
 //     within the server's budget; groups without jobs are released, least
 //     recently used first, when a new one does not fit;
@@ -511,11 +511,13 @@ void mdft_server_s::enqueue_step(Group& g, int k) {
   mdft::launch_check("server descent kernel launch");
 }
 
-// Captures the step graph of every active count 1..B of a new group, so that
-// no capture or instantiation lands in a running job's step; a count whose
-// capture fails runs directly (first step) and is tried again in step().
+// Captures the step graphs of the active counts 1..min(B, kPrecapture) of a
+// new group, so that no capture or instantiation lands in a running job's
+// step; a count whose capture fails, or a larger one, runs directly at its
+// first step and is captured at its second (step()).
+constexpr int kPrecapture = 16;
 void mdft_server_s::precapture(Group& g) {
-  for (int k = 1; k <= g.B; ++k) {
+  for (int k = 1; k <= std::min(g.B, kPrecapture); ++k) {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     bool ok = cudaStreamBeginCapture(g.stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
