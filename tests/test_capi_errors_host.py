@@ -52,6 +52,11 @@ def test_noalloc_rejects_grids_beyond_the_fixed_scratch_before_touching_the_gpu(
     assert "NULL argument" in _err(L)
 
 
+def test_scratch_pool_argument_check(L):
+    assert L.mdft_scratch_pool(None) == 1
+    assert "NULL argument" in _err(L)
+
+
 def test_vext_argument_checks(L):
     g = C.c_void_p()
     assert L.mdft_grid_create(C.byref(g), 4, 4, 4, 10.0, 10.0, 10.0, 3, 2) == 0
