@@ -430,26 +430,65 @@ __global__ void __launch_bounds__(kRedThreads, 4) eg_kernel(const EgArgs A) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   int o = (int)(i % A.no);
   const int ostep = (int)(stride % A.no);
-  // the next element's loads are issued before this element's arithmetic,
-  // so that each thread keeps a load of every input in flight meanwhile
-  double xn = 0.0, ven = 0.0;
-  TV vn = TV(0);
-  if (i < A.n) {
-    xn = xi[i];
-    vn = vx[i];
-    ven = vext ? vext[i] : 0.0;
-  }
   for (; i < A.n; i += stride) {
-    const double x = xn, ve = ven;
-    const TV vv = vn;
-    if (i + stride < A.n) {
-      xn = xi[i + stride];
-      vn = vx[i + stride];
-      ven = vext ? vext[i + stride] : 0.0;
-    }
+    const double x = xi[i], ve = vext ? vext[i] : 0.0;
+    const TV vv = vx[i];
     const unsigned ebits = (unsigned)(bits_of(x) >> 52) & 0x7ffu;
     double gi;
-    if (ebits - 1003u <= 40u) {  // 2^-20 <= |x| < 2^21
+    if constexpr (std::is_same<TV, float>::value) {
+      // the mixed form: FP32 arithmetic per element (its vexc is FP32), the
+      // sums still Dot2 double-float accumulators; 2^-120 <= |x| < 2^60
+      if (ebits - 903u < 180u) {
+        const float2 w2 = wf[o];
+        const float xf = df_from_double_bits(x).hi;                     // nearest float
+        const float tf = df_from_double_bits(fma(x, x, -1.0)).hi;       // xi^2 - 1, no cancellation
+        const float vef = df_from_double_bits(ve).hi, xsq = xf * xf;
+        float L, fid;  // ln xi^2 and (1 + t) ln(1 + t) - t
+        if (tf > -0.5f && tf < 1.f) {
+          // f = 2 s^2 Q(s) / (1 - s), s = t / (2 + t), Q = 1 + s/3 + s^2/3
+          // + s^3/5 + s^4/5 + ... (from ln(1 + t) = 2 atanh s): no
+          // cancellation near xi = 1; |s| < 1/3, the terms to s^14 leave a
+          // truncation below 4e-9 of f
+          L = log1pf(tf);
+          const float sv = __fdividef(tf, 2.f + tf);
+          float Q = 1.f / 15.f;
+          Q = fmaf(Q, sv, 1.f / 15.f);
+          Q = fmaf(Q, sv, 1.f / 13.f);
+          Q = fmaf(Q, sv, 1.f / 13.f);
+          Q = fmaf(Q, sv, 1.f / 11.f);
+          Q = fmaf(Q, sv, 1.f / 11.f);
+          Q = fmaf(Q, sv, 1.f / 9.f);
+          Q = fmaf(Q, sv, 1.f / 9.f);
+          Q = fmaf(Q, sv, 1.f / 7.f);
+          Q = fmaf(Q, sv, 1.f / 7.f);
+          Q = fmaf(Q, sv, 1.f / 5.f);
+          Q = fmaf(Q, sv, 1.f / 5.f);
+          Q = fmaf(Q, sv, 1.f / 3.f);
+          Q = fmaf(Q, sv, 1.f / 3.f);
+          Q = fmaf(Q, sv, 1.f);
+          fid = __fdividef(2.f * sv * sv * Q, 1.f - sv);
+        } else {
+          L = 2.f * logf(fabsf(xf));
+          fid = fmaf(xsq, L, -tf);
+        }
+        const DF wd(w2.x, w2.y);
+        acc_mac(a_id, wd, DF(fid, 0.f));
+        acc_mac(a_ext, wd, DF(xsq * vef, 0.f));
+        acc_mac(a_exc, wd, DF(vv * tf, 0.f));
+        const float gf = 2.f * xf * w2.x * (A.ch * fmaf(A.kh, L, vef) + A.xh * vv);
+        gi = f2d_bits(gf);
+        if (dir) acc_mac(a_gd, DF(gf, 0.f), DF(dir[i], 0.f));
+        if (hinv) hinv[i] = __fdividef(1.f, w2.x * c2k * fmaxf(L + 2.f + vef * ikT, 1.f));
+      } else {
+        const Terms64 tt = terms_f64(x, ws[o], (double)vv, ve, A);
+        d_id += tt.id;
+        d_ext += tt.ext;
+        d_exc += tt.exc;
+        gi = tt.g;
+        if (hinv) hinv[i] = tt.hinv;
+        if (dir) acc_mac(a_gd, df_from_double_bits(gi), DF(dir[i], 0.f));
+      }
+    } else if (ebits - 1003u <= 40u) {  // 2^-20 <= |x| < 2^21
       const LnSq q = df_ln_sq(x, A);
       const float2 w2 = wf[o];
       const DF wd(w2.x, w2.y), vd = eg_df(vv), ved = df_from_double_bits(ve);

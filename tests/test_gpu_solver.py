@@ -87,7 +87,8 @@ def test_energy_over_the_whole_xi_range(gpu_lib, prec):
     """The ideal and external terms for xi from 1e-30 to 1e8 (both signs,
     0, +-1, the sqrt 2 and 2^+-20 boundaries of the double-float logarithm),
     element by element: |g - g_oracle| within 1e-12 of the sizes of the
-    gradient's terms before they cancel."""
+    gradient's terms before they cancel; the mixed form computes them in
+    FP32 (sums in double-float), within 2e-6."""
     import torch
     M = gpu_lib
     n, box, mmax, mrso = (6, 6, 6), (9., 9., 9.), 2, 2
@@ -113,13 +114,14 @@ def test_energy_over_the_whole_xi_range(gpu_lib, prec):
     grad = torch.empty((N, no), dtype=torch.float64, device="cuda")
     t = solver.energy(torch.from_numpy(xi).cuda(), grad)
     scale = max(abs(t_o[1]), abs(t_o[2]))
+    tol = 2e-6 if prec == "f32" else 1e-12
     for k, name in enumerate(M.Solver.TERMS[:3]):
-        assert abs(t[name] - t_o[k]) <= 1e-12 * scale, name
+        assert abs(t[name] - t_o[k]) <= tol * scale, name
     x2 = xi * xi
     lx = np.where(x2 > 0, np.log(np.where(x2 > 0, x2, 1.0)), 0.0)
     size = 2 * np.abs(xi) * w[None, :] * rho0 * dv * (kT * np.abs(lx) + np.abs(vext))
     err = np.abs(grad.cpu().numpy() - g_o)
-    assert np.all(err <= 1e-12 * size + 1e-300), float((err / np.maximum(size, 1e-300)).max())
+    assert np.all(err <= tol * size + 1e-300), float((err / np.maximum(size, 1e-300)).max())
 
 
 def test_minimizer_reaches_boltzmann_density_without_excess(gpu_lib):
